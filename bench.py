@@ -1,0 +1,374 @@
+#!/usr/bin/env python
+"""Throughput of the pp.neighbors graph build on GB300.
+
+Workload (default): 1,000,000 cells x 50 dims f32, k = 15 non-self
+neighbours, a seeded 200-cluster Gaussian mixture with 1% exact duplicates
+(synthetic stand-in for a PCA embedding).  One step = kNN (exact, FP64-equal
+neighbour lists) + the distances rows + UMAP connectivities CSR, on inputs
+already resident in HBM.  `value` is cells/s over all ranks.  `e2e` is the
+same through the host-pointer C-ABI call, with the embedding uploaded from
+pinned memory and the kNN rows and connectivities CSR read back every step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--form plain|tensor]
+    python bench.py --impl reference      # the reference CPU path (restated)
+
+For N > 1 launch with torch.distributed.run; every rank builds its own
+replica graph (no data-path collective), so scaling is weak.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = {"name": "knn_graph_1M_x50_k15", "n": 1_000_000, "d": 50, "k": 15, "clusters": 200,
+            "dup_frac": 0.01, "seed": 0}
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--form", choices=["plain", "tensor"], default=None)
+    p.add_argument("--n", type=int, default=WORKLOAD["n"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-recall", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    return p.parse_args()
+
+
+def peaks():
+    try:
+        return json.loads(PEAKS_FILE.read_text()), "measured"
+    except Exception:
+        return FALLBACK_PEAKS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_data(n: int, seed: int):
+    from mrustsc_gb300 import synthetic
+
+    return synthetic.mixture(n, WORKLOAD["d"], clusters=WORKLOAD["clusters"], dup_frac=WORKLOAD["dup_frac"],
+                             seed=seed)
+
+
+# --------------------------------------------------------------------------- reference arm
+
+def cpu_reference_step(x: np.ndarray, k: int, rows: np.ndarray):
+    """The restated reference CPU path on a bounded sample: kNN of `rows` against all
+    cells (neighbors.rs:35-101) and the connectivities of that sample's graph."""
+    from oracle import oracle
+
+    idx, dist = oracle.knn_reference_cpu_rows(x, k, rows)
+    sub = (idx % len(rows)).astype(np.uint32)
+    oracle.connectivities(sub, dist)
+
+
+def calibrate_rows(x, k, seconds: float, cap: int = 50_000) -> tuple[np.ndarray, float]:
+    rng = np.random.default_rng(123)
+    probe = np.sort(rng.choice(len(x), 64, replace=False))
+    t0 = time.perf_counter()
+    cpu_reference_step(x, k, probe)
+    per_row = (time.perf_counter() - t0) / len(probe)
+    nrows = int(max(64, min(cap, len(x), seconds / max(per_row, 1e-9))))
+    rows = np.sort(rng.choice(len(x), nrows, replace=False))
+    return rows, per_row
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import oracle
+
+    oracle.build()
+    n, k = args.n, WORKLOAD["k"]
+    x = make_data(n, WORKLOAD["seed"])
+    step_seconds = min(10.0, max(2.0, 150.0 / max(1, args.steps + args.warmup)))
+    rows, _ = calibrate_rows(x, k, step_seconds)
+    for _ in range(args.warmup):
+        cpu_reference_step(x, k, rows)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        cpu_reference_step(x, k, rows)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * statistics.mean(times)
+    value = len(rows) / (ms / 1e3)
+    cores = oracle.num_threads()
+    sample = (f"{len(rows)} query cells against all {n} (kNN + connectivities of the sample graph) "
+              f"per step, restated reference CPU path (no Rust toolchain: port of neighbors.rs), {cores} threads")
+    line = {"metric": "kNN-graph cells/s", "value": value, "unit": "cells/s", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD["name"], "n_cells": n, "dims": WORKLOAD["d"], "k": k},
+            "cpu_baseline": {"value": value, "unit": "cells/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------------- our arm
+
+def fp64_recall(torch, xd, idx_dev, k: int, nrows: int = 256, seed: int = 5):
+    """Exact-row fraction and recall against an FP64 reference computed here with torch
+    (expansion to shortlist, difference form to rank, lowest index on ties)."""
+    n = xd.shape[0]
+    g = np.random.default_rng(seed)
+    rows = torch.as_tensor(np.sort(g.choice(n, nrows, replace=False)), device=xd.device)
+    X = xd.double()
+    A = X[rows]
+    nx = (X * X).sum(1)
+    exact, hit = 0, 0
+    for c0 in range(0, nrows, 32):
+        r = rows[c0:c0 + 32]
+        Ab = A[c0:c0 + 32]
+        d2 = (Ab * Ab).sum(1, keepdim=True) + nx[None, :] - 2.0 * Ab @ X.T
+        d2[torch.arange(len(r), device=xd.device), r] = float("inf")
+        cand = torch.topk(d2, k + 32, largest=False).indices
+        diff = X[cand] - Ab[:, None, :]
+        dd = (diff * diff).sum(-1)
+        dd = torch.where(cand == r[:, None], torch.full_like(dd, float("inf")), dd)
+        order = torch.argsort(cand, dim=1)
+        cand = torch.gather(cand, 1, order)
+        dd = torch.gather(dd, 1, order)
+        o2 = torch.argsort(dd, dim=1, stable=True)
+        truth = torch.gather(cand, 1, o2)[:, :k]
+        ours = idx_dev[r].long()
+        exact += int((truth == ours).all(1).sum())
+        for t_row, o_row in zip(truth.cpu().numpy(), ours.cpu().numpy()):
+            hit += len(set(t_row.tolist()) & set(o_row.tolist()))
+    return exact / nrows, hit / (nrows * k)
+
+
+def run_ours(args):
+    import torch
+
+    from mrustsc_gb300 import _lib, build
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    build.build()
+    L = _lib.lib()
+    form = args.form or ("tensor" if getattr(_lib, "TENSOR_FORM_READY", False) else "plain")
+    n, d, k = args.n, WORKLOAD["d"], WORKLOAD["k"]
+    x = make_data(n, WORKLOAD["seed"] + rank)
+    ctx = _lib.context(local)
+    stream = torch.cuda.ExternalStream(L.scrust_cuda_context_stream(ctx))
+    xd = torch.from_numpy(x).to(f"cuda:{local}")
+    idx = torch.empty((n, k), dtype=torch.int32, device=xd.device)
+    dst = torch.empty((n, k), dtype=torch.float32, device=xd.device)
+    opts = _lib.options(form=form)
+    st = _lib.Status()
+    csr = ctypes.c_void_p()
+
+    def step():
+        rc = L.scrust_cuda_neighbors_graph_device(ctx, xd.data_ptr(), n, d, k, ctypes.byref(opts), idx.data_ptr(),
+                                                  dst.data_ptr(), ctypes.byref(csr), ctypes.byref(st))
+        _lib.check(rc, st)
+        L.scrust_csr_free(csr)
+
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        step()
+    _lib.check(L.scrust_cuda_synchronize(ctx, ctypes.byref(st)), st)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+
+    # Timed region: K steps, events on the library's stream; phase events on.
+    L.scrust_cuda_set_timing(ctx, 1)
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = L.scrust_cuda_launch_count(ctx)
+    phases = []
+    buf = (ctypes.c_float * 4)()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    total_ms = 0.0
+    for _ in range(args.steps):
+        start.record(stream)
+        step()
+        end.record(stream)
+        end.synchronize()
+        total_ms += start.elapsed_time(end)
+        got = L.scrust_cuda_phase_times(ctx, buf, 4)
+        phases.append([buf[i] for i in range(got)])
+    torch.cuda.synchronize()
+    launches = int(L.scrust_cuda_launch_count(ctx) - launches0)
+    clk = clocks.stop()
+    L.scrust_cuda_set_timing(ctx, 0)
+    _lib.check(L.scrust_cuda_synchronize(ctx, ctypes.byref(st)), st)
+    ms_step = total_ms / args.steps
+    if world > 1:
+        t = torch.tensor([ms_step], device=xd.device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+        torch.distributed.barrier()
+    value = world * n / (ms_step / 1e3)
+
+    ph = np.array(phases) if phases and len(phases[0]) == 4 else np.zeros((1, 4))
+    ph_mean = ph.mean(0)
+    cand_ms = float(ph_mean[1])
+    pk, pk_kind = peaks()
+    flops = 2.0 * n * n * d
+    if form == "tensor":
+        achieved = flops / (cand_ms / 1e3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": achieved / pk["bf16_tflops"], "traffic": None,
+                "kernel": "knn_candidates_tc", "peak_source": pk_kind}
+    else:
+        sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+        fp32_peak = sm_count * 128 * 2 * float(pk.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+        achieved = flops / (cand_ms / 1e3) / 1e12
+        roof = {"bound": "fp32_cuda_core", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak, "traffic": None, "kernel": "plain_candidates_kernel",
+                "peak_source": f"{sm_count} SMs x 128 FP32 lanes x 2 x {pk.get('sm_max_mhz', 2070.0)} MHz"}
+
+    line = {"metric": "kNN-graph cells/s", "value": value, "unit": "cells/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if form == "plain" else "f16",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD["name"], "n_cells": n, "dims": d, "k": k,
+                       "clusters": WORKLOAD["clusters"], "dup_frac": WORKLOAD["dup_frac"], "form": form,
+                       "mode": "exact", "parallelism": f"replicas{world}",
+                       "l2": "inputs larger than L2 (200 MB embedding, >1 GB candidate lists per step)"},
+            "phases_ms": {"prep": float(ph_mean[0]), "candidates": float(ph_mean[1]),
+                          "rerank": float(ph_mean[2]), "connectivities": float(ph_mean[3])},
+            "gpu_launches": launches, "roofline": roof, "clocks": clk}
+
+    if rank == 0 and not args.no_recall:
+        ex, rec = fp64_recall(torch, xd, idx, k)
+        line["recall_fp64_sample"] = {"rows": 256, "exact_rows": ex, "recall": rec}
+        if form == "tensor":
+            idx_t = idx.clone()
+            opts_p = _lib.options(form="plain")
+            rc = L.scrust_cuda_knn_device(ctx, xd.data_ptr(), n, d, k, ctypes.byref(opts_p), idx.data_ptr(),
+                                          dst.data_ptr(), ctypes.byref(st))
+            _lib.check(rc, st)
+            torch.cuda.synchronize()
+            line["recall_vs_plain"] = float((idx_t == idx).all(1).float().mean().item())
+
+    if rank == 0 and not args.no_e2e:
+        xh = torch.from_numpy(x).pin_memory()
+        ih = np.empty((n, k), np.uint32)
+        dh = np.empty((n, k), np.float32)
+        e2e_steps = max(1, min(args.steps, 3))
+        nnz = 0
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            out = ctypes.c_void_p()
+            rc = L.scrust_cuda_neighbors_graph(ctx, xh.data_ptr(), n, d, k, ctypes.byref(opts), ih.ctypes.data,
+                                               dh.ctypes.data, ctypes.byref(out), ctypes.byref(st))
+            _lib.check(rc, st)
+            nnz = int(L.scrust_csr_nnz(out))
+            L.scrust_csr_free(out)
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        line["e2e"] = {"value": n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": n * d * 4,
+                       "d2h_bytes_per_step": n * k * 8 + (n + 1) * 4 + nnz * 8, "ms_per_step": e2e_s * 1e3}
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle
+
+        oracle.build()
+        rows, _ = calibrate_rows(x, k, args.cpu_seconds)
+        t0 = time.perf_counter()
+        cpu_reference_step(x, k, rows)
+        secs = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": len(rows) / secs, "unit": "cells/s", "cores": oracle.num_threads(),
+                                "kind": "port",
+                                "sample": f"{len(rows)} query cells against all {n}, restated reference CPU path "
+                                          f"(kNN + sample-graph connectivities), {secs:.1f} s"}
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,201 @@
+/*
+ * scrust_cuda.h -- C ABI of the GB300 (sm_103a) backend for scrust's
+ * `pp.neighbors` path: exact k-nearest neighbours on an embedding and the UMAP
+ * fuzzy-simplicial-set connectivities.
+ *
+ * Plain pointers and sizes only.  Every entry point returns a scrust_code and,
+ * when `status` is non-NULL, fills it with the same code and a message.  No
+ * entry point aborts the process.  Host-pointer entry points block until their
+ * results are in host memory; *_device entry points enqueue on the context's
+ * stream and return without synchronising.
+ *
+ * Reference interfaces replaced (paths inside the scrust repository):
+ *   scrust_cuda_knn                  scrust_core::neighbors::knn
+ *                                    crates/scrust-core/src/neighbors.rs:29
+ *                                    and scrust_gpu::kernels::knn::knn_metal
+ *                                    crates/scrust-gpu/src/kernels/knn.rs:36
+ *   scrust_cuda_connectivities       scrust_core::neighbors::connectivities
+ *                                    crates/scrust-core/src/neighbors.rs:208
+ *   scrust_cuda_smooth_knn_distances scrust_core::neighbors::smooth_knn_distances
+ *                                    crates/scrust-core/src/neighbors.rs:239
+ *   scrust_cuda_context_create/destroy  scrust_gpu::MetalContext::new / Drop
+ *                                    crates/scrust-gpu/src/context.rs:12-91
+ *   scrust_cuda_max_supported_k      scrust_gpu::kernels::knn::max_supported_k
+ *                                    crates/scrust-gpu/src/kernels/knn.rs:27
+ *   scrust_cuda_gpu_available        scrust_core::device::gpu_available
+ *                                    crates/scrust-core/src/device.rs:39
+ *   scrust_csr_*                     scrust_core::sparse::CsrMatrix accessors
+ *                                    crates/scrust-core/src/sparse.rs:10-90
+ *   scrust_cuda_neighbors_graph      the two FFI calls of python/scrust/pp/_basics.py:198,209
+ *                                    fused into one device pass
+ * Entry points with no reference counterpart (new semantics, parity against
+ * the FP64 oracle only): scrust_cuda_knn_batched (many samples in one launch)
+ * and the scrust_serve_* query service (queries against a resident atlas).
+ */
+#ifndef SCRUST_CUDA_H
+#define SCRUST_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SCRUST_API __attribute__((visibility("default")))
+#else
+#define SCRUST_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Mirrors scrust_core::Error (crates/scrust-core/src/error.rs:8-33); the
+ * Python layer maps SHAPE and INVALID_PARAMETER to ValueError and the rest
+ * to RuntimeError, as crates/scrust-py/src/lib.rs:26-35 does. */
+typedef enum scrust_code {
+    SCRUST_OK = 0,
+    SCRUST_SHAPE = 1,             /* Error::Shape */
+    SCRUST_INVALID_PARAMETER = 2, /* Error::InvalidParameter */
+    SCRUST_NO_GPU = 3,            /* Error::NoGpu */
+    SCRUST_KERNEL = 4,            /* Error::Kernel */
+    SCRUST_NOT_CONVERGED = 5,     /* Error::NotConverged */
+    SCRUST_OOM = 6,               /* device or host allocation failed / over budget */
+    SCRUST_TIMEOUT = 7            /* a bounded device wait ran out */
+} scrust_code;
+
+typedef struct scrust_status {
+    int32_t code;
+    char message[256];
+} scrust_status;
+
+typedef struct scrust_context scrust_context;
+typedef struct scrust_csr scrust_csr;
+
+/* How candidates are generated before the exact rerank. */
+typedef enum scrust_form {
+    SCRUST_FORM_PLAIN = 0,  /* FP32 tiled expansion on CUDA cores (the drop-in) */
+    SCRUST_FORM_TENSOR = 1  /* 16-bit tcgen05/TMEM candidate GEMM, FP32 accumulate */
+} scrust_form;
+
+typedef enum scrust_metric {
+    SCRUST_METRIC_EUCLIDEAN = 0,
+    SCRUST_METRIC_COSINE = 1 /* 1 - a.b/(|a||b|); no reference counterpart */
+} scrust_metric;
+
+typedef enum scrust_mode {
+    /* Neighbour lists equal the FP64 exact kNN with lowest-index tie-break. */
+    SCRUST_MODE_EXACT = 0,
+    /* The reference's GPU semantics: centred coordinates, sequential fused
+     * difference form and the sub-resolution snap of knn.rs:223-240. */
+    SCRUST_MODE_REFERENCE_SNAP = 1
+} scrust_mode;
+
+typedef enum scrust_precision {
+    SCRUST_PRECISION_FP16 = 0, /* 11-bit significand operands (default) */
+    SCRUST_PRECISION_BF16 = 1  /* 8-bit significand operands */
+} scrust_precision;
+
+typedef struct scrust_knn_options {
+    uint32_t struct_size;   /* sizeof(scrust_knn_options) */
+    int32_t form;           /* scrust_form */
+    int32_t metric;         /* scrust_metric */
+    int32_t mode;           /* scrust_mode */
+    int32_t precision;      /* scrust_precision, tensor form only */
+    uint32_t list_capacity; /* candidates kept per row between prunes; 0 = automatic */
+    uint32_t segments;      /* column segments per row tile; 0 = automatic */
+    uint32_t reserved[9];
+} scrust_knn_options;
+
+/* Fills `options` with the defaults: tensor form, Euclidean, exact, FP16. */
+SCRUST_API void scrust_knn_options_default(scrust_knn_options* options);
+
+/* 1 when a CUDA device of compute capability 10.3 is usable, else 0. */
+SCRUST_API int32_t scrust_cuda_gpu_available(void);
+
+/* A per-device context: stream, workspace arena, kernel configuration. */
+SCRUST_API scrust_context* scrust_cuda_context_create(int32_t device, scrust_status* status);
+SCRUST_API void scrust_cuda_context_destroy(scrust_context* context);
+/* The context's CUDA stream as an opaque pointer (a cudaStream_t). */
+SCRUST_API void* scrust_cuda_context_stream(scrust_context* context);
+/* Largest k the kernels serve; 0 for a NULL context. */
+SCRUST_API uint32_t scrust_cuda_max_supported_k(const scrust_context* context);
+
+/* Exact k nearest neighbours of every row of `embedding` (n x d, row-major
+ * f32), self excluded, nearest first, ties to the smaller id.  Outputs are
+ * caller-allocated n x k arrays.  Host pointers.  Errors mirror
+ * neighbors.rs:41-57: n == 0 or d == 0 -> SHAPE; k == 0 or k >= n ->
+ * INVALID_PARAMETER; k > scrust_cuda_max_supported_k -> INVALID_PARAMETER. */
+SCRUST_API int32_t scrust_cuda_knn(scrust_context* context, const float* embedding, uint64_t n, uint64_t d,
+                        uint32_t k, const scrust_knn_options* options, uint32_t* out_indices,
+                        float* out_distances, scrust_status* status);
+
+/* The same with device pointers, enqueued on the context stream. */
+SCRUST_API int32_t scrust_cuda_knn_device(scrust_context* context, const float* embedding, uint64_t n,
+                               uint64_t d, uint32_t k, const scrust_knn_options* options,
+                               uint32_t* out_indices, float* out_distances,
+                               scrust_status* status);
+
+/* UMAP connectivities of a kNN graph (n x k ids and distances, host
+ * pointers).  On success *out is a host-resident CSR (sorted columns, empty
+ * diagonal, values in (0, 1]) owned by the caller: free it with
+ * scrust_csr_free.  Errors mirror neighbors.rs:209-227. */
+SCRUST_API int32_t scrust_cuda_connectivities(scrust_context* context, const uint32_t* indices,
+                                   const float* distances, uint64_t n, uint32_t k,
+                                   scrust_csr** out, scrust_status* status);
+
+/* The same from device-resident inputs; *out is a device-resident CSR. */
+SCRUST_API int32_t scrust_cuda_connectivities_device(scrust_context* context, const uint32_t* indices,
+                                          const float* distances, uint64_t n, uint32_t k,
+                                          scrust_csr** out, scrust_status* status);
+
+/* Per-row sigma and rho of umap's smooth_knn_dist (host pointers). */
+SCRUST_API int32_t scrust_cuda_smooth_knn_distances(scrust_context* context, const float* distances,
+                                         uint64_t n, uint32_t k, float* sigmas, float* rhos,
+                                         scrust_status* status);
+
+/* pp.neighbors in one pass: kNN (out_indices / out_distances, the rows of
+ * obsp["distances"]) and the connectivities CSR.  Host pointers in and out. */
+SCRUST_API int32_t scrust_cuda_neighbors_graph(scrust_context* context, const float* embedding, uint64_t n,
+                                    uint64_t d, uint32_t k, const scrust_knn_options* options,
+                                    uint32_t* out_indices, float* out_distances,
+                                    scrust_csr** connectivities, scrust_status* status);
+
+/* The same with device pointers; the CSR is device-resident. */
+SCRUST_API int32_t scrust_cuda_neighbors_graph_device(scrust_context* context, const float* embedding,
+                                           uint64_t n, uint64_t d, uint32_t k,
+                                           const scrust_knn_options* options,
+                                           uint32_t* out_indices, float* out_distances,
+                                           scrust_csr** connectivities, scrust_status* status);
+
+/* CSR accessors.  Arrays live on the host or the device as the producing call
+ * says (scrust_csr_on_device).  nnz of a device CSR is final once the
+ * context stream has been synchronised (scrust_cuda_synchronize). */
+SCRUST_API uint64_t scrust_csr_n_rows(const scrust_csr* csr);
+SCRUST_API uint64_t scrust_csr_n_cols(const scrust_csr* csr);
+SCRUST_API uint64_t scrust_csr_nnz(const scrust_csr* csr);
+SCRUST_API int32_t scrust_csr_on_device(const scrust_csr* csr);
+SCRUST_API const uint32_t* scrust_csr_indptr(const scrust_csr* csr);
+SCRUST_API const uint32_t* scrust_csr_indices(const scrust_csr* csr);
+SCRUST_API const float* scrust_csr_values(const scrust_csr* csr);
+SCRUST_API void scrust_csr_free(scrust_csr* csr);
+
+/* Blocks until the context stream is idle; reports a pending kernel error. */
+SCRUST_API int32_t scrust_cuda_synchronize(scrust_context* context, scrust_status* status);
+
+/* Phase timing.  When enabled, each kNN / connectivities call records CUDA
+ * events on the context stream around its phases; scrust_cuda_phase_times
+ * writes the last call's milliseconds (after a synchronise) in the order
+ * prep, candidates, rerank, connectivities and returns how many it wrote. */
+SCRUST_API void scrust_cuda_set_timing(scrust_context* context, int32_t enable);
+SCRUST_API int32_t scrust_cuda_phase_times(scrust_context* context, float* ms, int32_t max_phases);
+
+/* Number of kernels this context has launched since it was created. */
+SCRUST_API uint64_t scrust_cuda_launch_count(const scrust_context* context);
+
+/* Library version string. */
+SCRUST_API const char* scrust_cuda_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCRUST_CUDA_H */

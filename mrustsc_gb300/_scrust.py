@@ -1,0 +1,145 @@
+"""Drop-in for the neighbours half of the reference's extension module
+``scrust._scrust`` (crates/scrust-py/src/embedding.rs:60-100, lib.rs:37-40).
+
+Same names, argument meaning, dtypes, return tuples and exceptions:
+
+* ``knn(embedding, k, device) -> (indices u32 (n, k), distances f32 (n, k))``
+* ``connectivities(indices, distances) -> (indptr u32, indices u32, values f32, n_cols)``
+* ``gpu_available() -> bool``
+
+plus ``smooth_knn_distances(distances) -> (sigmas, rhos)`` for the
+per-row bandwidths (crates/scrust-core/src/neighbors.rs:239).
+
+Devices: ``"auto"``, ``"gpu"`` and ``"cuda"`` run the CUDA library.  This
+backend has no CPU implementation: ``"cpu"`` raises ``ValueError`` (the
+reference's own CPU path serves it), and when no sm_103a GPU is present the
+call raises ``RuntimeError`` rather than falling back.  ``"metal"`` raises
+``RuntimeError`` as the reference does on a machine without Metal.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+DEVICES = ("auto", "gpu", "cuda", "cpu", "metal")
+
+
+def gpu_available() -> bool:
+    try:
+        return _lib.gpu_available()
+    except ImportError:
+        return False
+
+
+def _device_index(device: str) -> int:
+    if not isinstance(device, str):
+        raise TypeError(f"device must be a str, got {type(device).__name__}")
+    if device in ("auto", "gpu", "cuda"):
+        return 0
+    if device.startswith("cuda:") and device[5:].isdigit():
+        return int(device[5:])
+    if device == "cpu":
+        raise ValueError(
+            "device 'cpu' is served by the reference's own CPU path; this backend runs on CUDA devices only"
+        )
+    if device == "metal":
+        raise _lib.ScrustError(_lib.NO_GPU, "no Metal device is available on this machine")
+    raise ValueError(f"device must be one of auto, gpu, cuda, cpu, got {device}")
+
+
+def _array2(obj, dtype, name: str) -> np.ndarray:
+    """2-D array of exactly `dtype`; strided views are copied (convert.rs:70-93)."""
+    if not isinstance(obj, np.ndarray) or obj.ndim != 2 or obj.dtype != dtype:
+        raise ValueError(f"{name} must be a 2-D numpy array of {np.dtype(dtype)}")
+    return np.ascontiguousarray(obj)
+
+
+def _k(k) -> int:
+    k = int(k)
+    if k < 0:
+        raise OverflowError("can't convert negative int to unsigned")
+    return k
+
+
+def knn(embedding, k, device, *, metric: str = "euclidean", form: str = "plain", mode: str = "exact",
+        precision: str = "fp16"):
+    """Exact k nearest neighbours, self excluded, nearest first, ties to the smaller id."""
+    x = _array2(embedding, np.float32, "embedding")
+    k = _k(k)
+    dev = _device_index(device)
+    n, d = x.shape
+    L = _lib.lib()
+    st = _lib.Status()
+    opts = _lib.options(form=form, metric=metric, mode=mode, precision=precision)
+    ctx = None
+    # Argument errors are reported before a device is required, as the
+    # reference validates before dispatching (neighbors.rs:41-57).
+    if n and d and k and k < n and k <= 128:
+        ctx = _lib.context(dev)
+    idx = np.empty((n, k), dtype=np.uint32)
+    dist = np.empty((n, k), dtype=np.float32)
+    rc = L.scrust_cuda_knn(ctx, _lib.ptr(x) if x.size else None, n, d, k, ctypes.byref(opts),
+                           _lib.ptr(idx) if idx.size else None, _lib.ptr(dist) if dist.size else None,
+                           ctypes.byref(st))
+    _lib.check(rc, st)
+    return idx, dist
+
+
+def connectivities(indices, distances):
+    """UMAP fuzzy simplicial set of a kNN graph as CSR parts."""
+    idx = _array2(indices, np.uint32, "indices")
+    dist = _array2(distances, np.float32, "distances")
+    if idx.shape != dist.shape:
+        raise _lib.ScrustValueError(_lib.SHAPE, f"expected distances shaped {idx.shape}, got {dist.shape}")
+    n, k = idx.shape
+    L = _lib.lib()
+    st = _lib.Status()
+    ctx = _lib.context(0) if n and k else None
+    out = ctypes.c_void_p()
+    rc = L.scrust_cuda_connectivities(ctx, _lib.ptr(idx) if idx.size else None,
+                                      _lib.ptr(dist) if dist.size else None, n, k, ctypes.byref(out),
+                                      ctypes.byref(st))
+    _lib.check(rc, st)
+    return _lib.csr_host_arrays(out)
+
+
+def smooth_knn_distances(distances):
+    """(sigmas f32 (n,), rhos f32 (n,)) of umap's smooth_knn_dist."""
+    dist = _array2(distances, np.float32, "distances")
+    n, k = dist.shape
+    L = _lib.lib()
+    st = _lib.Status()
+    ctx = _lib.context(0) if n and k else None
+    sig = np.empty(n, dtype=np.float32)
+    rho = np.empty(n, dtype=np.float32)
+    rc = L.scrust_cuda_smooth_knn_distances(ctx, _lib.ptr(dist) if dist.size else None, n, k,
+                                            _lib.ptr(sig) if n else None, _lib.ptr(rho) if n else None,
+                                            ctypes.byref(st))
+    _lib.check(rc, st)
+    return sig, rho
+
+
+def neighbors_graph(embedding, k, device="auto", *, metric: str = "euclidean", form: str = "plain",
+                    mode: str = "exact", precision: str = "fp16"):
+    """kNN and connectivities in one device pass: (indices, distances, (indptr, cols, vals, n))."""
+    x = _array2(embedding, np.float32, "embedding")
+    k = _k(k)
+    dev = _device_index(device)
+    n, d = x.shape
+    L = _lib.lib()
+    st = _lib.Status()
+    opts = _lib.options(form=form, metric=metric, mode=mode, precision=precision)
+    ctx = _lib.context(dev) if (n and d and k and k < n and k <= 128) else None
+    idx = np.empty((n, k), dtype=np.uint32)
+    dist = np.empty((n, k), dtype=np.float32)
+    out = ctypes.c_void_p()
+    rc = L.scrust_cuda_neighbors_graph(ctx, _lib.ptr(x) if x.size else None, n, d, k, ctypes.byref(opts),
+                                       _lib.ptr(idx) if idx.size else None,
+                                       _lib.ptr(dist) if dist.size else None, ctypes.byref(out),
+                                       ctypes.byref(st))
+    _lib.check(rc, st)
+    return idx, dist, _lib.csr_host_arrays(out)

@@ -1,0 +1,710 @@
+// api.cu -- the C ABI (include/scrust_cuda.h): argument checks that mirror
+// the reference, the per-device context and its workspace arena, and the
+// orchestration of prep -> candidates -> exact rerank -> connectivities on
+// the context's stream.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace scrust {
+
+int32_t fail(scrust_status* st, int32_t code, const char* fmt, ...) {
+    if (st) {
+        st->code = code;
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(st->message, sizeof(st->message), fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+int32_t ok(scrust_status* st) {
+    if (st) {
+        st->code = SCRUST_OK;
+        st->message[0] = '\0';
+    }
+    return SCRUST_OK;
+}
+
+int32_t cuda_fail(scrust_status* st, cudaError_t e, const char* what) {
+    const int32_t code = e == cudaErrorMemoryAllocation ? SCRUST_OOM : SCRUST_KERNEL;
+    return fail(st, code, "CUDA kernel %s: %s", what, cudaGetErrorString(e));
+}
+
+void* ws_get(scrust_context* ctx, Slot slot, size_t bytes, cudaError_t* err) {
+    Workspace& ws = ctx->ws;
+    if (bytes == 0) bytes = 16;
+    if (ws.ptr[slot] && ws.bytes[slot] >= bytes) return ws.ptr[slot];
+    // Queued work may still read the old buffer.
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess && ws.ptr[slot]) e = cudaFree(ws.ptr[slot]);
+    ws.ptr[slot] = nullptr;
+    ws.bytes[slot] = 0;
+    if (e == cudaSuccess) {
+        size_t want = bytes + bytes / 8;
+        want = (want + (2u << 20) - 1) & ~(size_t)((2u << 20) - 1);
+        void* p = nullptr;
+        e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) {
+            ws.ptr[slot] = p;
+            ws.bytes[slot] = want;
+        } else {
+            cudaGetLastError();
+        }
+    }
+    if (err) *err = e;
+    return ws.ptr[slot];
+}
+
+bool encode_2d(scrust_context* ctx, CUtensorMap* map, CUtensorMapDataType dtype, void* base,
+               uint64_t inner, uint64_t outer, uint64_t row_bytes, uint32_t box_inner,
+               uint32_t box_outer, CUtensorMapSwizzle swizzle) {
+    if (!ctx->encode_tiled) return false;
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {row_bytes};
+    cuuint32_t box[2] = {box_inner, box_outer};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = ctx->encode_tiled(map, dtype, 2, base, dims, strides, box, estr,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+size_t plain_smem_bytes(int dp);
+
+void mark(scrust_context* ctx, Phase p) {
+    if (!ctx->timing) return;
+    if (!ctx->ev[p] && cudaEventCreate(&ctx->ev[p]) != cudaSuccess) return;
+    if (p == PH_START)
+        for (int i = 0; i < 5; i++) ctx->ev_recorded[i] = false;
+    if (cudaEventRecord(ctx->ev[p], ctx->stream) == cudaSuccess) ctx->ev_recorded[p] = true;
+}
+
+namespace {
+
+constexpr uint32_t kMaxK = 128;
+constexpr int kRerankCapacity = 1024;
+
+int32_t check_knn_args(uint64_t n, uint64_t d, uint32_t k, scrust_status* st) {
+    if (n == 0 || d == 0)
+        return fail(st, SCRUST_SHAPE, "expected a non-empty (cells, dimensions) embedding, got %llu x %llu",
+                    (unsigned long long)n, (unsigned long long)d);
+    if (k == 0) return fail(st, SCRUST_INVALID_PARAMETER, "k must be at least 1, got 0");
+    if ((uint64_t)k >= n)
+        return fail(st, SCRUST_INVALID_PARAMETER,
+                    "k must be smaller than the number of cells, since a cell is not its own neighbour, got %u",
+                    k);
+    if (k > kMaxK)
+        return fail(st, SCRUST_INVALID_PARAMETER, "k must be within the supported maximum of %u, got %u", kMaxK, k);
+    if (n >= 0xffffffffull)
+        return fail(st, SCRUST_SHAPE, "expected fewer than 2^32 - 1 cells, got %llu", (unsigned long long)n);
+    if (d > 65536) return fail(st, SCRUST_SHAPE, "expected at most 65536 dimensions, got %llu", (unsigned long long)d);
+    return SCRUST_OK;
+}
+
+int32_t check_options(const scrust_knn_options* o, scrust_status* st) {
+    if (!o) return SCRUST_OK;
+    if (o->form != SCRUST_FORM_PLAIN && o->form != SCRUST_FORM_TENSOR)
+        return fail(st, SCRUST_INVALID_PARAMETER, "form must be plain or tensor, got %d", o->form);
+    if (o->metric != SCRUST_METRIC_EUCLIDEAN && o->metric != SCRUST_METRIC_COSINE)
+        return fail(st, SCRUST_INVALID_PARAMETER, "metric must be euclidean or cosine, got %d", o->metric);
+    if (o->mode != SCRUST_MODE_EXACT && o->mode != SCRUST_MODE_REFERENCE_SNAP)
+        return fail(st, SCRUST_INVALID_PARAMETER, "mode must be exact or reference_snap, got %d", o->mode);
+    if (o->mode == SCRUST_MODE_REFERENCE_SNAP && o->metric == SCRUST_METRIC_COSINE)
+        return fail(st, SCRUST_INVALID_PARAMETER,
+                    "metric must be euclidean in reference_snap mode (the reference has no cosine), got cosine");
+    if (o->precision != SCRUST_PRECISION_FP16 && o->precision != SCRUST_PRECISION_BF16)
+        return fail(st, SCRUST_INVALID_PARAMETER, "precision must be fp16 or bf16, got %d", o->precision);
+    return SCRUST_OK;
+}
+
+// Maps the device error block to a status, then clears it.
+int32_t collect_device_errors(scrust_context* ctx, scrust_status* st) {
+    int h[DERR_COUNT] = {0};
+    cudaError_t e = cudaMemcpyAsync(h, ctx->d_err, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(st, e, "synchronize");
+    bool any = false;
+    for (int i = 0; i < DERR_COUNT; i++) any |= h[i] != 0;
+    if (!any) return ok(st);
+    cudaMemsetAsync(ctx->d_err, 0, sizeof(int) * DERR_COUNT, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    if (h[DERR_ZERO_ROW])
+        return fail(st, SCRUST_SHAPE, "expected rows with a non-zero norm for the cosine metric, got an all-zero row");
+    if (h[DERR_BAD_INDEX]) return fail(st, SCRUST_SHAPE, "expected neighbour ids below n, got an out-of-range neighbour id");
+    if (h[DERR_TIMEOUT]) return fail(st, SCRUST_TIMEOUT, "CUDA kernel knn: a bounded device wait ran out");
+    if (h[DERR_TIE_OVERFLOW])
+        return fail(st, SCRUST_KERNEL,
+                    "CUDA kernel knn_rerank: more than 4096 cells are equidistant from one cell within f32 resolution");
+    return fail(st, SCRUST_KERNEL, "CUDA kernel knn_rerank: inconsistent candidate set");
+}
+
+struct KnnBuffers {
+    const float* xr = nullptr;   // rows the rerank measures
+    float* xwork = nullptr;
+    double* norm64 = nullptr;
+    float* norm2 = nullptr;
+};
+
+// The kNN solve on device pointers, enqueued on ctx->stream.
+int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint64_t d64, uint32_t k,
+                        const scrust_knn_options* opt, uint32_t* out_idx, float* out_dist,
+                        scrust_status* st) {
+    cudaError_t e = cudaSuccess;
+    scrust_knn_options o;
+    scrust_knn_options_default(&o);
+    if (opt) o = *opt;
+    KnnPlan plan;
+    plan.nq = plan.nr = (int64_t)n64;
+    plan.d = (int)d64;
+    plan.k = (int)k;
+    plan.self = true;
+    plan.form = o.form;
+    plan.metric = o.metric;
+    plan.mode = o.mode;
+    plan.precision = o.precision;
+    const int64_t n = plan.nq;
+    const int d = plan.d;
+    const int64_t n_pad = (n + 127) / 128 * 128;
+    const int dp = d <= 64 ? (d + 3) / 4 * 4 : (d + 63) / 64 * 64;
+    const bool ref = o.mode == SCRUST_MODE_REFERENCE_SNAP;
+    const bool cosine = o.metric == SCRUST_METRIC_COSINE;
+    cudaStream_t s = ctx->stream;
+
+    const float* xwork = x;
+    float* xcentred = nullptr;
+    double* norm64 = nullptr;
+    mark(ctx, PH_START);
+    if (cosine) {
+        float* xn = (float*)ws_get(ctx, SLOT_XWORK, sizeof(float) * (size_t)n * d, &e);
+        norm64 = (double*)ws_get(ctx, SLOT_NORM64, sizeof(double) * (size_t)n, &e);
+        if (!xn || !norm64) return cuda_fail(st, e, "workspace");
+        if ((e = launch_normalise_rows(x, n, d, xn, norm64, ctx->d_err, s)) != cudaSuccess)
+            return cuda_fail(st, e, "normalise");
+        ctx->launches += 1;
+        xwork = xn;
+    } else if (ref) {
+        xcentred = (float*)ws_get(ctx, SLOT_XWORK, sizeof(float) * (size_t)n * d, &e);
+        if (!xcentred) return cuda_fail(st, e, "workspace");
+    }
+    const int mean_blocks = (int)((n + 2047) / 2048);
+    double* means = (double*)ws_get(ctx, SLOT_MEANS, sizeof(double) * ((size_t)d * (mean_blocks + 1)), &e);
+    float* coords_t = (float*)ws_get(ctx, SLOT_COORDS_T, sizeof(float) * (size_t)dp * n_pad, &e);
+    float* norm2 = (float*)ws_get(ctx, SLOT_NORM2, sizeof(float) * (size_t)n_pad, &e);
+    float* cnorm = (float*)ws_get(ctx, SLOT_CNORM, sizeof(float) * (size_t)n_pad, &e);
+    float* margin = (float*)ws_get(ctx, SLOT_MARGIN, sizeof(float) * (size_t)n_pad + 64, &e);
+    if (!means || !coords_t || !norm2 || !cnorm || !margin) return cuda_fail(st, e, "workspace");
+    uint32_t* max_bits = (uint32_t*)(margin + n_pad);  // two spare words
+    if ((e = cudaMemsetAsync(max_bits, 0, 2 * sizeof(uint32_t), s)) != cudaSuccess) return cuda_fail(st, e, "memset");
+    if ((e = launch_column_means(xwork, n, d, ref, means, means + d, s)) != cudaSuccess)
+        return cuda_fail(st, e, "column means");
+    if ((e = launch_centre_transpose(xwork, n, n_pad, d, dp, means, coords_t, norm2, cnorm, xcentred, max_bits, s)) !=
+        cudaSuccess)
+        return cuda_fail(st, e, "centre");
+    if ((e = launch_margins(cnorm, norm2, n, d, o.mode, o.metric, SCRUST_FORM_PLAIN, max_bits, nullptr, nullptr, 1.0f,
+                            margin, s)) != cudaSuccess)
+        return cuda_fail(st, e, "margins");
+    ctx->launches += ref ? 3 : 4;
+
+    // Candidate lists.
+    const int row_tiles = (int)(n_pad / 128);
+    const int col_tiles = row_tiles;
+    int segments = 1;
+    if (o.segments) {
+        segments = (int)o.segments;
+    } else if (row_tiles < 4 * ctx->sm_count) {
+        segments = (4 * ctx->sm_count + row_tiles - 1) / row_tiles;
+        segments = std::min(segments, std::max(1, kRerankCapacity / (4 * (int)k)));
+    }
+    segments = std::max(1, std::min(segments, col_tiles));
+    {
+        const int per = (col_tiles + segments - 1) / segments;
+        segments = (col_tiles + per - 1) / per;  // no empty segment
+    }
+    int cap = (int)o.list_capacity;
+    if (cap == 0) cap = std::max(64, (2 * (int)k + 32 + 31) / 32 * 32);
+    cap = std::max(cap, (int)k + 32);
+    const int ctot = cap + 128;
+    if (ctot > 512) return fail(st, SCRUST_INVALID_PARAMETER, "list_capacity must be at most 384, got %d", cap);
+    Lists lists;
+    lists.cap = cap;
+    lists.ctot = ctot;
+    lists.segments = segments;
+    const size_t slots = (size_t)n_pad * segments;
+    lists.ids = (uint32_t*)ws_get(ctx, SLOT_LIST_IDS, sizeof(uint32_t) * slots * ctot, &e);
+    lists.vals = (float*)ws_get(ctx, SLOT_LIST_VALS, sizeof(float) * slots * ctot, &e);
+    lists.cnt = (uint32_t*)ws_get(ctx, SLOT_LIST_CNT, sizeof(uint32_t) * slots, &e);
+    lists.overflow = (uint32_t*)ws_get(ctx, SLOT_OVERFLOW, sizeof(uint32_t) * (size_t)n_pad, &e);
+    if (!lists.ids || !lists.vals || !lists.cnt || !lists.overflow) return cuda_fail(st, e, "workspace");
+    if ((e = cudaMemsetAsync(lists.overflow, 0, sizeof(uint32_t) * (size_t)n_pad, s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(lists.cnt, 0, sizeof(uint32_t) * slots, s)) != cudaSuccess)
+        return cuda_fail(st, e, "memset");
+    plan.cap = cap;
+    plan.ctot = ctot;
+    plan.segments = segments;
+
+    mark(ctx, PH_PREP);
+    if ((e = launch_plain_candidates(ctx, plan, coords_t, n_pad, coords_t, n_pad, dp, norm2, margin, lists)) !=
+        cudaSuccess)
+        return cuda_fail(st, e, "knn_candidates_f32");
+    ctx->launches += 1;
+    mark(ctx, PH_CAND);
+
+    const float* xr = ref ? xcentred : xwork;
+    if ((e = launch_rerank(ctx, plan, xr, xr, norm2, norm2, norm64, norm64, x, x, margin, lists, out_idx,
+                           out_dist)) != cudaSuccess)
+        return cuda_fail(st, e, "knn_rerank");
+    ctx->launches += 2;
+    mark(ctx, PH_RERANK);
+    return ok(st);
+}
+
+int32_t take_csr_buffers(scrust_context* ctx, uint64_t rows, uint64_t nnz_cap, CsrBuffers* out,
+                         scrust_status* st) {
+    for (size_t i = 0; i < ctx->csr_pool.size(); ++i) {
+        CsrBuffers& b = ctx->csr_pool[i];
+        if (b.rows_cap >= rows && b.nnz_cap >= nnz_cap) {
+            *out = b;
+            ctx->csr_pool.erase(ctx->csr_pool.begin() + (long)i);
+            return SCRUST_OK;
+        }
+    }
+    CsrBuffers b;
+    b.rows_cap = rows;
+    b.nnz_cap = std::max<uint64_t>(nnz_cap, 1);
+    cudaError_t e = cudaMalloc(&b.indptr, sizeof(uint32_t) * (rows + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b.indices, sizeof(uint32_t) * b.nnz_cap);
+    if (e == cudaSuccess) e = cudaMalloc(&b.values, sizeof(float) * b.nnz_cap);
+    if (e != cudaSuccess) {
+        cudaFree(b.indptr);
+        cudaFree(b.indices);
+        cudaFree(b.values);
+        cudaGetLastError();
+        return cuda_fail(st, e, "csr allocation");
+    }
+    *out = b;
+    return SCRUST_OK;
+}
+
+void return_csr_buffers(scrust_context* ctx, const CsrBuffers& b) {
+    if (!b.indptr) return;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->csr_pool.push_back(b);
+}
+
+int32_t conn_device_impl(scrust_context* ctx, const uint32_t* idx, const float* dist, uint64_t n, uint32_t k,
+                         bool validate, scrust_csr** out, scrust_status* st) {
+    CsrBuffers b;
+    int32_t rc = take_csr_buffers(ctx, n, 2 * n * (uint64_t)k, &b, st);
+    if (rc) return rc;
+    rc = run_connectivities(ctx, idx, dist, (int64_t)n, (int)k, validate, &b, st);
+    mark(ctx, PH_CONN);
+    if (rc) {
+        ctx->csr_pool.push_back(b);
+        return rc;
+    }
+    scrust_csr* csr = new (std::nothrow) scrust_csr;
+    if (!csr) {
+        ctx->csr_pool.push_back(b);
+        return fail(st, SCRUST_OOM, "host allocation failed");
+    }
+    csr->n_rows = n;
+    csr->n_cols = n;
+    csr->nnz = UINT64_MAX;  // read from indptr[n] on first request
+    csr->on_device = 1;
+    csr->owner = ctx;
+    csr->buf = b;
+    *out = csr;
+    return ok(st);
+}
+
+// Copies a device CSR into a new host CSR (synchronising the stream).
+int32_t csr_to_host(scrust_context* ctx, scrust_csr* dev, scrust_csr** out, scrust_status* st) {
+    uint32_t nnz = 0;
+    cudaError_t e = cudaMemcpyAsync(&nnz, dev->buf.indptr + dev->n_rows, sizeof(uint32_t),
+                                    cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(st, e, "csr readback");
+    scrust_csr* h = new (std::nothrow) scrust_csr;
+    if (!h) return fail(st, SCRUST_OOM, "host allocation failed");
+    try {
+        h->h_indptr.resize(dev->n_rows + 1);
+        h->h_indices.resize(nnz);
+        h->h_values.resize(nnz);
+    } catch (...) {
+        delete h;
+        return fail(st, SCRUST_OOM, "host allocation failed");
+    }
+    h->n_rows = dev->n_rows;
+    h->n_cols = dev->n_cols;
+    h->nnz = nnz;
+    h->on_device = 0;
+    e = cudaMemcpyAsync(h->h_indptr.data(), dev->buf.indptr, sizeof(uint32_t) * (dev->n_rows + 1),
+                        cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && nnz)
+        e = cudaMemcpyAsync(h->h_indices.data(), dev->buf.indices, sizeof(uint32_t) * nnz, cudaMemcpyDeviceToHost,
+                            ctx->stream);
+    if (e == cudaSuccess && nnz)
+        e = cudaMemcpyAsync(h->h_values.data(), dev->buf.values, sizeof(float) * nnz, cudaMemcpyDeviceToHost,
+                            ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        delete h;
+        return cuda_fail(st, e, "csr readback");
+    }
+    *out = h;
+    return ok(st);
+}
+
+}  // namespace
+
+}  // namespace scrust
+
+using namespace scrust;
+
+extern "C" {
+
+void scrust_knn_options_default(scrust_knn_options* o) {
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->struct_size = sizeof(*o);
+    o->form = SCRUST_FORM_PLAIN;
+    o->metric = SCRUST_METRIC_EUCLIDEAN;
+    o->mode = SCRUST_MODE_EXACT;
+    o->precision = SCRUST_PRECISION_FP16;
+}
+
+int32_t scrust_cuda_gpu_available(void) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    for (int i = 0; i < count; i++) {
+        cudaDeviceProp p;
+        if (cudaGetDeviceProperties(&p, i) == cudaSuccess && p.major == 10 && p.minor == 3) return 1;
+    }
+    return 0;
+}
+
+scrust_context* scrust_cuda_context_create(int32_t device, scrust_status* st) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        fail(st, SCRUST_NO_GPU, "no CUDA device is available on this machine");
+        return nullptr;
+    }
+    if (device < 0 || device >= count) {
+        fail(st, SCRUST_NO_GPU, "no CUDA device %d on this machine (%d present)", device, count);
+        return nullptr;
+    }
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, device) != cudaSuccess || p.major != 10 || p.minor != 3) {
+        cudaGetLastError();
+        fail(st, SCRUST_NO_GPU, "CUDA device %d is not compute capability 10.3 (sm_103a)", device);
+        return nullptr;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        fail(st, SCRUST_NO_GPU, "cannot select CUDA device %d", device);
+        return nullptr;
+    }
+    scrust_context* ctx = new (std::nothrow) scrust_context;
+    if (!ctx) {
+        fail(st, SCRUST_OOM, "host allocation failed");
+        return nullptr;
+    }
+    ctx->device = device;
+    ctx->sm_count = p.multiProcessorCount;
+    ctx->smem_optin = p.sharedMemPerBlockOptin;
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int) * DERR_COUNT);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, sizeof(uint32_t) * 16);
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(int) * DERR_COUNT);
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_counter, 0, sizeof(uint32_t) * 16);
+    if (e == cudaSuccess) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e == cudaSuccess && q == cudaDriverEntryPointSuccess)
+            ctx->encode_tiled = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+        else
+            e = cudaErrorNotSupported;
+    }
+    if (e != cudaSuccess) {
+        cuda_fail(st, e, "context creation");
+        scrust_cuda_context_destroy(ctx);
+        return nullptr;
+    }
+    ok(st);
+    return ctx;
+}
+
+void scrust_cuda_context_destroy(scrust_context* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (int i = 0; i < SLOT_COUNT; i++)
+        if (ctx->ws.ptr[i]) cudaFree(ctx->ws.ptr[i]);
+    for (auto& b : ctx->csr_pool) {
+        cudaFree(b.indptr);
+        cudaFree(b.indices);
+        cudaFree(b.values);
+    }
+    for (int i = 0; i < 5; i++)
+        if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->d_err) cudaFree(ctx->d_err);
+    if (ctx->d_counter) cudaFree(ctx->d_counter);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    cudaGetLastError();
+    delete ctx;
+}
+
+void* scrust_cuda_context_stream(scrust_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+uint32_t scrust_cuda_max_supported_k(const scrust_context* ctx) { return ctx ? kMaxK : 0; }
+
+int32_t scrust_cuda_knn_device(scrust_context* ctx, const float* x, uint64_t n, uint64_t d, uint32_t k,
+                               const scrust_knn_options* opt, uint32_t* out_idx, float* out_dist,
+                               scrust_status* st) {
+    int32_t rc = check_knn_args(n, d, k, st);
+    if (rc) return rc;
+    if ((rc = check_options(opt, st))) return rc;
+    if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
+    if (!x || !out_idx || !out_dist) return fail(st, SCRUST_SHAPE, "expected non-null device pointers");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return knn_device_impl(ctx, x, n, d, k, opt, out_idx, out_dist, st);
+}
+
+int32_t scrust_cuda_knn(scrust_context* ctx, const float* x, uint64_t n, uint64_t d, uint32_t k,
+                        const scrust_knn_options* opt, uint32_t* out_idx, float* out_dist, scrust_status* st) {
+    int32_t rc = check_knn_args(n, d, k, st);
+    if (rc) return rc;
+    if ((rc = check_options(opt, st))) return rc;
+    if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
+    if (!x || !out_idx || !out_dist) return fail(st, SCRUST_SHAPE, "expected non-null host pointers");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaError_t e;
+    float* dx = (float*)ws_get(ctx, SLOT_HOST_IN, sizeof(float) * n * d, &e);
+    uint32_t* di = (uint32_t*)ws_get(ctx, SLOT_HOST_IDX, sizeof(uint32_t) * n * k, &e);
+    float* dd = (float*)ws_get(ctx, SLOT_HOST_DIST, sizeof(float) * n * k, &e);
+    if (!dx || !di || !dd) return cuda_fail(st, e, "workspace");
+    if ((e = cudaMemcpyAsync(dx, x, sizeof(float) * n * d, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
+        return cuda_fail(st, e, "upload");
+    if ((rc = knn_device_impl(ctx, dx, n, d, k, opt, di, dd, st))) return rc;
+    if ((e = cudaMemcpyAsync(out_idx, di, sizeof(uint32_t) * n * k, cudaMemcpyDeviceToHost, ctx->stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(out_dist, dd, sizeof(float) * n * k, cudaMemcpyDeviceToHost, ctx->stream)) !=
+            cudaSuccess)
+        return cuda_fail(st, e, "download");
+    return collect_device_errors(ctx, st);
+}
+
+int32_t scrust_cuda_connectivities_device(scrust_context* ctx, const uint32_t* idx, const float* dist, uint64_t n,
+                                          uint32_t k, scrust_csr** out, scrust_status* st) {
+    if (n == 0 || k == 0)
+        return fail(st, SCRUST_SHAPE, "expected a neighbour graph with at least one cell and one neighbour, got %llu x %u",
+                    (unsigned long long)n, k);
+    if (n >= 0xffffffffull || 2 * n * (uint64_t)k >= 0xffffffffull)
+        return fail(st, SCRUST_SHAPE, "expected fewer than 2^31 graph entries, got %llu x %u", (unsigned long long)n, k);
+    if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
+    if (!idx || !dist || !out) return fail(st, SCRUST_SHAPE, "expected non-null pointers");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return conn_device_impl(ctx, idx, dist, n, k, true, out, st);
+}
+
+int32_t scrust_cuda_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, uint64_t n,
+                                   uint32_t k, scrust_csr** out, scrust_status* st) {
+    if (n == 0 || k == 0)
+        return fail(st, SCRUST_SHAPE, "expected a neighbour graph with at least one cell and one neighbour, got %llu x %u",
+                    (unsigned long long)n, k);
+    if (n >= 0xffffffffull || 2 * n * (uint64_t)k >= 0xffffffffull)
+        return fail(st, SCRUST_SHAPE, "expected fewer than 2^31 graph entries, got %llu x %u", (unsigned long long)n, k);
+    if (!idx || !dist || !out) return fail(st, SCRUST_SHAPE, "expected non-null pointers");
+    for (uint64_t i = 0; i < n * k; i++)
+        if (idx[i] >= n)
+            return fail(st, SCRUST_SHAPE, "expected neighbour ids below %llu, got an out-of-range neighbour id",
+                        (unsigned long long)n);
+    if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaError_t e;
+    uint32_t* di = (uint32_t*)ws_get(ctx, SLOT_HOST_IDX, sizeof(uint32_t) * n * k, &e);
+    float* dd = (float*)ws_get(ctx, SLOT_HOST_DIST, sizeof(float) * n * k, &e);
+    if (!di || !dd) return cuda_fail(st, e, "workspace");
+    if ((e = cudaMemcpyAsync(di, idx, sizeof(uint32_t) * n * k, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dd, dist, sizeof(float) * n * k, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
+        return cuda_fail(st, e, "upload");
+    scrust_csr* dev = nullptr;
+    int32_t rc = conn_device_impl(ctx, di, dd, n, k, false, &dev, st);
+    if (rc) return rc;
+    rc = csr_to_host(ctx, dev, out, st);
+    ctx->csr_pool.push_back(dev->buf);
+    delete dev;
+    if (rc) return rc;
+    return collect_device_errors(ctx, st);
+}
+
+int32_t scrust_cuda_smooth_knn_distances(scrust_context* ctx, const float* dist, uint64_t n, uint32_t k,
+                                         float* sigmas, float* rhos, scrust_status* st) {
+    if (n == 0 || k == 0)
+        return fail(st, SCRUST_SHAPE, "expected a distance matrix with at least one cell and one neighbour, got %llu x %u",
+                    (unsigned long long)n, k);
+    if (!dist || !sigmas || !rhos) return fail(st, SCRUST_SHAPE, "expected non-null pointers");
+    if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaError_t e;
+    float* dd = (float*)ws_get(ctx, SLOT_HOST_DIST, sizeof(float) * n * k, &e);
+    float* so = (float*)ws_get(ctx, SLOT_CONN_G, sizeof(float) * 2 * n, &e);
+    if (!dd || !so) return cuda_fail(st, e, "workspace");
+    if ((e = cudaMemcpyAsync(dd, dist, sizeof(float) * n * k, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
+        return cuda_fail(st, e, "upload");
+    if ((e = launch_smooth_knn(ctx, dd, (int64_t)n, (int)k, so, so + n)) != cudaSuccess)
+        return cuda_fail(st, e, "smooth_knn");
+    if ((e = cudaMemcpyAsync(sigmas, so, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(rhos, so + n, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess)
+        return cuda_fail(st, e, "download");
+    return collect_device_errors(ctx, st);
+}
+
+int32_t scrust_cuda_neighbors_graph_device(scrust_context* ctx, const float* x, uint64_t n, uint64_t d, uint32_t k,
+                                           const scrust_knn_options* opt, uint32_t* out_idx, float* out_dist,
+                                           scrust_csr** conn, scrust_status* st) {
+    int32_t rc = check_knn_args(n, d, k, st);
+    if (rc) return rc;
+    if ((rc = check_options(opt, st))) return rc;
+    if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
+    if (!x || !out_idx || !out_dist || !conn) return fail(st, SCRUST_SHAPE, "expected non-null pointers");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if ((rc = knn_device_impl(ctx, x, n, d, k, opt, out_idx, out_dist, st))) return rc;
+    return conn_device_impl(ctx, out_idx, out_dist, n, k, false, conn, st);
+}
+
+int32_t scrust_cuda_neighbors_graph(scrust_context* ctx, const float* x, uint64_t n, uint64_t d, uint32_t k,
+                                    const scrust_knn_options* opt, uint32_t* out_idx, float* out_dist,
+                                    scrust_csr** conn, scrust_status* st) {
+    int32_t rc = check_knn_args(n, d, k, st);
+    if (rc) return rc;
+    if ((rc = check_options(opt, st))) return rc;
+    if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
+    if (!x || !out_idx || !out_dist || !conn) return fail(st, SCRUST_SHAPE, "expected non-null pointers");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaError_t e;
+    float* dx = (float*)ws_get(ctx, SLOT_HOST_IN, sizeof(float) * n * d, &e);
+    uint32_t* di = (uint32_t*)ws_get(ctx, SLOT_HOST_IDX, sizeof(uint32_t) * n * k, &e);
+    float* dd = (float*)ws_get(ctx, SLOT_HOST_DIST, sizeof(float) * n * k, &e);
+    if (!dx || !di || !dd) return cuda_fail(st, e, "workspace");
+    if ((e = cudaMemcpyAsync(dx, x, sizeof(float) * n * d, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
+        return cuda_fail(st, e, "upload");
+    if ((rc = knn_device_impl(ctx, dx, n, d, k, opt, di, dd, st))) return rc;
+    scrust_csr* dev = nullptr;
+    if ((rc = conn_device_impl(ctx, di, dd, n, k, false, &dev, st))) return rc;
+    if ((e = cudaMemcpyAsync(out_idx, di, sizeof(uint32_t) * n * k, cudaMemcpyDeviceToHost, ctx->stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(out_dist, dd, sizeof(float) * n * k, cudaMemcpyDeviceToHost, ctx->stream)) !=
+            cudaSuccess) {
+        ctx->csr_pool.push_back(dev->buf);
+        delete dev;
+        return cuda_fail(st, e, "download");
+    }
+    rc = csr_to_host(ctx, dev, conn, st);
+    ctx->csr_pool.push_back(dev->buf);
+    delete dev;
+    if (rc) return rc;
+    return collect_device_errors(ctx, st);
+}
+
+int32_t scrust_cuda_synchronize(scrust_context* ctx, scrust_status* st) {
+    if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return collect_device_errors(ctx, st);
+}
+
+uint64_t scrust_csr_n_rows(const scrust_csr* c) { return c ? c->n_rows : 0; }
+uint64_t scrust_csr_n_cols(const scrust_csr* c) { return c ? c->n_cols : 0; }
+
+uint64_t scrust_csr_nnz(const scrust_csr* c) {
+    if (!c) return 0;
+    if (c->nnz != UINT64_MAX) return c->nnz;
+    uint32_t nnz = 0;
+    scrust_csr* m = const_cast<scrust_csr*>(c);
+    if (c->owner) {
+        std::lock_guard<std::mutex> lock(c->owner->mu);
+        cudaSetDevice(c->owner->device);
+        if (cudaMemcpyAsync(&nnz, c->buf.indptr + c->n_rows, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            c->owner->stream) == cudaSuccess &&
+            cudaStreamSynchronize(c->owner->stream) == cudaSuccess)
+            m->nnz = nnz;
+        else
+            cudaGetLastError();
+    }
+    return c->nnz == UINT64_MAX ? 0 : c->nnz;
+}
+
+int32_t scrust_csr_on_device(const scrust_csr* c) { return c ? c->on_device : 0; }
+const uint32_t* scrust_csr_indptr(const scrust_csr* c) {
+    return c ? (c->on_device ? c->buf.indptr : c->h_indptr.data()) : nullptr;
+}
+const uint32_t* scrust_csr_indices(const scrust_csr* c) {
+    return c ? (c->on_device ? c->buf.indices : c->h_indices.data()) : nullptr;
+}
+const float* scrust_csr_values(const scrust_csr* c) {
+    return c ? (c->on_device ? c->buf.values : c->h_values.data()) : nullptr;
+}
+
+void scrust_csr_free(scrust_csr* c) {
+    if (!c) return;
+    if (c->on_device && c->owner) return_csr_buffers(c->owner, c->buf);
+    delete c;
+}
+
+void scrust_cuda_set_timing(scrust_context* ctx, int32_t enable) {
+    if (!ctx) return;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->timing = enable != 0;
+}
+
+int32_t scrust_cuda_phase_times(scrust_context* ctx, float* ms, int32_t max_phases) {
+    if (!ctx || !ms) return 0;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int written = 0;
+    int prev = PH_START;
+    if (!ctx->ev_recorded[PH_START]) return 0;
+    for (int p = PH_PREP; p <= PH_CONN && written < max_phases; ++p) {
+        float t = 0.f;
+        if (ctx->ev_recorded[p] && cudaEventElapsedTime(&t, ctx->ev[prev], ctx->ev[p]) == cudaSuccess) {
+            prev = p;
+        } else {
+            cudaGetLastError();
+            t = 0.f;
+        }
+        ms[written++] = t;
+    }
+    return written;
+}
+
+uint64_t scrust_cuda_launch_count(const scrust_context* ctx) { return ctx ? ctx->launches : 0; }
+
+const char* scrust_cuda_version(void) { return "scrust-gb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

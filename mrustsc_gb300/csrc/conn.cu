@@ -1,0 +1,442 @@
+// conn.cu -- UMAP connectivities on the device, following
+// crates/scrust-core/src/neighbors.rs:208-372:
+//   smooth_knn_distances (:239-298)  one thread per row: rho, the 64-step f32
+//                                    bisection with f64 tolerance test, sigma floor
+//   directed_weights (:300-327)      one thread per row, sorted by column
+//   symmetrise (:329-372)            transpose by a stable LSD radix sort of the
+//                                    directed edges keyed by target row, then a
+//                                    per-row sorted merge with (w + r) - (w * r)
+// Every f32 operation is written with explicit round-to-nearest intrinsics so
+// nothing is contracted into an fma, matching the reference's uncontracted Rust
+// arithmetic; exp is CUDA's expf.  Sums of a row use ndarray 0.16.1's
+// unrolled_fold order (crates/scrust-core/src/neighbors.rs:248,290); the global
+// mean is an FP64 sum rounded to f32.
+#include <math.h>
+
+#include <algorithm>
+#include <utility>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace scrust {
+
+namespace {
+
+// ndarray 0.16.1 numeric_util::unrolled_fold with f32 addition.
+__device__ float unrolled_sum(const float* xs, int len) {
+    float acc = 0.f;
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f, p4 = 0.f, p5 = 0.f, p6 = 0.f, p7 = 0.f;
+    while (len >= 8) {
+        p0 = __fadd_rn(p0, xs[0]);
+        p1 = __fadd_rn(p1, xs[1]);
+        p2 = __fadd_rn(p2, xs[2]);
+        p3 = __fadd_rn(p3, xs[3]);
+        p4 = __fadd_rn(p4, xs[4]);
+        p5 = __fadd_rn(p5, xs[5]);
+        p6 = __fadd_rn(p6, xs[6]);
+        p7 = __fadd_rn(p7, xs[7]);
+        xs += 8;
+        len -= 8;
+    }
+    acc = __fadd_rn(acc, __fadd_rn(p0, p4));
+    acc = __fadd_rn(acc, __fadd_rn(p1, p5));
+    acc = __fadd_rn(acc, __fadd_rn(p2, p6));
+    acc = __fadd_rn(acc, __fadd_rn(p3, p7));
+    for (int i = 0; i < len; i++) acc = __fadd_rn(acc, xs[i]);
+    return acc;
+}
+
+__global__ void check_ids_kernel(const uint32_t* __restrict__ idx, int64_t total, int64_t n, int* err) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x)
+        if ((int64_t)idx[i] >= n) atomicExch(err + DERR_BAD_INDEX, 1);
+}
+
+__global__ void sum_partial_kernel(const float* __restrict__ x, int64_t total, double* __restrict__ partial) {
+    __shared__ double ws[32];
+    double s = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x)
+        s += (double)x[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += ws[w];
+        partial[blockIdx.x] = t;
+    }
+}
+
+__global__ void mean_final_kernel(const double* __restrict__ partial, int blocks, int64_t total,
+                                  float* __restrict__ mean) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double t = 0.0;
+    for (int b = 0; b < blocks; b++) t += partial[b];
+    *mean = __fdiv_rn(__double2float_rn(t), (float)total);
+}
+
+__global__ void smooth_knn_kernel(const float* __restrict__ dist, int64_t n, int k, double target,
+                                  const float* __restrict__ mean, float* __restrict__ sigmas,
+                                  float* __restrict__ rhos) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* row = dist + i * k;
+    float rho = 0.f;
+    for (int j = 0; j < k; j++) {
+        float v = row[j];
+        if (v > 0.f) {
+            rho = v;
+            break;
+        }
+    }
+    const float fmax = 3.40282346638528859812e+38f;
+    float low = 0.f, high = fmax, mid = 1.f;
+    for (int it = 0; it < 64; it++) {
+        float card = 0.f;
+        for (int j = 0; j < k; j++) {
+            float offset = __fsub_rn(row[j], rho);
+            float term = offset > 0.f ? expf(__fdiv_rn(-offset, mid)) : 1.0f;
+            card = __fadd_rn(card, term);
+        }
+        double c64 = (double)card;
+        if (fabs(c64 - target) < 1e-5) break;
+        if (c64 > target) {
+            high = mid;
+            mid = __fdiv_rn(__fadd_rn(low, high), 2.0f);
+        } else {
+            low = mid;
+            mid = high >= fmax ? __fmul_rn(mid, 2.0f) : __fdiv_rn(__fadd_rn(low, high), 2.0f);
+        }
+    }
+    float reference = rho > 0.f ? __fdiv_rn(unrolled_sum(row, k), (float)(k + 1)) : *mean;
+    sigmas[i] = fmaxf(mid, __fmul_rn(1e-3f, reference));
+    rhos[i] = rho;
+}
+
+// Directed weights of one row, sorted by column (a stable insertion sort in
+// the row's own output slots, so equal columns keep their input order); also
+// emits the row's k edge slots for the transpose sort (invalid slots keyed
+// past n so they sort last).
+__global__ void directed_kernel(const uint32_t* __restrict__ idx, const float* __restrict__ dist,
+                                int64_t n, int k, const float* __restrict__ sigmas,
+                                const float* __restrict__ rhos, uint32_t* __restrict__ dcol,
+                                float* __restrict__ dw, uint32_t* __restrict__ dcnt,
+                                uint32_t* __restrict__ ekey, unsigned long long* __restrict__ eval,
+                                uint32_t* __restrict__ indeg) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t* col = dcol + i * k;
+    float* w = dw + i * k;
+    int m = 0;
+    const float sigma = sigmas[i], rho = rhos[i];
+    for (int j = 0; j < k; j++) {
+        const uint32_t nb = idx[i * k + j];
+        if ((int64_t)nb == i) continue;
+        const float offset = __fsub_rn(dist[i * k + j], rho);
+        const float wt = (offset <= 0.f || sigma == 0.f) ? 1.0f : expf(__fdiv_rn(-offset, sigma));
+        if (wt == 0.f) continue;
+        int s = m;
+        while (s > 0 && col[s - 1] > nb) {
+            col[s] = col[s - 1];
+            w[s] = w[s - 1];
+            s--;
+        }
+        col[s] = nb;
+        w[s] = wt;
+        m++;
+    }
+    dcnt[i] = (uint32_t)m;
+    for (int t = 0; t < k; t++) {
+        const int64_t slot = i * k + t;
+        if (t < m) {
+            ekey[slot] = col[t];
+            eval[slot] = ((unsigned long long)(uint32_t)i << 32) | __float_as_uint(w[t]);
+            atomicAdd(indeg + col[t], 1u);
+        } else {
+            ekey[slot] = (uint32_t)n;
+            eval[slot] = 0ull;
+        }
+    }
+}
+
+// ---- stable LSD radix sort (8-bit digits) ---------------------------------
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_ROUNDS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;  // 4096
+
+__global__ void rs_hist_kernel(const uint32_t* __restrict__ keys, int64_t total, int shift,
+                               uint32_t* __restrict__ block_hist, int nblocks) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t t0 = (int64_t)blockIdx.x * RS_TILE;
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const int64_t p = t0 + r * RS_THREADS + threadIdx.x;
+        if (p < total) atomicAdd(&h[(keys[p] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    block_hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void rs_scatter_kernel(const uint32_t* __restrict__ kin, const unsigned long long* __restrict__ vin,
+                                  uint32_t* __restrict__ kout, unsigned long long* __restrict__ vout,
+                                  int64_t total, int shift, const uint32_t* __restrict__ offsets,
+                                  int nblocks) {
+    __shared__ uint32_t wcnt[RS_WARPS][256];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int d = lane; d < 256; d += 32) wcnt[warp][d] = 0;
+    __syncwarp();
+    const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)warp * (RS_TILE / RS_WARPS);
+    uint32_t key[RS_ROUNDS];
+    unsigned long long val[RS_ROUNDS];
+    uint32_t rank[RS_ROUNDS];
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const int64_t p = base + r * 32 + lane;
+        const bool valid = p < total;
+        key[r] = valid ? kin[p] : 0xffffffffu;
+        val[r] = valid ? vin[p] : 0ull;
+        const uint32_t d = valid ? ((key[r] >> shift) & 255u) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t before = valid ? wcnt[warp][d] : 0u;
+        rank[r] = before + __popc(peers & lanemask_lt());
+        __syncwarp();
+        if (valid && (__ffs(peers) - 1) == lane) wcnt[warp][d] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        const int d = threadIdx.x;  // 256 threads, one digit each
+        uint32_t run = 0;
+        for (int w = 0; w < RS_WARPS; w++) {
+            const uint32_t c = wcnt[w][d];
+            wcnt[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; r++) {
+        const int64_t p = base + r * 32 + lane;
+        if (p < total) {
+            const uint32_t d = (key[r] >> shift) & 255u;
+            const int64_t dst = (int64_t)offsets[(int64_t)d * nblocks + blockIdx.x] + wcnt[warp][d] + rank[r];
+            kout[dst] = key[r];
+            vout[dst] = val[r];
+        }
+    }
+}
+
+// ---- exclusive scan of u32 --------------------------------------------------
+
+constexpr int SC_THREADS = 1024;
+constexpr int SC_TILE = 2 * SC_THREADS;
+
+__global__ void scan_tiles_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int64_t n,
+                                  uint32_t* __restrict__ sums) {
+    __shared__ uint32_t warp_tot[SC_THREADS / 32];
+    const int64_t p0 = (int64_t)blockIdx.x * SC_TILE + 2 * threadIdx.x;
+    const uint32_t a = p0 < n ? in[p0] : 0u;
+    const uint32_t b = p0 + 1 < n ? in[p0 + 1] : 0u;
+    const uint32_t t = a + b;
+    uint32_t x = t;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t v = warp_tot[lane];
+        uint32_t s = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        warp_tot[lane] = s - v;  // exclusive
+        if (lane == 31 && sums) sums[blockIdx.x] = s;
+    }
+    __syncthreads();
+    const uint32_t excl = warp_tot[warp] + x - t;
+    if (p0 < n) out[p0] = excl;
+    if (p0 + 1 < n) out[p0 + 1] = excl + a;
+}
+
+__global__ void scan_add_kernel(uint32_t* __restrict__ out, int64_t n, const uint32_t* __restrict__ sums) {
+    const int64_t p0 = (int64_t)blockIdx.x * SC_TILE + 2 * threadIdx.x;
+    const uint32_t add = sums[blockIdx.x];
+    if (p0 < n) out[p0] += add;
+    if (p0 + 1 < n) out[p0 + 1] += add;
+}
+
+// ---- symmetrise -------------------------------------------------------------
+
+__global__ void merge_kernel(const uint32_t* __restrict__ dcol, const float* __restrict__ dw,
+                             const uint32_t* __restrict__ dcnt, const unsigned long long* __restrict__ tval,
+                             const uint32_t* __restrict__ tstart, int64_t n, int k,
+                             const uint32_t* __restrict__ indptr, uint32_t* __restrict__ rowcnt,
+                             uint32_t* __restrict__ out_cols, float* __restrict__ out_vals) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t* fc = dcol + i * k;
+    const float* fw = dw + i * k;
+    const int nf = (int)dcnt[i];
+    const uint32_t b0 = tstart[i], b1 = tstart[i + 1];
+    const bool write = indptr != nullptr;
+    uint32_t out = write ? indptr[i] : 0u;
+    uint32_t count = 0;
+    int f = 0;
+    uint32_t b = b0;
+    while (f < nf || b < b1) {
+        const uint32_t fcol = f < nf ? fc[f] : 0xffffffffu;
+        const uint32_t bcol = b < b1 ? (uint32_t)(tval[b] >> 32) : 0xffffffffu;
+        const uint32_t c = fcol < bcol ? fcol : bcol;
+        float wv = 0.f, rv = 0.f;
+        if (f < nf && fcol == c) {
+            wv = fw[f];
+            f++;
+        }
+        if (b < b1 && bcol == c) {
+            rv = __uint_as_float((uint32_t)tval[b]);
+            b++;
+        }
+        if (write) {
+            out_cols[out + count] = c;
+            out_vals[out + count] = __fsub_rn(__fadd_rn(wv, rv), __fmul_rn(wv, rv));
+        }
+        count++;
+    }
+    if (!write) rowcnt[i] = count;
+}
+
+}  // namespace
+
+// Exclusive scan of n u32 values (in may equal out).
+cudaError_t device_exclusive_scan(scrust_context* ctx, const uint32_t* in, uint32_t* out, int64_t n,
+                                  uint32_t* scratch, size_t scratch_elems) {
+    const int64_t tiles = (n + SC_TILE - 1) / SC_TILE;
+    if (tiles <= 1) {
+        scan_tiles_kernel<<<1, SC_THREADS, 0, ctx->stream>>>(in, out, n, nullptr);
+        ctx->launches += 1;
+        return cudaGetLastError();
+    }
+    ctx->launches += 2;
+    if ((size_t)tiles > scratch_elems) return cudaErrorInvalidValue;
+    uint32_t* sums = scratch;
+    scan_tiles_kernel<<<(unsigned)tiles, SC_THREADS, 0, ctx->stream>>>(in, out, n, sums);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = device_exclusive_scan(ctx, sums, sums, tiles, scratch + tiles, scratch_elems - (size_t)tiles);
+    if (e != cudaSuccess) return e;
+    scan_add_kernel<<<(unsigned)tiles, SC_THREADS, 0, ctx->stream>>>(out, n, sums);
+    return cudaGetLastError();
+}
+
+size_t scan_scratch_elems(int64_t n) {
+    size_t total = 0;
+    int64_t t = (n + SC_TILE - 1) / SC_TILE;
+    while (t > 1) {
+        total += (size_t)t;
+        t = (t + SC_TILE - 1) / SC_TILE;
+    }
+    return total + 16;
+}
+
+cudaError_t launch_smooth_knn(scrust_context* ctx, const float* dist, int64_t n, int k, float* sigmas,
+                              float* rhos) {
+    cudaError_t e;
+    const int64_t total = n * (int64_t)k;
+    const int blocks = (int)std::min<int64_t>(1024, (total + 255) / 256);
+    double* partial = (double*)ws_get(ctx, SLOT_MISC, sizeof(double) * 1024 + 64, &e);
+    if (!partial) return e;
+    float* mean = (float*)(partial + 1024);
+    sum_partial_kernel<<<blocks, 256, 0, ctx->stream>>>(dist, total, partial);
+    mean_final_kernel<<<1, 32, 0, ctx->stream>>>(partial, blocks, total, mean);
+    const double target = log2((double)(k + 1));
+    smooth_knn_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(dist, n, k, target, mean,
+                                                                           sigmas, rhos);
+    return cudaGetLastError();
+}
+
+int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n, int k,
+                           bool validate, CsrBuffers* out, scrust_status* st) {
+    cudaError_t e = cudaSuccess;
+    cudaStream_t s = ctx->stream;
+    const int64_t E = n * (int64_t)k;
+    uint64_t scan_launches = 0;
+    if (validate) {
+        scan_launches += 1;
+        check_ids_kernel<<<1024, 256, 0, s>>>(idx, E, n, ctx->d_err);
+        int bad = 0;
+        if ((e = cudaMemcpyAsync(&bad, ctx->d_err + DERR_BAD_INDEX, sizeof(int), cudaMemcpyDeviceToHost, s)) !=
+                cudaSuccess ||
+            (e = cudaStreamSynchronize(s)) != cudaSuccess)
+            return cuda_fail(st, e, "connectivities: id check");
+        if (bad) {
+            cudaMemsetAsync(ctx->d_err + DERR_BAD_INDEX, 0, sizeof(int), s);
+            return fail(st, SCRUST_SHAPE, "expected neighbour ids below %lld, got an out-of-range neighbour id",
+                        (long long)n);
+        }
+    }
+    // Scratch layout.
+    const int nblocks = (int)((E + RS_TILE - 1) / RS_TILE);
+    const size_t scan_elems = scan_scratch_elems(std::max<int64_t>((int64_t)256 * nblocks, n + 1));
+    char* a = (char*)ws_get(ctx, SLOT_CONN_A, sizeof(float) * 2 * (size_t)n + sizeof(uint32_t) * 3 * (size_t)(n + 1) + 256, &e);
+    uint32_t* dcol = (uint32_t*)ws_get(ctx, SLOT_CONN_B, sizeof(uint32_t) * (size_t)E, &e);
+    float* dw = (float*)ws_get(ctx, SLOT_CONN_C, sizeof(float) * (size_t)E, &e);
+    uint32_t* keyA = (uint32_t*)ws_get(ctx, SLOT_CONN_D, sizeof(uint32_t) * 2 * (size_t)E, &e);
+    unsigned long long* valA = (unsigned long long*)ws_get(ctx, SLOT_CONN_E, sizeof(unsigned long long) * 2 * (size_t)E, &e);
+    uint32_t* hist = (uint32_t*)ws_get(ctx, SLOT_CONN_F, sizeof(uint32_t) * ((size_t)256 * nblocks + 16), &e);
+    uint32_t* scan_scratch = (uint32_t*)ws_get(ctx, SLOT_SCAN, sizeof(uint32_t) * scan_elems, &e);
+    if (!a || !dcol || !dw || !keyA || !valA || !hist || !scan_scratch) return cuda_fail(st, e, "connectivities: workspace");
+    float* sig = (float*)a;
+    float* rho = sig + n;
+    uint32_t* indeg = (uint32_t*)(rho + n);   // n + 1
+    uint32_t* rowcnt = indeg + (n + 1);        // n + 1
+    uint32_t* dcnt = rowcnt + (n + 1);         // n (+1 spare)
+    uint32_t* keyB = keyA + E;
+    unsigned long long* valB = valA + E;
+
+    if ((e = launch_smooth_knn(ctx, dist, n, k, sig, rho)) != cudaSuccess) return cuda_fail(st, e, "smooth_knn");
+    if ((e = cudaMemsetAsync(indeg, 0, sizeof(uint32_t) * (size_t)(n + 1), s)) != cudaSuccess)
+        return cuda_fail(st, e, "memset");
+    directed_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(idx, dist, n, k, sig, rho, dcol, dw, dcnt, keyA,
+                                                                 valA, indeg);
+    scan_launches += 3 /* smooth_knn */ + 1 /* directed */ + 2 /* merges */;
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "directed weights");
+    // Stable radix sort of the edge slots by target row.
+    int bits = 1;
+    while (((int64_t)1 << bits) <= n) bits++;
+    uint32_t *kin = keyA, *kout = keyB;
+    unsigned long long *vin = valA, *vout = valB;
+    for (int shift = 0; shift < bits; shift += 8) {
+        rs_hist_kernel<<<nblocks, RS_THREADS, 0, s>>>(kin, E, shift, hist, nblocks);
+        if ((e = device_exclusive_scan(ctx, hist, hist, (int64_t)256 * nblocks, scan_scratch, scan_elems)) != cudaSuccess)
+            return cuda_fail(st, e, "radix scan");
+        rs_scatter_kernel<<<nblocks, RS_THREADS, 0, s>>>(kin, vin, kout, vout, E, shift, hist, nblocks);
+        scan_launches += 2;
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "radix scatter");
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    // Transpose bucket starts.
+    if ((e = device_exclusive_scan(ctx, indeg, indeg, n + 1, scan_scratch, scan_elems)) != cudaSuccess)
+        return cuda_fail(st, e, "indegree scan");
+    merge_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(dcol, dw, dcnt, vin, indeg, n, k, nullptr, rowcnt,
+                                                             nullptr, nullptr);
+    if ((e = cudaMemsetAsync(rowcnt + n, 0, sizeof(uint32_t), s)) != cudaSuccess) return cuda_fail(st, e, "memset");
+    if ((e = device_exclusive_scan(ctx, rowcnt, out->indptr, n + 1, scan_scratch, scan_elems)) != cudaSuccess)
+        return cuda_fail(st, e, "row scan");
+    merge_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(dcol, dw, dcnt, vin, indeg, n, k, out->indptr, nullptr,
+                                                             out->indices, out->values);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "merge");
+    ctx->launches += scan_launches;
+    return ok(st);
+}
+
+}  // namespace scrust

@@ -1,0 +1,171 @@
+// internal.h -- host-side types shared by the translation units of the
+// library: the context (the analogue of the reference's MetalContext,
+// crates/scrust-gpu/src/context.rs:12-91), its workspace arena, and the
+// launch functions each .cu file provides.
+#pragma once
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "scrust_cuda.h"
+
+namespace scrust {
+
+// Named workspace slots; each grows on demand and is reused across calls.
+enum Slot : int {
+    SLOT_MEANS = 0,
+    SLOT_COORDS_T,      // centred coordinates, transposed (plain form)
+    SLOT_NORM2,         // squared centred norms per row (+inf on padding)
+    SLOT_MARGIN,        // per-row candidate margin (s-space)
+    SLOT_CNORM,         // per-row centred norm (for bounds)
+    SLOT_LIST_IDS,
+    SLOT_LIST_VALS,
+    SLOT_LIST_CNT,
+    SLOT_OVERFLOW,
+    SLOT_FALLBACK_ROWS,
+    SLOT_FALLBACK_SCRATCH,
+    SLOT_XWORK,         // normalised (cosine) or centred (reference-snap) rows
+    SLOT_NORM64,        // FP64 norms (cosine)
+    SLOT_A16,           // tensor form operands
+    SLOT_B16,
+    SLOT_QERR,          // per-row quantisation error norms (tensor form)
+    SLOT_HOST_IN,       // staging of host inputs
+    SLOT_HOST_IDX,
+    SLOT_HOST_DIST,
+    SLOT_CONN_A,        // connectivities scratch
+    SLOT_CONN_B,
+    SLOT_CONN_C,
+    SLOT_CONN_D,
+    SLOT_CONN_E,
+    SLOT_CONN_F,
+    SLOT_CONN_G,
+    SLOT_SCAN,
+    SLOT_MISC,
+    SLOT_WORKQ,
+    SLOT_COUNT
+};
+
+struct Workspace {
+    void* ptr[SLOT_COUNT] = {};
+    size_t bytes[SLOT_COUNT] = {};
+};
+
+struct CsrBuffers {
+    uint32_t* indptr = nullptr;
+    uint32_t* indices = nullptr;
+    float* values = nullptr;
+    size_t rows_cap = 0;   // indptr holds rows_cap + 1 entries
+    size_t nnz_cap = 0;
+};
+
+}  // namespace scrust
+
+struct scrust_context {
+    int device = 0;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    scrust::Workspace ws;
+    int* d_err = nullptr;          // scrust::DERR_COUNT ints
+    uint32_t* d_counter = nullptr; // small device counters (fallback rows, work queue)
+    std::vector<scrust::CsrBuffers> csr_pool;
+    PFN_cuTensorMapEncodeTiled_v12000 encode_tiled = nullptr;
+    uint64_t launches = 0;              // kernels enqueued so far
+    bool timing = false;
+    cudaEvent_t ev[5] = {};             // phase boundaries: prep | candidates | rerank | connectivities
+    bool ev_recorded[5] = {};
+};
+
+struct scrust_csr {
+    uint64_t n_rows = 0;
+    uint64_t n_cols = 0;
+    uint64_t nnz = 0;
+    int32_t on_device = 0;
+    scrust_context* owner = nullptr;  // device CSRs return their buffers to this pool
+    scrust::CsrBuffers buf;
+    std::vector<uint32_t> h_indptr, h_indices;
+    std::vector<float> h_values;
+};
+
+namespace scrust {
+
+// Phase boundary events (no-ops unless timing is enabled).
+enum Phase { PH_START = 0, PH_PREP = 1, PH_CAND = 2, PH_RERANK = 3, PH_CONN = 4 };
+void mark(scrust_context* ctx, Phase p);
+
+// Status helpers.
+int32_t fail(scrust_status* st, int32_t code, const char* fmt, ...);
+int32_t ok(scrust_status* st);
+int32_t cuda_fail(scrust_status* st, cudaError_t e, const char* what);
+
+// Workspace access (may cudaMalloc; call with the context lock held).
+void* ws_get(scrust_context* ctx, Slot slot, size_t bytes, cudaError_t* err);
+
+// Parameters of one kNN solve on device-resident data.
+struct KnnPlan {
+    int64_t nq = 0, nr = 0;   // query rows, reference rows (equal for self-kNN)
+    int d = 0, k = 0;
+    bool self = true;         // query i is reference i (exclude it)
+    int form = SCRUST_FORM_PLAIN;
+    int metric = SCRUST_METRIC_EUCLIDEAN;
+    int mode = SCRUST_MODE_EXACT;
+    int precision = SCRUST_PRECISION_FP16;
+    int cap = 0;              // list capacity that triggers a prune
+    int ctot = 0;             // list storage per (row, segment)
+    int segments = 1;
+};
+
+// Candidate lists as the candidate kernels write them and the rerank reads.
+struct Lists {
+    uint32_t* ids = nullptr;
+    float* vals = nullptr;
+    uint32_t* cnt = nullptr;       // [rows_pad * segments]
+    uint32_t* overflow = nullptr;  // [rows_pad]
+    int cap = 0, ctot = 0, segments = 1;
+};
+
+// prep.cu
+cudaError_t launch_column_means(const float* x, int64_t n, int d, bool sequential, double* means,
+                                double* partial, cudaStream_t s);
+cudaError_t launch_normalise_rows(const float* x, int64_t n, int d, float* xn, double* norm64,
+                                  int* d_err, cudaStream_t s);
+cudaError_t launch_centre_transpose(const float* x, int64_t n, int64_t n_pad, int d, int dp,
+                                    const double* means, float* coords_t, float* norm2,
+                                    float* cnorm, float* xcentred, uint32_t* max_norm_bits,
+                                    cudaStream_t s);
+cudaError_t launch_margins(const float* cnorm, const float* norm2, int64_t n, int d, int mode,
+                           int metric, int form, const uint32_t* max_norm_bits,
+                           const float* qerr, const uint32_t* max_qerr_bits, float scale2,
+                           float* margin, cudaStream_t s);
+
+// knn_plain.cu
+cudaError_t launch_plain_candidates(scrust_context* ctx, const KnnPlan& plan, const float* q_t,
+                                    int64_t nq_pad, const float* r_t, int64_t nr_pad, int dp,
+                                    const float* r_norm2, const float* margin, const Lists& lists);
+
+// rerank.cu
+cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float* qx,
+                          const float* rx, const float* qnorm2, const float* rnorm2,
+                          const double* qn64, const double* rn64, const float* qraw,
+                          const float* rraw, const float* margin, const Lists& lists,
+                          uint32_t* out_idx, float* out_dist);
+
+// conn.cu
+cudaError_t launch_smooth_knn(scrust_context* ctx, const float* dist, int64_t n, int k,
+                              float* sigmas, float* rhos);
+int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n,
+                           int k, bool validate, CsrBuffers* out, scrust_status* st);
+
+// Tensor-map encoding through the driver entry point.
+bool encode_2d(scrust_context* ctx, CUtensorMap* map, CUtensorMapDataType dtype, void* base,
+               uint64_t inner, uint64_t outer, uint64_t row_bytes, uint32_t box_inner,
+               uint32_t box_outer, CUtensorMapSwizzle swizzle);
+
+}  // namespace scrust

@@ -1,0 +1,348 @@
+// rerank.cu -- exact finish of every row: candidates from the lists are
+// pruned to the final threshold, re-measured in the FP32 difference form on
+// the caller's coordinates, sorted by (distance, id), and any group of
+// candidates whose FP32 gap is inside the difference form's error bound and
+// that reaches the first k positions is adjudicated in FP64.
+//
+// This is what makes the neighbour lists equal to the FP64 exact kNN with
+// lowest-index tie-break (tests/test_neighbors_audit.py:52-61) whatever form
+// produced the candidates.  In reference-snap mode the value is instead the
+// reference Metal kernel's (crates/scrust-gpu/src/kernels/knn.rs:223-244) and
+// the order its (d^2, id) order (knn.rs:179-182), with no adjudication.
+//
+// One warp per row in the common case; rows whose lists overflowed, or whose
+// union exceeds the warp's capacity, go to a block-per-row fallback that
+// re-measures the whole row.
+#include "common.cuh"
+#include "internal.h"
+
+namespace scrust {
+
+namespace {
+
+constexpr int RR_WARPS = 4;
+constexpr int RC = 1024;      // keys per warp
+constexpr int FB_CAP = 4096;  // keys per fallback block
+constexpr int FB_THREADS = 256;
+constexpr int FB_BLOCKS = 32;
+
+struct RerankArgs {
+    const float* qx;
+    const float* rx;
+    const float* qn2;
+    const float* rn2;
+    const double* qn64;
+    const double* rn64;
+    const float* qraw;
+    const float* rraw;
+    const float* margin;
+    Lists lists;
+    int64_t nq, nr;
+    int d, k, mode, metric, self;
+    float gamma;
+    uint32_t* out_idx;
+    float* out_dist;
+    uint32_t* fb_rows;
+    uint32_t* fb_count;
+    uint32_t* fb_next;
+    float* fb_scratch;
+    int* err;
+};
+
+__device__ __forceinline__ float compute_r(const RerankArgs& a, int64_t q, uint32_t j) {
+    if (a.mode == SCRUST_MODE_REFERENCE_SNAP)
+        return dist2_reference_snap(a.qx + q * a.d, a.rx + (int64_t)j * a.d, a.d, a.qn2[q], a.rn2[j]);
+    return dist2_f32(a.qx + q * a.d, a.rx + (int64_t)j * a.d, a.d);
+}
+
+// Two sorted FP32 values that the difference form cannot order reliably.
+__device__ __forceinline__ bool tied(const RerankArgs& a, float r1, float r2) {
+    if (a.mode == SCRUST_MODE_REFERENCE_SNAP) return false;
+    float tol = a.gamma * (r1 + r2) + kTieAbs;
+    if (a.metric == SCRUST_METRIC_COSINE)
+        tol += 2.384185791015625e-07f * (sqrtf(r1) + sqrtf(r2)) + 1e-14f;
+    return (r2 - r1) <= tol;
+}
+
+__device__ __forceinline__ double adjudicate(const RerankArgs& a, int64_t q, uint32_t j) {
+    if (a.metric == SCRUST_METRIC_COSINE)
+        return cosine_f64(a.qraw + q * a.d, a.rraw + (int64_t)j * a.d, a.d, a.qn64[q], a.rn64[j]);
+    return sqrt(dist2_f64(a.qraw + q * a.d, a.rraw + (int64_t)j * a.d, a.d));
+}
+
+__device__ __forceinline__ float key_r(unsigned long long key) { return key_float((uint32_t)(key >> 32)); }
+__device__ __forceinline__ uint32_t key_id(unsigned long long key) { return (uint32_t)key; }
+
+// Writes the first k of the sorted candidates keys[0..m), resolving tie
+// groups that reach position k-1 by FP64 (distance, id).
+template <class Team>
+__device__ void finalize_row(const Team& team, const RerankArgs& a, int64_t q,
+                             const unsigned long long* keys, int m, double* dbl) {
+    const int k = a.k;
+    for (int p = team.rank; p < m; p += team.size()) {
+        int gs = p;
+        while (gs > 0 && tied(a, key_r(keys[gs - 1]), key_r(keys[gs]))) gs--;
+        if (gs >= k) continue;
+        int ge = p;
+        while (ge + 1 < m && tied(a, key_r(keys[ge]), key_r(keys[ge + 1]))) ge++;
+        if (ge > gs || a.metric == SCRUST_METRIC_COSINE) dbl[p] = adjudicate(a, q, key_id(keys[p]));
+    }
+    team.sync();
+    for (int p = team.rank; p < m; p += team.size()) {
+        int gs = p;
+        while (gs > 0 && tied(a, key_r(keys[gs - 1]), key_r(keys[gs]))) gs--;
+        if (gs >= k) continue;
+        int ge = p;
+        while (ge + 1 < m && tied(a, key_r(keys[ge]), key_r(keys[ge + 1]))) ge++;
+        const uint32_t id = key_id(keys[p]);
+        int pos = p;
+        if (ge > gs) {
+            const double dv = dbl[p];
+            int rank = 0;
+            for (int o = gs; o <= ge; ++o) {
+                const double dq = dbl[o];
+                const uint32_t io = key_id(keys[o]);
+                rank += (dq < dv) || (dq == dv && io < id);
+            }
+            pos = gs + rank;
+        }
+        if (pos < k) {
+            float dist;
+            if (a.metric == SCRUST_METRIC_COSINE || ge > gs)
+                dist = __double2float_rn(dbl[p]);
+            else
+                dist = sqrtf(key_r(keys[p]));
+            a.out_idx[q * k + pos] = id;
+            a.out_dist[q * k + pos] = dist;
+        }
+    }
+    team.sync();
+}
+
+__device__ void push_fallback(const RerankArgs& a, int64_t q) {
+    uint32_t pos = atomicAdd(a.fb_count, 1u);
+    a.fb_rows[pos] = (uint32_t)q;
+}
+
+__global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a) {
+    extern __shared__ unsigned long long rr_smem[];
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    unsigned long long* A = rr_smem + (size_t)warp * 2 * RC;
+    unsigned long long* B = A + RC;
+    const int64_t q = (int64_t)blockIdx.x * RR_WARPS + warp;
+    if (q >= a.nq) return;
+    WarpTeam team;
+    if (a.lists.overflow[q]) {
+        if (lane == 0) push_fallback(a, q);
+        return;
+    }
+    const int segs = a.lists.segments;
+    int m0 = 0;
+    for (int s = 0; s < segs; ++s) m0 += (int)min(a.lists.cnt[q * segs + s], (uint32_t)a.lists.ctot);
+    if (m0 > RC || m0 < a.k) {
+        if (lane == 0) push_fallback(a, q);
+        return;
+    }
+    int off = 0;
+    for (int s = 0; s < segs; ++s) {
+        const int c = (int)min(a.lists.cnt[q * segs + s], (uint32_t)a.lists.ctot);
+        const int64_t base = (q * segs + s) * (int64_t)a.lists.ctot;
+        for (int p = lane; p < c; p += 32) {
+            uint32_t id = a.lists.ids[base + p];
+            float v = a.lists.vals[base + p];
+            if ((int64_t)id >= a.nr) {  // never written by a candidate kernel: refuse to read it
+                atomicExch(a.err + DERR_CANDIDATES, 1);
+                id = 0;
+                v = __int_as_float(0x7f800000);
+            }
+            A[off + p] = ((unsigned long long)float_key(v) << 32) | id;
+        }
+        off += c;
+    }
+    __syncwarp();
+    const uint32_t kth = team_select_hi(team, A, m0, a.k);
+    const float theta = key_float(kth) + a.margin[q];
+    int m = 0;
+    for (int b0 = 0; b0 < m0; b0 += 32) {
+        const int p = b0 + lane;
+        bool keep = false;
+        uint32_t id = 0;
+        if (p < m0) {
+            const unsigned long long kk = A[p];
+            keep = key_r(kk) < theta;
+            id = key_id(kk);
+        }
+        const uint32_t ballot = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+            const float r = compute_r(a, q, id);
+            B[m + __popc(ballot & lanemask_lt())] = ((unsigned long long)float_key(r) << 32) | id;
+        }
+        m += __popc(ballot);
+    }
+    __syncwarp();
+    const int P = next_pow2(m);
+    for (int p = m + lane; p < P; p += 32) B[p] = ~0ull;
+    __syncwarp();
+    team_bitonic_sort(team, B, P);
+    finalize_row(team, a, q, B, m, reinterpret_cast<double*>(A));
+}
+
+// One block per row, over every reference row: used for rows whose
+// candidate lists overflowed (many cells within the margin, e.g. duplicates).
+__global__ void __launch_bounds__(FB_THREADS) rerank_fallback_kernel(RerankArgs a) {
+    extern __shared__ unsigned long long fb_smem[];
+    unsigned long long* keys = fb_smem;
+    double* dbl = reinterpret_cast<double*>(fb_smem + FB_CAP);
+    __shared__ int scratch;
+    __shared__ uint32_t row_s;
+    __shared__ uint32_t hist[256];
+    __shared__ uint32_t sel_prefix;
+    __shared__ int sel_rank;
+    __shared__ int cnt_s;
+    BlockTeam team(&scratch);
+    const int tid = threadIdx.x;
+    float* sc = a.fb_scratch + (int64_t)blockIdx.x * a.nr;
+    for (;;) {
+        if (tid == 0) {
+            const uint32_t i = atomicAdd(a.fb_next, 1u);
+            row_s = i < *a.fb_count ? a.fb_rows[i] : 0xffffffffu;
+        }
+        __syncthreads();
+        const uint32_t row = row_s;
+        __syncthreads();
+        if (row == 0xffffffffu) break;
+        const int64_t q = row;
+        for (int64_t j = tid; j < a.nr; j += blockDim.x)
+            sc[j] = (a.self && j == q) ? __int_as_float(0x7f800000) : compute_r(a, q, (uint32_t)j);
+        __syncthreads();
+        // k-th smallest of the row: four 8-bit radix passes.
+        if (tid == 0) {
+            sel_prefix = 0;
+            sel_rank = a.k;
+        }
+        uint32_t mask = 0;
+        for (int pass = 0; pass < 4; ++pass) {
+            const int shift = 24 - 8 * pass;
+            hist[tid] = 0;
+            __syncthreads();
+            const uint32_t prefix = sel_prefix;
+            for (int64_t j = tid; j < a.nr; j += blockDim.x) {
+                const uint32_t key = float_key(sc[j]);
+                if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+            }
+            __syncthreads();
+            if (tid == 0) {
+                int rank = sel_rank;
+                uint32_t b = 0;
+                for (; b < 256; ++b) {
+                    if ((int)hist[b] >= rank) break;
+                    rank -= (int)hist[b];
+                }
+                sel_rank = rank;
+                sel_prefix = prefix | (b << shift);
+            }
+            mask |= 255u << shift;
+            __syncthreads();
+        }
+        const float vk = key_float(sel_prefix);
+        float T = vk;
+        if (a.mode != SCRUST_MODE_REFERENCE_SNAP) T = vk + 4.0f * (a.gamma * 2.0f * vk + kTieAbs) +
+                                                      (a.metric == SCRUST_METRIC_COSINE ? 1e-6f : 0.0f);
+        int m = 0;
+        for (int attempt = 0; attempt < 8; ++attempt) {
+            if (tid == 0) cnt_s = 0;
+            __syncthreads();
+            for (int64_t j = tid; j < a.nr; j += blockDim.x) {
+                const float r = sc[j];
+                if (r <= T) {
+                    const int pos = atomicAdd(&cnt_s, 1);
+                    if (pos < FB_CAP) keys[pos] = ((unsigned long long)float_key(r) << 32) | (uint32_t)j;
+                }
+            }
+            __syncthreads();
+            m = cnt_s;
+            if (m > FB_CAP) break;
+            const int P = next_pow2(m);
+            for (int p = m + tid; p < P; p += blockDim.x) keys[p] = ~0ull;
+            __syncthreads();
+            team_bitonic_sort(team, keys, P);
+            if (a.mode == SCRUST_MODE_REFERENCE_SNAP) break;
+            // If the tie group holding the last collected candidate reaches
+            // position k-1, make sure nothing just outside T could join it.
+            const float rl = key_r(keys[m - 1]);
+            int gs = m - 1;
+            while (gs > 0 && tied(a, key_r(keys[gs - 1]), key_r(keys[gs]))) gs--;
+            if (gs >= a.k) break;
+            const float T2 = rl + 2.0f * (a.gamma * 2.0f * rl + kTieAbs) +
+                             (a.metric == SCRUST_METRIC_COSINE ? 1e-6f : 0.0f);
+            int outside = 0;
+            for (int64_t j = tid; j < a.nr; j += blockDim.x) outside += (sc[j] > T && sc[j] <= T2);
+            if (team.sum(outside) == 0) break;
+            T = T2;
+        }
+        if (m > FB_CAP || m < a.k) {
+            if (tid == 0) atomicExch(a.err + (m > FB_CAP ? DERR_TIE_OVERFLOW : DERR_CANDIDATES), 1);
+            __syncthreads();
+            continue;
+        }
+        finalize_row(team, a, q, keys, m, dbl);
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float* qx,
+                          const float* rx, const float* qnorm2, const float* rnorm2,
+                          const double* qn64, const double* rn64, const float* qraw,
+                          const float* rraw, const float* margin, const Lists& lists,
+                          uint32_t* out_idx, float* out_dist) {
+    cudaError_t e;
+    uint32_t* fb_rows = (uint32_t*)ws_get(ctx, SLOT_FALLBACK_ROWS, sizeof(uint32_t) * (size_t)plan.nq, &e);
+    if (!fb_rows) return e;
+    float* fb_scratch =
+        (float*)ws_get(ctx, SLOT_FALLBACK_SCRATCH, sizeof(float) * (size_t)plan.nr * FB_BLOCKS, &e);
+    if (!fb_scratch) return e;
+    RerankArgs a;
+    a.qx = qx;
+    a.rx = rx;
+    a.qn2 = qnorm2;
+    a.rn2 = rnorm2;
+    a.qn64 = qn64;
+    a.rn64 = rn64;
+    a.qraw = qraw;
+    a.rraw = rraw;
+    a.margin = margin;
+    a.lists = lists;
+    a.nq = plan.nq;
+    a.nr = plan.nr;
+    a.d = plan.d;
+    a.k = plan.k;
+    a.mode = plan.mode;
+    a.metric = plan.metric;
+    a.self = plan.self ? 1 : 0;
+    a.gamma = dist2_f32_gamma(plan.d);
+    a.out_idx = out_idx;
+    a.out_dist = out_dist;
+    a.fb_rows = fb_rows;
+    a.fb_count = ctx->d_counter;
+    a.fb_next = ctx->d_counter + 1;
+    a.fb_scratch = fb_scratch;
+    a.err = ctx->d_err;
+    e = cudaMemsetAsync(ctx->d_counter, 0, 2 * sizeof(uint32_t), ctx->stream);
+    if (e != cudaSuccess) return e;
+    const size_t smem_w = (size_t)RR_WARPS * 2 * RC * sizeof(unsigned long long);
+    e = cudaFuncSetAttribute(rerank_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_w);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = (unsigned)((plan.nq + RR_WARPS - 1) / RR_WARPS);
+    rerank_warp_kernel<<<blocks, RR_WARPS * 32, smem_w, ctx->stream>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const size_t smem_f = (size_t)FB_CAP * (sizeof(unsigned long long) + sizeof(double));
+    e = cudaFuncSetAttribute(rerank_fallback_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
+    if (e != cudaSuccess) return e;
+    rerank_fallback_kernel<<<FB_BLOCKS, FB_THREADS, smem_f, ctx->stream>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace scrust

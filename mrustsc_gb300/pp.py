@@ -1,0 +1,43 @@
+"""``pp.neighbors`` with the reference's surface (python/scrust/pp/_basics.py:186-215),
+plus the ``metric`` keyword the scanpy API has ("euclidean" or "cosine").
+
+Stores ``obsp["distances"]`` (one fixed-width row per cell, nearest first,
+stored zeros kept), ``obsp["connectivities"]`` (UMAP fuzzy union) and
+``uns["neighbors"]`` exactly as the reference does.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from ._shared import _INDEX_DTYPE, _VALUE_DTYPE, _csr_from_parts, _extension, _representation
+
+METRICS = ("euclidean", "cosine")
+
+
+def neighbors(adata, *, n_neighbors: int = 15, use_rep: str = "X_pca", device: str = "auto",
+              metric: str = "euclidean", form: str = "plain") -> None:
+    """Build the k-nearest-neighbour graph and its UMAP connectivities."""
+    if n_neighbors < 2:
+        raise ValueError(f"n_neighbors must be at least 2, got {n_neighbors}")
+    if metric not in METRICS:
+        raise ValueError(f"metric must be one of {list(METRICS)}, got {metric!r}")
+    extension = _extension()
+    # scanpy counts the cell itself among its n_neighbors; the core does not.
+    kwargs = {} if metric == "euclidean" and form == "plain" else {"metric": metric, "form": form}
+    indices, distances = extension.knn(_representation(adata, use_rep), n_neighbors - 1, device, **kwargs)
+    indices = np.asarray(indices)
+    distances = np.asarray(distances, dtype=_VALUE_DTYPE)
+
+    n_obs, k = indices.shape
+    indptr = np.arange(0, n_obs * k + 1, k, dtype=_INDEX_DTYPE)
+    adata.obsp["distances"] = _csr_from_parts((indptr, indices.ravel(), distances.ravel()), (n_obs, n_obs))
+    adata.obsp["connectivities"] = _csr_from_parts(extension.connectivities(indices, distances), (n_obs, n_obs))
+    params = {"n_neighbors": n_neighbors, "method": "umap", "use_rep": use_rep}
+    if metric != "euclidean":
+        params["metric"] = metric
+    adata.uns["neighbors"] = {
+        "connectivities_key": "connectivities",
+        "distances_key": "distances",
+        "params": params,
+    }

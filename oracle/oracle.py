@@ -1,0 +1,220 @@
+"""The oracle for the pp.neighbors path -- TEST INFRASTRUCTURE ONLY.
+
+ctypes access to ``neighbors_oracle.c`` (a C restatement of the reference's
+CPU path, the CPU twin of its Metal kernel, and the FP64 exact kNN).  Only the
+tests, the smoke entry point and bench.py's CPU-baseline leg import this
+module, and only as the checker or as the timed CPU baseline.  The shipped
+library never imports it.
+
+Functions mirror the reference files they restate:
+  knn_reference_cpu  crates/scrust-core/src/neighbors.rs:29-101, 171-191
+  knn_metal_twin     crates/scrust-gpu/src/kernels/knn.rs:135-158, 282-313
+  knn_fp64           tests/test_neighbors_audit.py:52-61
+  smooth_knn         crates/scrust-core/src/neighbors.rs:239-298
+  connectivities     crates/scrust-core/src/neighbors.rs:208-372
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import pathlib
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = pathlib.Path(__file__).resolve().parent
+_SRC = _HERE / "neighbors_oracle.c"
+_OUT = _HERE / "_build" / "liboracle.so"
+_LOCK = threading.Lock()
+_LIB = None
+
+OK, SHAPE, INVALID_PARAMETER, OOM = 0, 1, 2, 6
+
+
+class OracleError(ValueError):
+    """An argument the reference would reject (Shape / InvalidParameter)."""
+
+
+def build(force: bool = False) -> pathlib.Path:
+    """Compile the restatement with gcc (no -march flags: same code on x86 and Arm)."""
+    _OUT.parent.mkdir(parents=True, exist_ok=True)
+    if force or not _OUT.exists() or _OUT.stat().st_mtime < _SRC.stat().st_mtime:
+        tmp = _OUT.with_suffix(f".{os.getpid()}.tmp.so")
+        cmd = [
+            "gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+            str(_SRC), "-o", str(tmp), "-lm",
+        ]
+        subprocess.run(cmd, check=True)
+        os.replace(tmp, _OUT)
+    return _OUT
+
+
+def _lib():
+    global _LIB
+    with _LOCK:
+        if _LIB is None:
+            lib = ctypes.CDLL(str(build()))
+            i64, f32p, u32p, f64p, i64p = (
+                ctypes.c_int64,
+                ctypes.POINTER(ctypes.c_float),
+                ctypes.POINTER(ctypes.c_uint32),
+                ctypes.POINTER(ctypes.c_double),
+                ctypes.POINTER(ctypes.c_int64),
+            )
+            lib.oracle_knn_reference_cpu.argtypes = [f32p, i64, i64, i64, i64, u32p, f32p]
+            lib.oracle_knn_reference_cpu_rows.argtypes = [f32p, i64, i64, i64, i64p, i64, u32p, f32p]
+            lib.oracle_knn_metal_twin.argtypes = [f32p, i64, i64, i64, u32p, f32p]
+            lib.oracle_knn_fp64_rows.argtypes = [f32p, i64, i64, i64, i64p, i64, u32p, f64p, f32p]
+            lib.oracle_knn_cosine_fp64_rows.argtypes = [f32p, i64, i64, i64, i64p, i64, u32p, f64p, f32p]
+            lib.oracle_smooth_knn.argtypes = [f32p, i64, i64, f32p, f32p]
+            lib.oracle_connectivities.argtypes = [u32p, f32p, i64, i64, u32p, u32p, f32p, i64p]
+            lib.oracle_directed_weights.argtypes = [u32p, f32p, i64, i64, f32p]
+            lib.oracle_centred.argtypes = [f32p, i64, i64, f32p]
+            lib.oracle_unrolled_sum_f32.argtypes = [f32p, i64]
+            lib.oracle_unrolled_sum_f32.restype = ctypes.c_float
+            lib.oracle_num_threads.restype = ctypes.c_int
+            _LIB = lib
+    return _LIB
+
+
+def _p(array, ctype):
+    return array.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def _check(rc: int, what: str) -> None:
+    if rc == SHAPE:
+        raise OracleError(f"{what}: shape")
+    if rc == INVALID_PARAMETER:
+        raise OracleError(f"{what}: invalid parameter")
+    if rc != OK:
+        raise MemoryError(f"{what}: status {rc}")
+
+
+def _f32(x) -> np.ndarray:
+    return np.ascontiguousarray(x, dtype=np.float32)
+
+
+def num_threads() -> int:
+    return int(_lib().oracle_num_threads())
+
+
+def knn_reference_cpu(x, k: int, tile_rows: int = 0):
+    """The reference CPU kNN (expansion form, snap, (d^2, id) order)."""
+    x = _f32(x)
+    n, d = x.shape if x.ndim == 2 else (0, 0)
+    idx = np.zeros((max(n, 1), max(k, 1)), np.uint32)
+    dist = np.zeros((max(n, 1), max(k, 1)), np.float32)
+    _check(_lib().oracle_knn_reference_cpu(_p(x, ctypes.c_float), n, d, k, tile_rows,
+                                           _p(idx, ctypes.c_uint32), _p(dist, ctypes.c_float)),
+           "knn_reference_cpu")
+    return idx[:n, :k], dist[:n, :k]
+
+
+def knn_reference_cpu_rows(x, k: int, rows):
+    """The reference CPU kNN for the query rows `rows`, each against all cells."""
+    x = _f32(x)
+    n, d = x.shape
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    idx = np.zeros((len(rows), k), np.uint32)
+    dist = np.zeros((len(rows), k), np.float32)
+    _check(_lib().oracle_knn_reference_cpu_rows(_p(x, ctypes.c_float), n, d, k,
+                                                _p(rows, ctypes.c_int64), len(rows),
+                                                _p(idx, ctypes.c_uint32), _p(dist, ctypes.c_float)),
+           "knn_reference_cpu_rows")
+    return idx, dist
+
+
+def knn_metal_twin(x, k: int):
+    """CPU twin of the reference Metal kernel (difference form on centred data + snap)."""
+    x = _f32(x)
+    n, d = x.shape if x.ndim == 2 else (0, 0)
+    idx = np.zeros((max(n, 1), max(k, 1)), np.uint32)
+    dist = np.zeros((max(n, 1), max(k, 1)), np.float32)
+    _check(_lib().oracle_knn_metal_twin(_p(x, ctypes.c_float), n, d, k,
+                                        _p(idx, ctypes.c_uint32), _p(dist, ctypes.c_float)),
+           "knn_metal_twin")
+    return idx[:n, :k], dist[:n, :k]
+
+
+def knn_fp64(x, k: int, rows=None, metric: str = "euclidean"):
+    """FP64 exact kNN: (idx u32, d64 f64, dist f32) for `rows` (default all)."""
+    x = _f32(x)
+    n, d = x.shape
+    if rows is None:
+        nrows, rows_p = n, None
+    else:
+        rows = np.ascontiguousarray(rows, dtype=np.int64)
+        nrows, rows_p = len(rows), _p(rows, ctypes.c_int64)
+    idx = np.zeros((nrows, k), np.uint32)
+    d64 = np.zeros((nrows, k), np.float64)
+    dist = np.zeros((nrows, k), np.float32)
+    fn = _lib().oracle_knn_fp64_rows if metric == "euclidean" else _lib().oracle_knn_cosine_fp64_rows
+    _check(fn(_p(x, ctypes.c_float), n, d, k, rows_p, nrows, _p(idx, ctypes.c_uint32),
+              _p(d64, ctypes.c_double), _p(dist, ctypes.c_float)), "knn_fp64")
+    return idx, d64, dist
+
+
+def smooth_knn(distances):
+    dist = _f32(distances)
+    n, k = dist.shape
+    sig = np.zeros(n, np.float32)
+    rho = np.zeros(n, np.float32)
+    _check(_lib().oracle_smooth_knn(_p(dist, ctypes.c_float), n, k, _p(sig, ctypes.c_float),
+                                    _p(rho, ctypes.c_float)), "smooth_knn")
+    return sig, rho
+
+
+def directed_weights(indices, distances):
+    idx = np.ascontiguousarray(indices, dtype=np.uint32)
+    dist = _f32(distances)
+    n, k = dist.shape
+    w = np.zeros((n, k), np.float32)
+    _check(_lib().oracle_directed_weights(_p(idx, ctypes.c_uint32), _p(dist, ctypes.c_float), n, k,
+                                          _p(w, ctypes.c_float)), "directed_weights")
+    return w
+
+
+def connectivities(indices, distances):
+    """(indptr u32, indices u32, values f32, n_cols), the reference's return shape."""
+    idx = np.ascontiguousarray(indices, dtype=np.uint32)
+    dist = _f32(distances)
+    if idx.shape != dist.shape or idx.ndim != 2:
+        raise OracleError("connectivities: shape")
+    n, k = dist.shape
+    indptr = np.zeros(n + 1, np.uint32)
+    cols = np.zeros(max(2 * n * k, 1), np.uint32)
+    vals = np.zeros(max(2 * n * k, 1), np.float32)
+    nnz = np.zeros(1, np.int64)
+    _check(_lib().oracle_connectivities(_p(idx, ctypes.c_uint32), _p(dist, ctypes.c_float), n, k,
+                                        _p(indptr, ctypes.c_uint32), _p(cols, ctypes.c_uint32),
+                                        _p(vals, ctypes.c_float), _p(nnz, ctypes.c_int64)),
+           "connectivities")
+    m = int(nnz[0])
+    return indptr, cols[:m].copy(), vals[:m].copy(), n
+
+
+def centred(x):
+    x = _f32(x)
+    out = np.zeros_like(x)
+    _check(_lib().oracle_centred(_p(x, ctypes.c_float), x.shape[0], x.shape[1],
+                                 _p(out, ctypes.c_float)), "centred")
+    return out
+
+
+def unrolled_sum(x) -> np.float32:
+    x = _f32(np.ravel(x))
+    return np.float32(_lib().oracle_unrolled_sum_f32(_p(x, ctypes.c_float), x.size))
+
+
+def exact_knn_numpy(x, k: int):
+    """tests/test_neighbors_audit.py:52-61 verbatim in semantics (numpy, small n only)."""
+    x64 = np.asarray(x, dtype=np.float64)
+    d = np.sqrt(np.maximum(((x64[:, None, :] - x64[None, :, :]) ** 2).sum(-1), 0.0))
+    n = d.shape[0]
+    indices = np.zeros((n, k), dtype=np.int64)
+    for cell in range(n):
+        order = sorted((j for j in range(n) if j != cell), key=lambda j: (d[cell, j], j))
+        indices[cell] = order[:k]
+    return indices, np.take_along_axis(d, indices, 1)

@@ -1,0 +1,80 @@
+"""Regenerate the golden fixtures in this folder from the reference's own tests.
+
+Run once in a container that has the reference checkout:
+
+    python tests/golden/make_golden.py /root/reference
+
+It reads the scanpy constants the reference pins in
+crates/scrust-core/src/neighbors.rs:498-544 (ten sample cells of
+`reference_embedding(300, 20, 42)` with their scanpy neighbour rows and
+connectivity rows, and the exact nnz / weight sum / square sum of the whole
+matrix) and writes them, unchanged, to `scanpy_reference_embedding_300x20.json`.
+The values are parsed from the source text, not re-typed.
+"""
+
+from __future__ import annotations
+
+import json
+import pathlib
+import re
+import sys
+
+HERE = pathlib.Path(__file__).resolve().parent
+
+
+def _block(text: str, name: str) -> str:
+    start = text.index(name)
+    eq = text.index("=", start)
+    end = text.index("];", eq)
+    return text[eq + 1 : end + 1]
+
+
+def _rust_float(token: str) -> float:
+    return float(token.replace("_", ""))
+
+
+def parse(neighbors_rs: str) -> dict:
+    cells = [int(v) for v in re.findall(r"\d+", _block(neighbors_rs, "SCANPY_SAMPLE_CELLS"))]
+    nb_block = _block(neighbors_rs, "SCANPY_NEIGHBORS")
+    rows = re.findall(r"\[([\d,\s]+)\]", nb_block)
+    neighbours = [[int(v) for v in re.findall(r"\d+", row)] for row in rows]
+    conn_block = _block(neighbors_rs, "SCANPY_CONNECTIVITY_ROWS")
+    conn_rows = []
+    for row in re.findall(r"&\[(.*?)\]", conn_block, flags=re.S):
+        pairs = re.findall(r"\((\d+),\s*([0-9eE_.+-]+)\)", row)
+        conn_rows.append([[int(c), _rust_float(v)] for c, v in pairs])
+    nnz = int(re.search(r"SCANPY_NNZ:\s*usize\s*=\s*([\d_]+)", neighbors_rs).group(1).replace("_", ""))
+    wsum = _rust_float(re.search(r"SCANPY_WEIGHT_SUM:\s*f32\s*=\s*([0-9eE_.+-]+);", neighbors_rs).group(1))
+    wsq = _rust_float(
+        re.search(r"SCANPY_WEIGHT_SQUARE_SUM:\s*f32\s*=\s*([0-9eE_.+-]+);", neighbors_rs).group(1)
+    )
+    assert len(cells) == 10 and len(neighbours) == 10 and len(conn_rows) == 10
+    assert all(len(r) == 14 for r in neighbours)
+    return {
+        "source": "crates/scrust-core/src/neighbors.rs:493-544",
+        "embedding": {"generator": "splitmix64", "n_cells": 300, "n_dims": 20, "seed": 42},
+        "k": 14,
+        "sample_cells": cells,
+        "scanpy_neighbors": neighbours,
+        "scanpy_connectivity_rows": conn_rows,
+        "nnz": nnz,
+        "weight_sum": wsum,
+        "weight_square_sum": wsq,
+        "bars": {
+            "neighbour_overlap_min_fraction": 0.9,
+            "connectivity_relative_tolerance": 1e-3,
+            "source": "crates/scrust-core/src/neighbors.rs:546-590",
+        },
+    }
+
+
+def main(argv: list[str]) -> None:
+    root = pathlib.Path(argv[1] if len(argv) > 1 else "/root/reference")
+    text = (root / "crates/scrust-core/src/neighbors.rs").read_text()
+    out = HERE / "scanpy_reference_embedding_300x20.json"
+    out.write_text(json.dumps(parse(text), indent=1) + "\n")
+    print(f"wrote {out}")
+
+
+if __name__ == "__main__":
+    main(sys.argv)

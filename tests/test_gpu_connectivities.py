@@ -1,0 +1,135 @@
+"""Connectivities on the GPU against the oracle's restatement of
+crates/scrust-core/src/neighbors.rs:208-372: CSR structure bit-exact, values
+within 1e-5 absolute, sigma/rho within 1e-5 relative; plus the reference's own
+golden vectors (neighbors.rs:498-590) and invariants (:468-491), and the
+pp.neighbors surface end to end."""
+
+from __future__ import annotations
+
+import json
+import pathlib
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import refdata
+from mrustsc_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+CONN_ATOL = 1e-5
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden" / "scanpy_reference_embedding_300x20.json"
+
+
+@pytest.fixture(scope="module")
+def scrust(built_library):
+    from mrustsc_gb300 import _scrust
+
+    assert _scrust.gpu_available(), "these tests need an sm_103a GPU"
+    return _scrust
+
+
+def assert_same_csr(ours, ref, atol=CONN_ATOL):
+    np.testing.assert_array_equal(ours[0], ref[0])
+    np.testing.assert_array_equal(ours[1], ref[1])
+    np.testing.assert_allclose(ours[2], ref[2], rtol=0, atol=atol)
+    assert ours[3] == ref[3]
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_connectivities_match_the_oracle(scrust, oracle, seed):
+    x = synthetic.plain_small(seed=seed)
+    idx, dist = scrust.knn(x, 14, "auto")
+    ours = scrust.connectivities(idx, dist)
+    assert_same_csr(ours, oracle.connectivities(idx, dist))
+    # and against the graph built from the FP64 kNN
+    fi, _, fd = oracle.knn_fp64(x, 14)
+    assert_same_csr(ours, oracle.connectivities(fi, fd))
+
+
+def test_smooth_knn_matches_the_oracle(scrust, oracle):
+    x = synthetic.plain_small(seed=2)
+    _, dist = scrust.knn(x, 15, "auto")
+    s_gpu, r_gpu = scrust.smooth_knn_distances(dist)
+    s_ref, r_ref = oracle.smooth_knn(dist)
+    np.testing.assert_array_equal(r_gpu, r_ref)
+    np.testing.assert_allclose(s_gpu, s_ref, rtol=1e-5)
+
+
+def test_scanpy_golden_vectors_through_the_gpu(scrust):
+    g = json.loads(GOLDEN.read_text())
+    e = g["embedding"]
+    x = refdata.reference_embedding(e["n_cells"], e["n_dims"], e["seed"])
+    idx, dist = scrust.knn(x, g["k"], "auto")
+    for cell, expected in zip(g["sample_cells"], g["scanpy_neighbors"]):
+        assert len(set(idx[cell].tolist()) & set(expected)) * 10 >= g["k"] * 9
+    indptr, cols, vals, n = scrust.connectivities(idx, dist)
+    for cell, row in zip(g["sample_cells"], g["scanpy_connectivity_rows"]):
+        ours = dict(zip(cols[indptr[cell]:indptr[cell + 1]].tolist(), vals[indptr[cell]:indptr[cell + 1]].tolist()))
+        for c, v in row:
+            if c in ours:
+                assert abs(ours[c] - v) <= 1e-3 * abs(v)
+    assert len(vals) == g["nnz"]
+    assert abs(float(vals.sum(dtype=np.float32)) - g["weight_sum"]) <= 1e-3 * g["weight_sum"]
+    assert abs(float((vals * vals).sum(dtype=np.float32)) - g["weight_square_sum"]) <= 1e-3 * g["weight_square_sum"]
+
+
+def test_symmetric_with_an_empty_diagonal(scrust):
+    idx, dist = scrust.knn(refdata.reference_embedding(120, 5, 3), 10, "auto")
+    indptr, cols, vals, n = scrust.connectivities(idx, dist)
+    m = sp.csr_matrix((vals, cols, indptr), shape=(n, n))
+    assert m.diagonal().max() == 0
+    assert abs(m - m.T).max() < 1e-6
+    assert vals.min() > 0 and vals.max() <= 1
+    for r in range(n):
+        assert np.all(np.diff(cols[indptr[r]:indptr[r + 1]].astype(np.int64)) > 0)
+
+
+def test_rejects_a_degenerate_graph(scrust):
+    with pytest.raises(ValueError, match="out-of-range"):
+        scrust.connectivities(np.array([[1], [9]], np.uint32), np.ones((2, 1), np.float32))
+    with pytest.raises(ValueError):
+        scrust.connectivities(np.zeros((0, 3), np.uint32), np.zeros((0, 3), np.float32))
+
+
+@pytest.mark.parametrize("k", [2, 5, 14, 30])
+def test_various_k_and_duplicate_rows(scrust, oracle, k):
+    x = refdata.audit_embedding(240, 10, 11)
+    x[:20] = x[0]
+    x[20:25] = x[0] + (np.random.default_rng(6).normal(size=(5, 10)) * 1e-2).astype(np.float32)
+    idx, dist = scrust.knn(x, k, "auto")
+    assert_same_csr(scrust.connectivities(idx, dist), oracle.connectivities(idx, dist))
+
+
+def test_arbitrary_graph_input(scrust, oracle):
+    rng = np.random.default_rng(3)
+    n, k = 500, 7
+    idx = rng.integers(0, n, size=(n, k)).astype(np.uint32)
+    dist = np.sort(rng.random((n, k)).astype(np.float32), axis=1)
+    assert_same_csr(scrust.connectivities(idx, dist), oracle.connectivities(idx, dist))
+
+
+def test_neighbors_graph_in_one_pass(scrust, oracle):
+    x = synthetic.plain_small(seed=4)
+    idx, dist, conn = scrust.neighbors_graph(x, 15)
+    i2, d2 = scrust.knn(x, 15, "auto")
+    np.testing.assert_array_equal(idx, i2)
+    np.testing.assert_array_equal(dist, d2)
+    assert_same_csr(conn, oracle.connectivities(idx, dist))
+
+
+def test_pp_neighbors_end_to_end(oracle):
+    from mrustsc_gb300 import pp
+    from mrustsc_gb300.anndata_lite import AnnData
+
+    x = refdata.audit_embedding()
+    adata = AnnData(np.zeros((x.shape[0], 3), np.float32), obsm={"X_pca": x})
+    pp.neighbors(adata, n_neighbors=15, use_rep="X_pca")
+    d = adata.obsp["distances"]
+    assert np.all(np.diff(d.indptr) == 14)
+    ei, _, _ = oracle.knn_fp64(x, 14)
+    np.testing.assert_array_equal(d.indices.reshape(-1, 14), ei)
+    c = adata.obsp["connectivities"]
+    assert np.count_nonzero(c.diagonal()) == 0
+    assert adata.uns["neighbors"]["params"] == {"n_neighbors": 15, "method": "umap", "use_rep": "X_pca"}
