@@ -181,6 +181,22 @@ SCRUST_API void scrust_csr_free(scrust_csr* csr);
 /* Blocks until the context stream is idle; reports a pending kernel error. */
 SCRUST_API int32_t scrust_cuda_synchronize(scrust_context* context, scrust_status* status);
 
+/* No counterpart in the reference.  scrust_cuda_smooth_knn_distances for
+ * callers that cannot let a library allocate device memory -- processes whose
+ * own pool allocator owns the GPU's memory, or services that reserve their
+ * HBM budget up front -- on device pointers they own: `distances` (n x k),
+ * `sigmas` and `rhos` (n).  The computation's only scratch is a fixed 33 KB
+ * array compiled into the library (held by every GPU that loads it until the
+ * process exits), so n * k is limited to 16,777,216; larger inputs return
+ * SCRUST_INVALID_PARAMETER.  Enqueued on `stream` (a cudaStream_t; NULL is
+ * the legacy default stream) without synchronising.  The first call on each
+ * device looks up the array's device address, so make it before any stream
+ * capture.  All calls on a device share the array: calls that overlap on the
+ * GPU race on it and must be ordered by the caller. */
+SCRUST_API int32_t scrust_cuda_smooth_knn_distances_noalloc(const float* distances, uint64_t n, uint32_t k,
+                                                            float* sigmas, float* rhos, void* stream,
+                                                            scrust_status* status);
+
 /* Phase timing.  When enabled, each kNN / connectivities call records CUDA
  * events on the context stream around its phases; scrust_cuda_phase_times
  * writes the last call's milliseconds (after a synchronise) in the order

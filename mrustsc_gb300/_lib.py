@@ -102,6 +102,8 @@ _SIGNATURES = {
     "scrust_csr_values": (_P, [_P]),
     "scrust_csr_free": (None, [_P]),
     "scrust_cuda_synchronize": (ctypes.c_int32, [_P, ctypes.POINTER(Status)]),
+    "scrust_cuda_smooth_knn_distances_noalloc": (ctypes.c_int32, [_P, ctypes.c_uint64, ctypes.c_uint32, _P, _P,
+                                                                   _P, ctypes.POINTER(Status)]),
     "scrust_cuda_set_timing": (None, [_P, ctypes.c_int32]),
     "scrust_cuda_phase_times": (ctypes.c_int32, [_P, ctypes.POINTER(ctypes.c_float), ctypes.c_int32]),
     "scrust_cuda_launch_count": (ctypes.c_uint64, [_P]),
