@@ -21,6 +21,7 @@ LIB_PATH = pathlib.Path(__file__).resolve().parent / "libscrust_cuda.so"
 OK, SHAPE, INVALID_PARAMETER, NO_GPU, KERNEL, NOT_CONVERGED, OOM, TIMEOUT = range(8)
 
 FORM_PLAIN, FORM_TENSOR = 0, 1
+TENSOR_FORM_READY = True
 METRIC_EUCLIDEAN, METRIC_COSINE = 0, 1
 MODE_EXACT, MODE_REFERENCE_SNAP = 0, 1
 PRECISION_FP16, PRECISION_BF16 = 0, 1

@@ -154,6 +154,53 @@ struct KnnBuffers {
     float* norm2 = nullptr;
 };
 
+// Candidate-list geometry: column segments per row block (so small inputs
+// still fill the GPU) and the list capacity that triggers a prune.
+int32_t plan_lists(scrust_context* ctx, const scrust_knn_options& o, int k, int row_blocks, int col_tiles,
+                   int blocks_wanted, int headroom, Lists* lists, scrust_status* st) {
+    int segments = 1;
+    if (o.segments) {
+        segments = (int)o.segments;
+    } else if (row_blocks < blocks_wanted) {
+        segments = (blocks_wanted + row_blocks - 1) / row_blocks;
+        segments = std::min(segments, std::max(1, kRerankCapacity / (4 * k)));
+    }
+    segments = std::max(1, std::min(segments, col_tiles));
+    const int per = (col_tiles + segments - 1) / segments;
+    segments = (col_tiles + per - 1) / per;  // no empty segment
+    int cap = (int)o.list_capacity;
+    if (cap == 0) cap = std::max(64, (2 * k + 32 + 31) / 32 * 32);
+    cap = std::max(cap, k + 32);
+    const int ctot = cap + headroom;
+    if (ctot > 512)
+        return fail(st, SCRUST_INVALID_PARAMETER, "list_capacity must be at most %d, got %d", 512 - headroom, cap);
+    lists->cap = cap;
+    lists->ctot = ctot;
+    lists->segments = segments;
+    (void)ctx;
+    return SCRUST_OK;
+}
+
+int32_t alloc_lists(scrust_context* ctx, int64_t rows_pad, Lists* lists, scrust_status* st) {
+    cudaError_t e = cudaSuccess;
+    const size_t slots = (size_t)rows_pad * lists->segments;
+    lists->ids = (uint32_t*)ws_get(ctx, SLOT_LIST_IDS, sizeof(uint32_t) * slots * lists->ctot, &e);
+    lists->vals = (float*)ws_get(ctx, SLOT_LIST_VALS, sizeof(float) * slots * lists->ctot, &e);
+    lists->cnt = (uint32_t*)ws_get(ctx, SLOT_LIST_CNT, sizeof(uint32_t) * slots, &e);
+    lists->overflow = (uint32_t*)ws_get(ctx, SLOT_OVERFLOW, sizeof(uint32_t) * (size_t)rows_pad, &e);
+    if (!lists->ids || !lists->vals || !lists->cnt || !lists->overflow) return cuda_fail(st, e, "workspace");
+    if ((e = cudaMemsetAsync(lists->overflow, 0, sizeof(uint32_t) * (size_t)rows_pad, ctx->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(lists->cnt, 0, sizeof(uint32_t) * slots, ctx->stream)) != cudaSuccess)
+        return cuda_fail(st, e, "memset");
+    return SCRUST_OK;
+}
+
+// Whether a solve runs the tensor form: it is asked for, the mode is exact,
+// and the row plus the three norm columns fits one 64-wide operand row.
+bool uses_tensor_form(const scrust_knn_options& o, int d) {
+    return o.form == SCRUST_FORM_TENSOR && o.mode == SCRUST_MODE_EXACT && d + 3 <= 64;
+}
+
 // The kNN solve on device pointers, enqueued on ctx->stream.
 int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint64_t d64, uint32_t k,
                         const scrust_knn_options* opt, uint32_t* out_idx, float* out_dist,
@@ -173,10 +220,11 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
     plan.precision = o.precision;
     const int64_t n = plan.nq;
     const int d = plan.d;
-    const int64_t n_pad = (n + 127) / 128 * 128;
-    const int dp = d <= 64 ? (d + 3) / 4 * 4 : (d + 63) / 64 * 64;
     const bool ref = o.mode == SCRUST_MODE_REFERENCE_SNAP;
     const bool cosine = o.metric == SCRUST_METRIC_COSINE;
+    const bool tensor = uses_tensor_form(o, d);
+    const int64_t n_pad = tensor ? (n + 255) / 256 * 256 : (n + 127) / 128 * 128;
+    const int dp = d <= 64 ? (d + 3) / 4 * 4 : (d + 63) / 64 * 64;
     cudaStream_t s = ctx->stream;
 
     const float* xwork = x;
@@ -197,69 +245,76 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
     }
     const int mean_blocks = (int)((n + 2047) / 2048);
     double* means = (double*)ws_get(ctx, SLOT_MEANS, sizeof(double) * ((size_t)d * (mean_blocks + 1)), &e);
-    float* coords_t = (float*)ws_get(ctx, SLOT_COORDS_T, sizeof(float) * (size_t)dp * n_pad, &e);
     float* norm2 = (float*)ws_get(ctx, SLOT_NORM2, sizeof(float) * (size_t)n_pad, &e);
     float* cnorm = (float*)ws_get(ctx, SLOT_CNORM, sizeof(float) * (size_t)n_pad, &e);
     float* margin = (float*)ws_get(ctx, SLOT_MARGIN, sizeof(float) * (size_t)n_pad + 64, &e);
-    if (!means || !coords_t || !norm2 || !cnorm || !margin) return cuda_fail(st, e, "workspace");
-    uint32_t* max_bits = (uint32_t*)(margin + n_pad);  // two spare words
-    if ((e = cudaMemsetAsync(max_bits, 0, 2 * sizeof(uint32_t), s)) != cudaSuccess) return cuda_fail(st, e, "memset");
+    if (!means || !norm2 || !cnorm || !margin) return cuda_fail(st, e, "workspace");
+    uint32_t* max_bits = (uint32_t*)(margin + n_pad);  // spare words: max norm, max eps, max |b_hat|
+    if ((e = cudaMemsetAsync(max_bits, 0, 4 * sizeof(uint32_t), s)) != cudaSuccess) return cuda_fail(st, e, "memset");
     if ((e = launch_column_means(xwork, n, d, ref, means, means + d, s)) != cudaSuccess)
         return cuda_fail(st, e, "column means");
-    if ((e = launch_centre_transpose(xwork, n, n_pad, d, dp, means, coords_t, norm2, cnorm, xcentred, max_bits, s)) !=
-        cudaSuccess)
-        return cuda_fail(st, e, "centre");
-    if ((e = launch_margins(cnorm, norm2, n, d, o.mode, o.metric, SCRUST_FORM_PLAIN, max_bits, nullptr, nullptr, 1.0f,
-                            margin, s)) != cudaSuccess)
-        return cuda_fail(st, e, "margins");
-    ctx->launches += ref ? 3 : 4;
+    ctx->launches += ref ? 1 : 2;
 
-    // Candidate lists.
-    const int row_tiles = (int)(n_pad / 128);
-    const int col_tiles = row_tiles;
-    int segments = 1;
-    if (o.segments) {
-        segments = (int)o.segments;
-    } else if (row_tiles < 4 * ctx->sm_count) {
-        segments = (4 * ctx->sm_count + row_tiles - 1) / row_tiles;
-        segments = std::min(segments, std::max(1, kRerankCapacity / (4 * (int)k)));
-    }
-    segments = std::max(1, std::min(segments, col_tiles));
-    {
-        const int per = (col_tiles + segments - 1) / segments;
-        segments = (col_tiles + per - 1) / per;  // no empty segment
-    }
-    int cap = (int)o.list_capacity;
-    if (cap == 0) cap = std::max(64, (2 * (int)k + 32 + 31) / 32 * 32);
-    cap = std::max(cap, (int)k + 32);
-    const int ctot = cap + 128;
-    if (ctot > 512) return fail(st, SCRUST_INVALID_PARAMETER, "list_capacity must be at most 384, got %d", cap);
     Lists lists;
-    lists.cap = cap;
-    lists.ctot = ctot;
-    lists.segments = segments;
-    const size_t slots = (size_t)n_pad * segments;
-    lists.ids = (uint32_t*)ws_get(ctx, SLOT_LIST_IDS, sizeof(uint32_t) * slots * ctot, &e);
-    lists.vals = (float*)ws_get(ctx, SLOT_LIST_VALS, sizeof(float) * slots * ctot, &e);
-    lists.cnt = (uint32_t*)ws_get(ctx, SLOT_LIST_CNT, sizeof(uint32_t) * slots, &e);
-    lists.overflow = (uint32_t*)ws_get(ctx, SLOT_OVERFLOW, sizeof(uint32_t) * (size_t)n_pad, &e);
-    if (!lists.ids || !lists.vals || !lists.cnt || !lists.overflow) return cuda_fail(st, e, "workspace");
-    if ((e = cudaMemsetAsync(lists.overflow, 0, sizeof(uint32_t) * (size_t)n_pad, s)) != cudaSuccess ||
-        (e = cudaMemsetAsync(lists.cnt, 0, sizeof(uint32_t) * slots, s)) != cudaSuccess)
-        return cuda_fail(st, e, "memset");
-    plan.cap = cap;
-    plan.ctot = ctot;
-    plan.segments = segments;
-
-    mark(ctx, PH_PREP);
-    if ((e = launch_plain_candidates(ctx, plan, coords_t, n_pad, coords_t, n_pad, dp, norm2, margin, lists)) !=
-        cudaSuccess)
-        return cuda_fail(st, e, "knn_candidates_f32");
-    ctx->launches += 1;
-    mark(ctx, PH_CAND);
+    RowBounds bounds;
+    if (tensor) {
+        const bool bf16 = o.precision == SCRUST_PRECISION_BF16;
+        void* A16 = ws_get(ctx, SLOT_A16, (size_t)n_pad * 64 * 2, &e);
+        void* B16 = ws_get(ctx, SLOT_B16, (size_t)n_pad * 64 * 2, &e);
+        float* rb = (float*)ws_get(ctx, SLOT_QERR, sizeof(float) * 4 * (size_t)n_pad, &e);
+        if (!A16 || !B16 || !rb) return cuda_fail(st, e, "workspace");
+        float *bA = rb, *beps = rb + n_pad, *bdelta = rb + 2 * n_pad, *beps2 = rb + 3 * n_pad;
+        if ((e = launch_centre_transpose(xwork, n, n_pad, d, dp, means, nullptr, norm2, cnorm, nullptr, max_bits, s)) !=
+                cudaSuccess ||
+            (e = launch_tensor_operands(xwork, n, n_pad, d, means, max_bits, cosine, bf16, A16, B16, bA, beps,
+                                        max_bits + 1, max_bits + 2, s)) != cudaSuccess ||
+            (e = launch_tensor_bounds(n, bA, beps, max_bits + 1, max_bits + 2, bdelta, beps2, s)) != cudaSuccess)
+            return cuda_fail(st, e, "tensor operands");
+        ctx->launches += 3;
+        const int items = (int)(n_pad / 256);
+        int32_t rc = plan_lists(ctx, o, (int)k, items, (int)(n_pad / 256), 8 * ctx->sm_count, 64, &lists, st);
+        if (rc) return rc;
+        if ((rc = alloc_lists(ctx, n_pad, &lists, st))) return rc;
+        plan.cap = lists.cap;
+        plan.ctot = lists.ctot;
+        plan.segments = lists.segments;
+        mark(ctx, PH_PREP);
+        if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
+                                          nullptr)) != cudaSuccess)
+            return cuda_fail(st, e, "knn_candidates_tc");
+        ctx->launches += 1;
+        mark(ctx, PH_CAND);
+        bounds.A = bA;
+        bounds.delta = bdelta;
+        bounds.eps2 = beps2;
+    } else {
+        float* coords_t = (float*)ws_get(ctx, SLOT_COORDS_T, sizeof(float) * (size_t)dp * n_pad, &e);
+        if (!coords_t) return cuda_fail(st, e, "workspace");
+        if ((e = launch_centre_transpose(xwork, n, n_pad, d, dp, means, coords_t, norm2, cnorm, xcentred, max_bits,
+                                         s)) != cudaSuccess)
+            return cuda_fail(st, e, "centre");
+        if ((e = launch_margins(cnorm, norm2, n, d, o.mode, o.metric, SCRUST_FORM_PLAIN, max_bits, nullptr, nullptr,
+                                1.0f, margin, s)) != cudaSuccess)
+            return cuda_fail(st, e, "margins");
+        ctx->launches += 2;
+        const int row_tiles = (int)(n_pad / 128);
+        int32_t rc = plan_lists(ctx, o, (int)k, row_tiles, row_tiles, 4 * ctx->sm_count, 128, &lists, st);
+        if (rc) return rc;
+        if ((rc = alloc_lists(ctx, n_pad, &lists, st))) return rc;
+        plan.cap = lists.cap;
+        plan.ctot = lists.ctot;
+        plan.segments = lists.segments;
+        mark(ctx, PH_PREP);
+        if ((e = launch_plain_candidates(ctx, plan, coords_t, n_pad, coords_t, n_pad, dp, norm2, margin, lists)) !=
+            cudaSuccess)
+            return cuda_fail(st, e, "knn_candidates_f32");
+        ctx->launches += 1;
+        mark(ctx, PH_CAND);
+        bounds.margin = margin;
+    }
 
     const float* xr = ref ? xcentred : xwork;
-    if ((e = launch_rerank(ctx, plan, xr, xr, norm2, norm2, norm64, norm64, x, x, margin, lists, out_idx,
+    if ((e = launch_rerank(ctx, plan, xr, xr, norm2, norm2, norm64, norm64, x, x, bounds, lists, out_idx,
                            out_dist)) != cudaSuccess)
         return cuda_fail(st, e, "knn_rerank");
     ctx->launches += 2;

@@ -150,11 +150,32 @@ cudaError_t launch_plain_candidates(scrust_context* ctx, const KnnPlan& plan, co
                                     int64_t nq_pad, const float* r_t, int64_t nr_pad, int dp,
                                     const float* r_norm2, const float* margin, const Lists& lists);
 
+// knn_tensor.cu
+size_t tensor_smem_bytes();
+cudaError_t launch_tensor_operands(const float* x, int64_t n, int64_t n_pad, int d, const double* means,
+                                   const uint32_t* max_norm_bits, bool cosine, bool bf16, void* A16, void* B16,
+                                   float* bA, float* eps, uint32_t* max_eps_bits, uint32_t* max_bhat_bits,
+                                   cudaStream_t s);
+cudaError_t launch_tensor_bounds(int64_t n, const float* bA, const float* eps, const uint32_t* max_eps_bits,
+                                 const uint32_t* max_bhat_bits, float* bdelta, float* beps2, cudaStream_t s);
+cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, const void* A16, int64_t nq_pad,
+                                     const void* B16, int64_t nr_pad, const float* bA, const float* bdelta,
+                                     const float* beps2, const Lists& lists, bool bf16, int* grid_out);
+
+// Per-row bound of the candidate lists, as the rerank re-applies it: the
+// plain form's additive margin, or the tensor form's (A, delta, eps2).
+struct RowBounds {
+    const float* margin = nullptr;
+    const float* A = nullptr;
+    const float* delta = nullptr;
+    const float* eps2 = nullptr;
+};
+
 // rerank.cu
 cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float* qx,
                           const float* rx, const float* qnorm2, const float* rnorm2,
                           const double* qn64, const double* rn64, const float* qraw,
-                          const float* rraw, const float* margin, const Lists& lists,
+                          const float* rraw, const RowBounds& bounds, const Lists& lists,
                           uint32_t* out_idx, float* out_dist);
 
 // conn.cu

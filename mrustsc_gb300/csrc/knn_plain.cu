@@ -14,6 +14,7 @@
 // neighbour rows.
 #include "common.cuh"
 #include "internal.h"
+#include "lists.cuh"
 #include "tma.cuh"
 
 namespace scrust {
@@ -21,7 +22,6 @@ namespace scrust {
 namespace {
 
 constexpr int BM = 128, BN = 128, KC = 64, THREADS = 256;
-constexpr int MAXE = 16;  // list storage per (row, segment) <= 32 * MAXE
 
 struct PlainArgs {
     const float* r_norm2;
@@ -37,71 +37,6 @@ struct PlainArgs {
     int tiles_per_seg;
     int* err;
 };
-
-// Prunes one row's list (warp-cooperative): threshold <- min(threshold,
-// k-th smallest + margin), entries at or above the threshold dropped.
-__device__ void prune_list(uint32_t* ids, float* vals, uint32_t cnt, int k, int cap, float margin,
-                           float* thr, uint32_t* cnt_out, uint32_t* overflow_flag) {
-    const int lane = threadIdx.x & 31;
-    float v[MAXE];
-    uint32_t id[MAXE];
-#pragma unroll
-    for (int e = 0; e < MAXE; e++) {
-        int p = e * 32 + lane;
-        if (p < (int)cnt) {
-            v[e] = vals[p];
-            id[e] = ids[p];
-        } else {
-            v[e] = __int_as_float(0x7f800000);
-            id[e] = 0xffffffffu;
-        }
-    }
-    // k-th smallest key by binary radix selection.
-    uint32_t prefix = 0, decided = 0;
-    int rank = k;
-    for (int bit = 31; bit >= 0; --bit) {
-        const uint32_t b = 1u << bit;
-        int c0 = 0;
-#pragma unroll
-        for (int e = 0; e < MAXE; e++) {
-            uint32_t key = float_key(v[e]);
-            c0 += ((key & decided) == prefix) && !(key & b);
-        }
-        int total = __reduce_add_sync(0xffffffffu, c0);
-        if (rank > total) {
-            rank -= total;
-            prefix |= b;
-        }
-        decided |= b;
-    }
-    float theta = fminf(*thr, key_float(prefix) + margin);
-    uint32_t out = 0;
-#pragma unroll
-    for (int e = 0; e < MAXE; e++) {
-        bool keep = (e * 32 + lane < (int)cnt) && (v[e] < theta);
-        uint32_t ballot = __ballot_sync(0xffffffffu, keep);
-        if (keep) {
-            uint32_t pos = out + __popc(ballot & lanemask_lt());
-            ids[pos] = id[e];
-            vals[pos] = v[e];
-        }
-        out += __popc(ballot);
-    }
-    __syncwarp();
-    if (lane == 0) {
-        if ((int)out >= cap) {
-            // More candidates within the margin than the list holds: the row
-            // is finished by the exact fallback instead.
-            *overflow_flag = 1u;
-            *thr = __int_as_float(0xff800000);
-            *cnt_out = 0;
-        } else {
-            *thr = theta;
-            *cnt_out = out;
-        }
-    }
-    __syncwarp();
-}
 
 __global__ void __launch_bounds__(THREADS, 2)
     plain_candidates_kernel(const __grid_constant__ CUtensorMap tq, const __grid_constant__ CUtensorMap tr,
@@ -251,9 +186,9 @@ __global__ void __launch_bounds__(THREADS, 2)
                 if (c >= (uint32_t)a.lists.cap) {
                     const int64_t row = row0 + lr;
                     const int64_t lbase = (row * a.lists.segments + seg) * (int64_t)a.lists.ctot;
-                    prune_list(a.lists.ids + lbase, a.lists.vals + lbase,
-                               min(c, (uint32_t)a.lists.ctot), a.k, a.lists.cap, margin_s[lr],
-                               &thr_s[lr], &cnt_s[lr], a.lists.overflow + row);
+                    prune_list(a.lists.ids + lbase, a.lists.vals + lbase, min(c, (uint32_t)a.lists.ctot), a.k,
+                               a.lists.cap, PlainBound{margin_s[lr]}, &thr_s[lr], &cnt_s[lr],
+                               a.lists.overflow + row);
                 }
             }
         }

@@ -15,6 +15,7 @@
 // re-measures the whole row.
 #include "common.cuh"
 #include "internal.h"
+#include "lists.cuh"
 
 namespace scrust {
 
@@ -35,7 +36,7 @@ struct RerankArgs {
     const double* rn64;
     const float* qraw;
     const float* rraw;
-    const float* margin;
+    RowBounds bounds;
     Lists lists;
     int64_t nq, nr;
     int d, k, mode, metric, self;
@@ -162,7 +163,9 @@ __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a
     }
     __syncwarp();
     const uint32_t kth = team_select_hi(team, A, m0, a.k);
-    const float theta = key_float(kth) + a.margin[q];
+    const float theta = a.bounds.margin ? PlainBound{a.bounds.margin[q]}.theta(key_float(kth))
+                                        : TensorBound{a.bounds.A[q], a.bounds.delta[q], a.bounds.eps2[q]}.theta(
+                                              key_float(kth));
     int m = 0;
     for (int b0 = 0; b0 < m0; b0 += 32) {
         const int p = b0 + lane;
@@ -296,7 +299,7 @@ __global__ void __launch_bounds__(FB_THREADS) rerank_fallback_kernel(RerankArgs 
 cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float* qx,
                           const float* rx, const float* qnorm2, const float* rnorm2,
                           const double* qn64, const double* rn64, const float* qraw,
-                          const float* rraw, const float* margin, const Lists& lists,
+                          const float* rraw, const RowBounds& bounds, const Lists& lists,
                           uint32_t* out_idx, float* out_dist) {
     cudaError_t e;
     uint32_t* fb_rows = (uint32_t*)ws_get(ctx, SLOT_FALLBACK_ROWS, sizeof(uint32_t) * (size_t)plan.nq, &e);
@@ -313,7 +316,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.rn64 = rn64;
     a.qraw = qraw;
     a.rraw = rraw;
-    a.margin = margin;
+    a.bounds = bounds;
     a.lists = lists;
     a.nq = plan.nq;
     a.nr = plan.nr;
