@@ -204,6 +204,15 @@ SCRUST_API int32_t scrust_cuda_smooth_knn_distances_noalloc(const float* distanc
 SCRUST_API void scrust_cuda_set_timing(scrust_context* context, int32_t enable);
 SCRUST_API int32_t scrust_cuda_phase_times(scrust_context* context, float* ms, int32_t max_phases);
 
+/* Kernel counters (observability).  enable = 1 turns collection on (later
+ * calls accumulate), enable = 0 turns it off.  Writes up to max_words
+ * counters accumulated since the previous read and resets them; returns how
+ * many it wrote.  For the tensor form: appends, prunes, overflow rows,
+ * epilogue wait / busy cycles, MMA wait cycles (B tiles, accumulators),
+ * producer wait cycles, tiles, prune cycles. */
+SCRUST_API int32_t scrust_cuda_kernel_stats(scrust_context* context, int32_t enable, uint64_t* out,
+                                            int32_t max_words);
+
 /* Number of kernels this context has launched since it was created. */
 SCRUST_API uint64_t scrust_cuda_launch_count(const scrust_context* context);
 

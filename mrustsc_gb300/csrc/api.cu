@@ -157,7 +157,7 @@ struct KnnBuffers {
 // Candidate-list geometry: column segments per row block (so small inputs
 // still fill the GPU) and the list capacity that triggers a prune.
 int32_t plan_lists(scrust_context* ctx, const scrust_knn_options& o, int k, int row_blocks, int col_tiles,
-                   int blocks_wanted, int headroom, Lists* lists, scrust_status* st) {
+                   int blocks_wanted, int headroom, int default_cap, Lists* lists, scrust_status* st) {
     int segments = 1;
     if (o.segments) {
         segments = (int)o.segments;
@@ -169,7 +169,7 @@ int32_t plan_lists(scrust_context* ctx, const scrust_knn_options& o, int k, int 
     const int per = (col_tiles + segments - 1) / segments;
     segments = (col_tiles + per - 1) / per;  // no empty segment
     int cap = (int)o.list_capacity;
-    if (cap == 0) cap = std::max(64, (2 * k + 32 + 31) / 32 * 32);
+    if (cap == 0) cap = std::max(default_cap, (2 * k + 32 + 31) / 32 * 32);
     cap = std::max(cap, k + 32);
     const int ctot = cap + headroom;
     if (ctot > 512)
@@ -272,15 +272,19 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
             return cuda_fail(st, e, "tensor operands");
         ctx->launches += 3;
         const int items = (int)(n_pad / 256);
-        int32_t rc = plan_lists(ctx, o, (int)k, items, (int)(n_pad / 256), 8 * ctx->sm_count, 64, &lists, st);
+        // Headroom of 128: a tensor-form list is checked once per tile, after
+        // its warp has appended up to 128 columns.
+        int32_t rc =
+            plan_lists(ctx, o, (int)k, items, (int)(n_pad / 256), 8 * ctx->sm_count, 128, 64, &lists, st);
         if (rc) return rc;
+        lists.segments *= 2;  // one list per (column segment, column part) of a row
         if ((rc = alloc_lists(ctx, n_pad, &lists, st))) return rc;
         plan.cap = lists.cap;
         plan.ctot = lists.ctot;
         plan.segments = lists.segments;
         mark(ctx, PH_PREP);
         if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                          nullptr)) != cudaSuccess)
+                                          nullptr, ctx->d_stats)) != cudaSuccess)
             return cuda_fail(st, e, "knn_candidates_tc");
         ctx->launches += 1;
         mark(ctx, PH_CAND);
@@ -298,7 +302,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
             return cuda_fail(st, e, "margins");
         ctx->launches += 2;
         const int row_tiles = (int)(n_pad / 128);
-        int32_t rc = plan_lists(ctx, o, (int)k, row_tiles, row_tiles, 4 * ctx->sm_count, 128, &lists, st);
+        int32_t rc = plan_lists(ctx, o, (int)k, row_tiles, row_tiles, 4 * ctx->sm_count, 128, 64, &lists, st);
         if (rc) return rc;
         if ((rc = alloc_lists(ctx, n_pad, &lists, st))) return rc;
         plan.cap = lists.cap;
@@ -516,6 +520,7 @@ void scrust_cuda_context_destroy(scrust_context* ctx) {
     }
     for (int i = 0; i < 5; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->d_stats) cudaFree(ctx->d_stats);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -759,6 +764,37 @@ int32_t scrust_cuda_phase_times(scrust_context* ctx, float* ms, int32_t max_phas
 }
 
 uint64_t scrust_cuda_launch_count(const scrust_context* ctx) { return ctx ? ctx->launches : 0; }
+
+int32_t scrust_cuda_kernel_stats(scrust_context* ctx, int32_t enable, uint64_t* out, int32_t max_words) {
+    if (!ctx) return 0;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (enable && !ctx->d_stats) {
+        if (cudaMalloc(&ctx->d_stats, 16 * sizeof(unsigned long long)) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->d_stats = nullptr;
+            return 0;
+        }
+        cudaMemsetAsync(ctx->d_stats, 0, 16 * sizeof(unsigned long long), ctx->stream);
+    }
+    int written = 0;
+    if (ctx->d_stats && out && max_words > 0) {
+        unsigned long long h[16] = {0};
+        if (cudaMemcpyAsync(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess &&
+            cudaStreamSynchronize(ctx->stream) == cudaSuccess) {
+            written = max_words < 16 ? max_words : 16;
+            for (int i = 0; i < written; i++) out[i] = h[i];
+        }
+        cudaMemsetAsync(ctx->d_stats, 0, 16 * sizeof(unsigned long long), ctx->stream);
+    }
+    if (!enable && ctx->d_stats) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->d_stats);
+        ctx->d_stats = nullptr;
+    }
+    cudaGetLastError();
+    return written;
+}
 
 const char* scrust_cuda_version(void) { return "scrust-gb300 0.1.0 (sm_103a)"; }
 

@@ -347,6 +347,34 @@ size_t scan_scratch_elems(int64_t n) {
     return total + 16;
 }
 
+// Stable LSD radix sort of (key, payload) pairs on the low `bits` bits of the
+// keys, 8 bits per pass.  Ping-pongs between the A and B buffers; *keys_out
+// and *vals_out point at whichever holds the result.  `hist` holds
+// 256 * ceil(n / 4096) words and `scan_scratch` scan_scratch_elems(that) words.
+cudaError_t radix_sort_pairs(scrust_context* ctx, uint32_t* kA, unsigned long long* vA, uint32_t* kB,
+                             unsigned long long* vB, int64_t n, int bits, uint32_t* hist, uint32_t* scan_scratch,
+                             size_t scan_elems, uint32_t** keys_out, unsigned long long** vals_out) {
+    const int nblocks = (int)((n + RS_TILE - 1) / RS_TILE);
+    uint32_t *kin = kA, *kout = kB;
+    unsigned long long *vin = vA, *vout = vB;
+    cudaError_t e = cudaSuccess;
+    for (int shift = 0; shift < bits; shift += 8) {
+        rs_hist_kernel<<<nblocks, RS_THREADS, 0, ctx->stream>>>(kin, n, shift, hist, nblocks);
+        if ((e = device_exclusive_scan(ctx, hist, hist, (int64_t)256 * nblocks, scan_scratch, scan_elems)) != cudaSuccess)
+            return e;
+        rs_scatter_kernel<<<nblocks, RS_THREADS, 0, ctx->stream>>>(kin, vin, kout, vout, n, shift, hist, nblocks);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        ctx->launches += 2;
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    *keys_out = kin;
+    *vals_out = vin;
+    return cudaSuccess;
+}
+
+int radix_blocks(int64_t n) { return (int)((n + RS_TILE - 1) / RS_TILE); }
+
 cudaError_t launch_smooth_knn(scrust_context* ctx, const float* dist, int64_t n, int k, float* sigmas,
                               float* rhos) {
     cudaError_t e;

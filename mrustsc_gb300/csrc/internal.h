@@ -78,6 +78,7 @@ struct scrust_context {
     std::vector<scrust::CsrBuffers> csr_pool;
     PFN_cuTensorMapEncodeTiled_v12000 encode_tiled = nullptr;
     uint64_t launches = 0;              // kernels enqueued so far
+    unsigned long long* d_stats = nullptr;  // kernel counters when statistics are on (16 words)
     bool timing = false;
     cudaEvent_t ev[5] = {};             // phase boundaries: prep | candidates | rerank | connectivities
     bool ev_recorded[5] = {};
@@ -160,7 +161,8 @@ cudaError_t launch_tensor_bounds(int64_t n, const float* bA, const float* eps, c
                                  const uint32_t* max_bhat_bits, float* bdelta, float* beps2, cudaStream_t s);
 cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, const void* A16, int64_t nq_pad,
                                      const void* B16, int64_t nr_pad, const float* bA, const float* bdelta,
-                                     const float* beps2, const Lists& lists, bool bf16, int* grid_out);
+                                     const float* beps2, const Lists& lists, bool bf16, int* grid_out,
+                                     unsigned long long* stats);
 
 // Per-row bound of the candidate lists, as the rerank re-applies it: the
 // plain form's additive margin, or the tensor form's (A, delta, eps2).
@@ -183,6 +185,15 @@ cudaError_t launch_smooth_knn(scrust_context* ctx, const float* dist, int64_t n,
                               float* sigmas, float* rhos);
 int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n,
                            int k, bool validate, CsrBuffers* out, scrust_status* st);
+
+// Device-wide primitives (conn.cu).
+cudaError_t device_exclusive_scan(scrust_context* ctx, const uint32_t* in, uint32_t* out, int64_t n,
+                                  uint32_t* scratch, size_t scratch_elems);
+size_t scan_scratch_elems(int64_t n);
+int radix_blocks(int64_t n);
+cudaError_t radix_sort_pairs(scrust_context* ctx, uint32_t* kA, unsigned long long* vA, uint32_t* kB,
+                             unsigned long long* vB, int64_t n, int bits, uint32_t* hist, uint32_t* scan_scratch,
+                             size_t scan_elems, uint32_t** keys_out, unsigned long long** vals_out);
 
 // Tensor-map encoding through the driver entry point.
 bool encode_2d(scrust_context* ctx, CUtensorMap* map, CUtensorMapDataType dtype, void* base,

@@ -13,15 +13,19 @@
 // pair's squared distance scales with the pair's distance, not with the
 // norms (see TensorBound in lists.cuh).
 //
-// Kernel layout (persistent, one CTA per SM, 320 threads):
+// Kernel layout (persistent, one CTA per SM, 576 threads):
 //   warp 0      TMA producer: A (256 query rows) per work item, B (256
 //               reference rows) per tile, 4-stage ring
 //   warp 1      TMEM owner and MMA issuer: per B tile, two M=128 x N=256 x
 //               K=16 x4 chains into two TMEM accumulators (query halves)
-//   warps 2-9   epilogue: warp w reads TMEM lanes 32*(w%4).. of half (w-2)/4;
-//               each thread owns one query row, tests 32 columns at a time
-//               against its threshold (3-input min), appends survivors to
-//               its list and prunes full lists warp-cooperatively
+//   warps 2-17  epilogue: 8 warps per half; warp w reads TMEM lanes
+//               32*(w%4).. and one 128-column part of its half's
+//               accumulator.  Each thread owns one query row and one list per
+//               column part; it tests 32 columns at a time against its
+//               threshold (3-input min) while the next 32 are loaded from
+//               TMEM, appends survivors, and after releasing the accumulator
+//               prunes full lists warp-cooperatively.  The two parts of a row
+//               share their thresholds through shared memory.
 // The two accumulators ping-pong: the epilogue drains half 0 of tile j while
 // the tensor core computes half 1 of tile j, so each B tile is read once per
 // 256 query rows.  Every wait is bounded (tma.cuh).
@@ -46,12 +50,15 @@ constexpr int TK = 64;                 // halves per operand row
 constexpr int HALVES = 2;              // query halves per work item
 constexpr int ROWS = TBM * HALVES;     // 256 query rows per work item
 constexpr int STAGES = 4;
-constexpr int EPI_WARPS = 8;
+constexpr int PARTS = 2;               // column parts of a tile, one epilogue warp each
+constexpr int EPI_WARPS = HALVES * PARTS * 4;
 constexpr int THREADS = (2 + EPI_WARPS) * 32;
 constexpr uint32_t A_BYTES = ROWS * TK * 2;
 constexpr uint32_t B_BYTES = TBN * TK * 2;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr size_t SMEM_BYTES = 2 * A_BYTES + STAGES * B_BYTES + 1024;
+constexpr int kFinalPrune = 64;  // lists longer than this are pruned once more when a work item ends
+constexpr int kPartCols = TBN / PARTS;  // columns one epilogue warp drains per tile
 
 struct TensorArgs {
     Lists lists;
@@ -66,9 +73,43 @@ struct TensorArgs {
     int items;
     uint32_t idesc;
     int* err;
+    unsigned long long* stats;  // optional counters (TensorStat), null when off
+};
+
+// Counters gathered when statistics are on (summed over all CTAs).
+enum TensorStat : int {
+    TS_APPENDS = 0,        // candidates appended to lists
+    TS_PRUNES = 1,         // warp-cooperative prunes
+    TS_OVERFLOWS = 2,      // rows sent to the exact fallback
+    TS_EPI_WAIT = 3,       // epilogue cycles waiting for an accumulator (lane 0 of each warp)
+    TS_EPI_BUSY = 4,       // epilogue cycles draining accumulators
+    TS_MMA_WAIT_FULL = 5,  // MMA issuer cycles waiting for B tiles
+    TS_MMA_WAIT_EMPTY = 6, // MMA issuer cycles waiting for a drained accumulator
+    TS_TMA_WAIT = 7,       // producer cycles waiting for a free stage
+    TS_TILES = 8,          // (work item, B tile) pairs
+    TS_PRUNE_CYCLES = 9,   // epilogue cycles spent in prunes
+    TS_LD_CYCLES = 10,     // epilogue cycles from issuing TMEM loads to their completion
+    TS_APPEND_CALLS = 11,  // 32-column chunks that had survivors in some lane (per warp)
+    TS_COUNT = 16
 };
 
 __device__ __forceinline__ float f_of(uint32_t u) { return __uint_as_float(u); }
+
+// The i-th column tile a work item visits: its home tile first, then tiles at
+// growing distance alternately after and before it, within [ct0, ct1).  When
+// rows are ordered so that nearby cells sit at nearby positions, the first
+// tiles hold most of a row's neighbours and its threshold tightens at once.
+__device__ __forceinline__ int sweep_tile(int i, int home, int ct0, int ct1) {
+    const int hw = min(max(home, ct0), ct1 - 1);
+    if (i == 0) return hw;
+    const int L = hw - ct0, R = ct1 - 1 - hw;
+    const int m = min(L, R);
+    if (i <= 2 * m) {
+        const int d = (i + 1) >> 1;
+        return (i & 1) ? hw + d : hw - d;
+    }
+    return R > L ? hw + (i - m) : hw - (i - m);
+}
 
 __device__ __forceinline__ float min32(const uint32_t (&v)[32]) {
     float m[11];
@@ -83,16 +124,73 @@ __device__ __forceinline__ float min32(const uint32_t (&v)[32]) {
 }
 
 // Appends the columns of one 32-column chunk that pass the row's threshold.
-__device__ __forceinline__ void append_chunk(const uint32_t (&v)[32], int64_t colbase, float th, int64_t row,
-                                             const TensorArgs& a, uint32_t* ids, float* vals, uint32_t& cnt) {
+// `valid` masks out columns past the reference rows and the row itself.  The
+// survivors' slots come from prefix popcounts of the mask, so the stores are
+// independent of one another.
+__device__ __forceinline__ void append_chunk(const uint32_t (&v)[32], int64_t colbase, float th, uint32_t valid,
+                                             uint32_t* ids, float* vals, uint32_t& cnt) {
+    uint32_t mask = 0;
+#pragma unroll
+    for (int j = 0; j < 32; j++) mask |= (f_of(v[j]) < th) ? (1u << j) : 0u;
+    mask &= valid;
 #pragma unroll
     for (int j = 0; j < 32; j++) {
-        const float t = f_of(v[j]);
-        const int64_t col = colbase + j;
-        if (t < th && col < a.nr && !(a.self && col == row)) {
-            ids[cnt] = (uint32_t)col;
-            vals[cnt] = t;
-            cnt++;
+        if (mask & (1u << j)) {
+            const uint32_t pos = cnt + __popc(mask & ((1u << j) - 1u));
+            ids[pos] = (uint32_t)(colbase + j);
+            vals[pos] = f_of(v[j]);
+        }
+    }
+    cnt += __popc(mask);
+}
+
+// Columns of the chunk starting at colbase that may be appended: below nr and
+// not the row itself.
+__device__ __forceinline__ uint32_t chunk_valid(int64_t colbase, int64_t nr, bool self, int64_t row) {
+    uint32_t m = 0xffffffffu;
+    if (colbase + 32 > nr) m = colbase >= nr ? 0u : ((1u << (uint32_t)(nr - colbase)) - 1u);
+    if (self && row >= colbase && row < colbase + 32) m &= ~(1u << (uint32_t)(row - colbase));
+    return m;
+}
+
+
+// Tests one 32-column chunk against the row's threshold; survivors are rare,
+// so the warp branches once and lanes without survivors append an empty mask.
+__device__ __forceinline__ void test_chunk(const uint32_t (&v)[32], int64_t colbase, float th, int64_t row,
+                                           const TensorArgs& a, uint32_t* ids, float* vals, uint32_t& cnt) {
+    const float m = min32(v);
+    if (__any_sync(0xffffffffu, m < th))
+        append_chunk(v, colbase, th, chunk_valid(colbase, a.nr, a.self != 0, row), ids, vals, cnt);
+}
+
+// Prunes, with the whole warp, the lists of the lanes set in `need`; each
+// lane keeps its own threshold and count in registers.
+__device__ __forceinline__ void prune_lanes(uint32_t need, const TensorArgs& a, int seg, int64_t row,
+                                            const TensorBound& bnd, float& th, uint32_t& cnt,
+                                            uint32_t& n_ovf, uint32_t* hist) {
+    const int lane = threadIdx.x & 31;
+    const int segs = a.lists.segments;
+    while (need) {
+        const int l = __ffs(need) - 1;
+        need &= need - 1;
+        const uint32_t lc = __shfl_sync(0xffffffffu, cnt, l);
+        const float lth = __shfl_sync(0xffffffffu, th, l);
+        const TensorBound lb{__shfl_sync(0xffffffffu, bnd.A, l), __shfl_sync(0xffffffffu, bnd.delta, l),
+                             __shfl_sync(0xffffffffu, bnd.eps2, l)};
+        const int64_t lrow = __shfl_sync(0xffffffffu, row, l);
+        const int64_t off = (lrow * segs + seg) * (int64_t)a.lists.ctot;  // seg: list slot within the row
+        const PruneResult r =
+            prune_core(a.lists.ids + off, a.lists.vals + off, min(lc, (uint32_t)a.lists.ctot), a.k, lb, lth, hist);
+        if (lane == l) {
+            if ((int)r.cnt >= a.lists.cap) {
+                a.lists.overflow[row] = 1u;
+                th = __int_as_float(0xff800000);
+                cnt = 0;
+                n_ovf++;
+            } else {
+                th = r.theta;
+                cnt = r.cnt;
+            }
         }
     }
 }
@@ -108,10 +206,13 @@ __global__ void __launch_bounds__(THREADS, 1)
     __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], afull[2], aempty[2], tfull[HALVES],
         tempty[HALVES];
     __shared__ uint32_t tmem_slot;
+    __shared__ uint32_t hist_s[EPI_WARPS][256];
+    __shared__ unsigned long long theta_s[HALVES][PARTS][TBM];
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int segs = a.lists.segments;
+    const int segs = a.lists.segments;        // lists per row
+    const int csegs = segs / PARTS;           // column segments
 
     if (threadIdx.x == 0) {
         prefetch_tensormap(&ta);
@@ -126,7 +227,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         for (int h = 0; h < HALVES; h++) {
             mbar_init(&tfull[h], 1);
-            mbar_init(&tempty[h], 32 * (EPI_WARPS / HALVES));
+            mbar_init(&tempty[h], EPI_WARPS / HALVES);  // one arrival per epilogue warp
         }
         fence_barrier_init();
     }
@@ -143,9 +244,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         // ---------------- TMA producer ----------------
         if (lane == 0) {
             uint32_t sc = 0, ac = 0;
+            long long w_tma = 0;
             bool ok = true;
             for (int w = blockIdx.x; w < a.items && ok; w += gridDim.x) {
-                const int qt = w / segs, seg = w % segs;
+                const int qt = w / csegs, seg = w % csegs;
                 const int ct0 = seg * a.tiles_per_seg;
                 const int ct1 = min(a.col_tiles, ct0 + a.tiles_per_seg);
                 const uint32_t ab = ac & 1, au = ac >> 1;
@@ -156,12 +258,15 @@ __global__ void __launch_bounds__(THREADS, 1)
                 mbar_arrive_expect_tx(&afull[ab], A_BYTES);
                 tma_load_2d(sA + ab * A_BYTES, &ta, 0, qt * ROWS, &afull[ab]);
                 ac++;
-                for (int ct = ct0; ct < ct1; ++ct) {
+                for (int it = 0; it < ct1 - ct0; ++it) {
+                    const int ct = sweep_tile(it, qt * ROWS / TBN, ct0, ct1);
                     const uint32_t st = sc % STAGES, su = sc / STAGES;
+                    const long long t0 = a.stats ? clock64() : 0;
                     if (!mbar_wait_bounded(&empty[st], (su & 1) ^ 1, a.err)) {
                         ok = false;
                         break;
                     }
+                    if (a.stats) w_tma += clock64() - t0;
                     mbar_arrive_expect_tx(&full[st], B_BYTES);
                     tma_load_2d(sB + st * B_BYTES, &tb, 0, ct * TBN, &full[st]);
                     sc++;
@@ -174,14 +279,16 @@ __global__ void __launch_bounds__(THREADS, 1)
                 mbar_wait_bounded(&full[idx % STAGES], (idx / STAGES) & 1, a.err, 100000000ull);
             }
             if (ac) mbar_wait_bounded(&afull[(ac - 1) & 1], ((ac - 1) >> 1) & 1, a.err, 100000000ull);
+            if (a.stats) atomicAdd(a.stats + TS_TMA_WAIT, (unsigned long long)w_tma);
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
             uint32_t sc = 0, ac = 0, tc = 0;
+            long long w_full = 0, w_empty = 0;
             bool ok = true;
             for (int w = blockIdx.x; w < a.items && ok; w += gridDim.x) {
-                const int seg = w % segs;
+                const int seg = w % csegs;
                 const int ct0 = seg * a.tiles_per_seg;
                 const int ct1 = min(a.col_tiles, ct0 + a.tiles_per_seg);
                 const uint32_t ab = ac & 1, au = ac >> 1;
@@ -191,19 +298,23 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
                 tc_fence_after();
                 const uint32_t a_base = smem_addr(sA + ab * A_BYTES);
-                for (int ct = ct0; ct < ct1 && ok; ++ct) {
+                for (int it = ct0; it < ct1 && ok; ++it) {
                     const uint32_t st = sc % STAGES, su = sc / STAGES;
+                    long long t0 = a.stats ? clock64() : 0;
                     if (!mbar_wait_bounded(&full[st], su & 1, a.err)) {
                         ok = false;
                         break;
                     }
+                    if (a.stats) w_full += clock64() - t0;
                     tc_fence_after();
                     const uint32_t b_base = smem_addr(sB + st * B_BYTES);
                     for (int h = 0; h < HALVES; ++h) {
+                        t0 = a.stats ? clock64() : 0;
                         if (!mbar_wait_bounded(&tempty[h], (tc & 1) ^ 1, a.err)) {
                             ok = false;
                             break;
                         }
+                        if (a.stats) w_empty += clock64() - t0;
                         tc_fence_after();
                         const uint32_t d = tmem + (uint32_t)(h * TBN);
 #pragma unroll
@@ -223,18 +334,28 @@ __global__ void __launch_bounds__(THREADS, 1)
                 umma_commit(&aempty[ab]);
                 ac++;
             }
+            if (a.stats) {
+                atomicAdd(a.stats + TS_MMA_WAIT_FULL, (unsigned long long)w_full);
+                atomicAdd(a.stats + TS_MMA_WAIT_EMPTY, (unsigned long long)w_empty);
+                atomicAdd(a.stats + TS_TILES, (unsigned long long)tc);
+            }
         }
     } else {
         // ---------------- epilogue ----------------
         const int e = warp - 2;
         const int h = e / (EPI_WARPS / HALVES);
+        const int part = (e / 4) % PARTS;
         const int quarter = warp & 3;
         const int r_local = quarter * 32 + lane;
         const int cap = a.lists.cap;
+        const int col_segs = csegs;
+        volatile unsigned long long* my_th = &theta_s[h][part][r_local];
+        volatile unsigned long long* other_th = &theta_s[h][part ^ 1][r_local];
         uint32_t tc = 0;
+        uint32_t n_app = 0, n_prune = 0, n_ovf = 0;
         bool ok = true;
         for (int w = blockIdx.x; w < a.items && ok; w += gridDim.x) {
-            const int qt = w / segs, seg = w % segs;
+            const int qt = w / col_segs, seg = w % col_segs;
             const int ct0 = seg * a.tiles_per_seg;
             const int ct1 = min(a.col_tiles, ct0 + a.tiles_per_seg);
             const int64_t row = (int64_t)qt * ROWS + h * TBM + r_local;
@@ -243,55 +364,77 @@ __global__ void __launch_bounds__(THREADS, 1)
             uint32_t cnt = 0;
             TensorBound bnd{0.f, 0.f, 0.f};
             if (valid) bnd = TensorBound{a.bA[row], a.bdelta[row], a.beps2[row]};
-            const int64_t lbase = (row * segs + seg) * (int64_t)a.lists.ctot;
-            uint32_t* ids = a.lists.ids + lbase;
-            float* vals = a.lists.vals + lbase;
-            for (int ct = ct0; ct < ct1; ++ct) {
+            const int64_t lslot = (row * col_segs + seg) * PARTS + part;
+            uint32_t* ids = a.lists.ids + lslot * (int64_t)a.lists.ctot;
+            float* vals = a.lists.vals + lslot * (int64_t)a.lists.ctot;
+            const uint64_t tag = (uint64_t)(uint32_t)w << 32;
+            *my_th = tag | __float_as_uint(th);
+            for (int it = 0; it < ct1 - ct0; ++it) {
+                const int ct = sweep_tile(it, qt * ROWS / TBN, ct0, ct1);
                 if (!mbar_wait_bounded(&tfull[h], tc & 1, a.err)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                const int64_t col0 = (int64_t)ct * TBN;
-                const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(h * TBN);
-#pragma unroll 1
-                for (int c2 = 0; c2 < TBN / 64; ++c2) {
-                    uint32_t v0[32], v1[32];
-                    tmem_ld32(tbase + c2 * 64, v0);
-                    tmem_ld32(tbase + c2 * 64 + 32, v1);
-                    tmem_ld_wait2(v0, v1);
-                    if (min32(v0) < th) append_chunk(v0, col0 + c2 * 64, th, row, a, ids, vals, cnt);
-                    if (min32(v1) < th) append_chunk(v1, col0 + c2 * 64 + 32, th, row, a, ids, vals, cnt);
-                    uint32_t need = __ballot_sync(0xffffffffu, cnt >= (uint32_t)cap);
-                    while (need) {
-                        const int l = __ffs(need) - 1;
-                        need &= need - 1;
-                        const uint32_t lc = __shfl_sync(0xffffffffu, cnt, l);
-                        const float lth = __shfl_sync(0xffffffffu, th, l);
-                        const TensorBound lb{__shfl_sync(0xffffffffu, bnd.A, l),
-                                             __shfl_sync(0xffffffffu, bnd.delta, l),
-                                             __shfl_sync(0xffffffffu, bnd.eps2, l)};
-                        const int64_t lrow = __shfl_sync(0xffffffffu, row, l);
-                        const int64_t lb_off = (lrow * segs + seg) * (int64_t)a.lists.ctot;
-                        const PruneResult r = prune_core(a.lists.ids + lb_off, a.lists.vals + lb_off,
-                                                         min(lc, (uint32_t)a.lists.ctot), a.k, lb, lth);
-                        if (lane == l) {
-                            if ((int)r.cnt >= cap) {
-                                a.lists.overflow[row] = 1u;
-                                th = __int_as_float(0xff800000);
-                                cnt = 0;
-                            } else {
-                                th = r.theta;
-                                cnt = r.cnt;
-                            }
-                        }
-                    }
+                // The partner part's threshold bounds this row just as well.
+                const unsigned long long o = *other_th;
+                if ((o & 0xffffffff00000000ull) == tag) th = fminf(th, __uint_as_float((uint32_t)o));
+                const int64_t col0 = (int64_t)ct * TBN + part * kPartCols;
+                const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(h * TBN + part * kPartCols);
+                const uint32_t before = cnt;
+                {
+                    // Four 32-column chunks; each TMEM load overlaps the
+                    // previous chunk's threshold test.
+                    uint32_t va[32], vb[32];
+                    tmem_ld32(tbase, va);
+                    tmem_ld_wait(va);
+                    tmem_ld32(tbase + 32, vb);
+                    test_chunk(va, col0, th, row, a, ids, vals, cnt);
+                    tmem_ld_wait(vb);
+                    tmem_ld32(tbase + 64, va);
+                    test_chunk(vb, col0 + 32, th, row, a, ids, vals, cnt);
+                    tmem_ld_wait(va);
+                    tmem_ld32(tbase + 96, vb);
+                    test_chunk(va, col0 + 64, th, row, a, ids, vals, cnt);
+                    tmem_ld_wait(vb);
+                    test_chunk(vb, col0 + 96, th, row, a, ids, vals, cnt);
                 }
+                // Release the accumulator before any prune, so the tensor
+                // core refills it while this warp prunes.
                 tc_fence_before();
-                mbar_arrive(&tempty[h]);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&tempty[h]);
+                n_app += cnt - before;
+                const uint32_t need = __ballot_sync(0xffffffffu, cnt >= (uint32_t)cap);
+                if (need) {
+                    n_prune += __popc(need);
+                    prune_lanes(need, a, seg * PARTS + part, row, bnd, th, cnt, n_ovf, hist_s[e]);
+                    *my_th = tag | __float_as_uint(th);
+                }
                 tc++;
             }
-            if (valid && ok) a.lists.cnt[row * segs + seg] = min(cnt, (uint32_t)a.lists.ctot);
+            // A last prune keeps every finished list short, so the union of a
+            // row's lists stays within the rerank's capacity.
+            if (ok) {
+                const uint32_t need = __ballot_sync(0xffffffffu, cnt > (uint32_t)kFinalPrune);
+                if (need) {
+                    n_prune += __popc(need);
+                    prune_lanes(need, a, seg * PARTS + part, row, bnd, th, cnt, n_ovf, hist_s[e]);
+                }
+            }
+            if (valid && ok) a.lists.cnt[lslot] = min(cnt, (uint32_t)a.lists.ctot);
+        }
+        if (a.stats) {
+            unsigned long long s_app = n_app, s_ovf = n_ovf;
+            for (int o = 16; o > 0; o >>= 1) {
+                s_app += __shfl_xor_sync(0xffffffffu, s_app, o);
+                s_ovf += __shfl_xor_sync(0xffffffffu, s_ovf, o);
+            }
+            if (lane == 0) {
+                atomicAdd(a.stats + TS_APPENDS, s_app);
+                atomicAdd(a.stats + TS_OVERFLOWS, s_ovf);
+                atomicAdd(a.stats + TS_PRUNES, (unsigned long long)n_prune);
+            }
         }
     }
 
@@ -441,7 +584,8 @@ cudaError_t launch_tensor_bounds(int64_t n, const float* bA, const float* eps, c
 
 cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, const void* A16, int64_t nq_pad,
                                      const void* B16, int64_t nr_pad, const float* bA, const float* bdelta,
-                                     const float* beps2, const Lists& lists, bool bf16, int* grid_out) {
+                                     const float* beps2, const Lists& lists, bool bf16, int* grid_out,
+                                     unsigned long long* stats) {
     if (nq_pad % ROWS || nr_pad % TBN) return cudaErrorInvalidValue;
     CUtensorMap ta, tb;
     const CUtensorMapDataType dt = bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
@@ -459,12 +603,15 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.k = plan.k;
     a.self = plan.self ? 1 : 0;
     a.col_tiles = (int)(nr_pad / TBN);
-    a.tiles_per_seg = (a.col_tiles + lists.segments - 1) / lists.segments;
-    if ((a.col_tiles + a.tiles_per_seg - 1) / a.tiles_per_seg != lists.segments) return cudaErrorInvalidValue;
-    if (lists.ctot < lists.cap + 64 || lists.ctot > 32 * kListMaxEntriesPerLane) return cudaErrorInvalidValue;
-    a.items = (int)(nq_pad / ROWS) * lists.segments;
+    const int col_segs = lists.segments / PARTS;
+    a.tiles_per_seg = (a.col_tiles + col_segs - 1) / col_segs;
+    if ((a.col_tiles + a.tiles_per_seg - 1) / a.tiles_per_seg != col_segs) return cudaErrorInvalidValue;
+    if (lists.ctot < lists.cap + kPartCols || lists.ctot > 32 * kListMaxEntriesPerLane) return cudaErrorInvalidValue;
+    if (lists.segments % PARTS) return cudaErrorInvalidValue;
+    a.items = (int)(nq_pad / ROWS) * (lists.segments / PARTS);
     a.idesc = umma_idesc_f16(TBM, TBN, bf16);
     a.err = ctx->d_err;
+    a.stats = stats;
     cudaError_t e =
         cudaFuncSetAttribute(tensor_candidates_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
     if (e != cudaSuccess) return e;
