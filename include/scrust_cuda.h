@@ -94,6 +94,15 @@ typedef enum scrust_precision {
     SCRUST_PRECISION_BF16 = 1  /* 8-bit significand operands */
 } scrust_precision;
 
+/* Whether the tensor form first orders the rows by a nearest-anchor
+ * partition so each row meets its neighbours early in the sweep.  The
+ * neighbour lists do not depend on it; only the speed does. */
+typedef enum scrust_ordering {
+    SCRUST_ORDERING_AUTO = 0, /* on for large self-kNN solves with one column segment */
+    SCRUST_ORDERING_OFF = 1,
+    SCRUST_ORDERING_ON = 2    /* whenever the solve has one column segment */
+} scrust_ordering;
+
 typedef struct scrust_knn_options {
     uint32_t struct_size;   /* sizeof(scrust_knn_options) */
     int32_t form;           /* scrust_form */
@@ -102,10 +111,12 @@ typedef struct scrust_knn_options {
     int32_t precision;      /* scrust_precision, tensor form only */
     uint32_t list_capacity; /* candidates kept per row between prunes; 0 = automatic */
     uint32_t segments;      /* column segments per row tile; 0 = automatic */
-    uint32_t reserved[9];
+    int32_t ordering;       /* scrust_ordering, tensor form only */
+    uint32_t reserved[8];
 } scrust_knn_options;
 
-/* Fills `options` with the defaults: tensor form, Euclidean, exact, FP16. */
+/* Fills `options` with the defaults: plain form, Euclidean, exact, FP16,
+ * automatic ordering. */
 SCRUST_API void scrust_knn_options_default(scrust_knn_options* options);
 
 /* 1 when a CUDA device of compute capability 10.3 is usable, else 0. */

@@ -30,6 +30,7 @@ FORMS = {"plain": FORM_PLAIN, "tensor": FORM_TENSOR}
 METRICS = {"euclidean": METRIC_EUCLIDEAN, "cosine": METRIC_COSINE}
 MODES = {"exact": MODE_EXACT, "reference_snap": MODE_REFERENCE_SNAP}
 PRECISIONS = {"fp16": PRECISION_FP16, "bf16": PRECISION_BF16}
+ORDERINGS = {"auto": 0, "off": 1, "on": 2}
 
 
 class Status(ctypes.Structure):
@@ -45,7 +46,8 @@ class KnnOptions(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("list_capacity", ctypes.c_uint32),
         ("segments", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32 * 9),
+        ("ordering", ctypes.c_int32),
+        ("reserved", ctypes.c_uint32 * 8),
     ]
 
 
@@ -172,7 +174,8 @@ def context(device: int = 0) -> int:
 
 
 def options(form: str | int = "plain", metric: str | int = "euclidean", mode: str | int = "exact",
-            precision: str | int = "fp16", list_capacity: int = 0, segments: int = 0) -> KnnOptions:
+            precision: str | int = "fp16", list_capacity: int = 0, segments: int = 0,
+            ordering: str | int = "auto") -> KnnOptions:
     o = KnnOptions()
     lib().scrust_knn_options_default(ctypes.byref(o))
 
@@ -189,6 +192,7 @@ def options(form: str | int = "plain", metric: str | int = "euclidean", mode: st
     o.precision = pick(PRECISIONS, precision, "precision")
     o.list_capacity = int(list_capacity)
     o.segments = int(segments)
+    o.ordering = pick(ORDERINGS, ordering, "ordering")
     return o
 
 

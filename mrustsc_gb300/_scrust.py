@@ -66,15 +66,19 @@ def _k(k) -> int:
 
 
 def knn(embedding, k, device, *, metric: str = "euclidean", form: str = "plain", mode: str = "exact",
-        precision: str = "fp16"):
-    """Exact k nearest neighbours, self excluded, nearest first, ties to the smaller id."""
+        precision: str = "fp16", ordering: str = "auto"):
+    """Exact k nearest neighbours, self excluded, nearest first, ties to the smaller id.
+
+    `ordering` ("auto", "off", "on") controls the tensor form's row ordering,
+    which changes the speed and never the result.
+    """
     x = _array2(embedding, np.float32, "embedding")
     k = _k(k)
     dev = _device_index(device)
     n, d = x.shape
     L = _lib.lib()
     st = _lib.Status()
-    opts = _lib.options(form=form, metric=metric, mode=mode, precision=precision)
+    opts = _lib.options(form=form, metric=metric, mode=mode, precision=precision, ordering=ordering)
     ctx = None
     # Argument errors are reported before a device is required, as the
     # reference validates before dispatching (neighbors.rs:41-57).

@@ -92,6 +92,7 @@ namespace {
 
 constexpr uint32_t kMaxK = 128;
 constexpr int kRerankCapacity = 1024;
+constexpr int64_t kOrderMinRows = 65536;  // automatic ordering from this many rows
 
 int32_t check_knn_args(uint64_t n, uint64_t d, uint32_t k, scrust_status* st) {
     if (n == 0 || d == 0)
@@ -123,6 +124,8 @@ int32_t check_options(const scrust_knn_options* o, scrust_status* st) {
                     "metric must be euclidean in reference_snap mode (the reference has no cosine), got cosine");
     if (o->precision != SCRUST_PRECISION_FP16 && o->precision != SCRUST_PRECISION_BF16)
         return fail(st, SCRUST_INVALID_PARAMETER, "precision must be fp16 or bf16, got %d", o->precision);
+    if (o->ordering != SCRUST_ORDERING_AUTO && o->ordering != SCRUST_ORDERING_OFF && o->ordering != SCRUST_ORDERING_ON)
+        return fail(st, SCRUST_INVALID_PARAMETER, "ordering must be auto, off or on, got %d", o->ordering);
     return SCRUST_OK;
 }
 
@@ -181,6 +184,8 @@ int32_t plan_lists(scrust_context* ctx, const scrust_knn_options& o, int k, int 
     return SCRUST_OK;
 }
 
+}  // namespace
+
 int32_t alloc_lists(scrust_context* ctx, int64_t rows_pad, Lists* lists, scrust_status* st) {
     cudaError_t e = cudaSuccess;
     const size_t slots = (size_t)rows_pad * lists->segments;
@@ -194,6 +199,8 @@ int32_t alloc_lists(scrust_context* ctx, int64_t rows_pad, Lists* lists, scrust_
         return cuda_fail(st, e, "memset");
     return SCRUST_OK;
 }
+
+namespace {
 
 // Whether a solve runs the tensor form: it is asked for, the mode is exact,
 // and the row plus the three norm columns fits one 64-wide operand row.
@@ -257,6 +264,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
 
     Lists lists;
     RowBounds bounds;
+    const uint32_t* perm = nullptr;  // rows of the lists -> input rows (tensor form with ordering)
     if (tensor) {
         const bool bf16 = o.precision == SCRUST_PRECISION_BF16;
         void* A16 = ws_get(ctx, SLOT_A16, (size_t)n_pad * 64 * 2, &e);
@@ -265,17 +273,33 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
         if (!A16 || !B16 || !rb) return cuda_fail(st, e, "workspace");
         float *bA = rb, *beps = rb + n_pad, *bdelta = rb + 2 * n_pad, *beps2 = rb + 3 * n_pad;
         if ((e = launch_centre_transpose(xwork, n, n_pad, d, dp, means, nullptr, norm2, cnorm, nullptr, max_bits, s)) !=
-                cudaSuccess ||
-            (e = launch_tensor_operands(xwork, n, n_pad, d, means, max_bits, cosine, bf16, A16, B16, bA, beps,
-                                        max_bits + 1, max_bits + 2, s)) != cudaSuccess ||
+            cudaSuccess)
+            return cuda_fail(st, e, "centre");
+        ctx->launches += 1;
+        const int items = (int)(n_pad / 256);
+        // Ordering needs one column segment: it is on for large solves, where
+        // the row blocks alone fill the GPU, or when asked for.
+        const bool order_rows = n <= kOrderMaxRows &&
+                                (o.ordering == SCRUST_ORDERING_ON     ? (o.segments <= 1)
+                                 : o.ordering == SCRUST_ORDERING_AUTO ? (o.segments <= 1 && n >= kOrderMinRows)
+                                                                      : false);
+        scrust_knn_options lo = o;
+        if (order_rows) lo.segments = 1;
+        RowOrder order;
+        if (order_rows) {
+            int32_t rc = build_row_order(ctx, xwork, n, d, means, max_bits, cosine, bf16, A16, B16, bA, beps, bdelta,
+                                         beps2, &order, st);
+            if (rc) return rc;
+        }
+        if ((e = launch_tensor_operands(xwork, n, n_pad, d, means, max_bits, cosine, bf16, order.perm, A16, B16, bA,
+                                        beps, max_bits + 1, max_bits + 2, s)) != cudaSuccess ||
             (e = launch_tensor_bounds(n, bA, beps, max_bits + 1, max_bits + 2, bdelta, beps2, s)) != cudaSuccess)
             return cuda_fail(st, e, "tensor operands");
-        ctx->launches += 3;
-        const int items = (int)(n_pad / 256);
+        ctx->launches += 2;
         // Headroom of 128: a tensor-form list is checked once per tile, after
         // its warp has appended up to 128 columns.
         int32_t rc =
-            plan_lists(ctx, o, (int)k, items, (int)(n_pad / 256), 8 * ctx->sm_count, 128, 64, &lists, st);
+            plan_lists(ctx, lo, (int)k, items, (int)(n_pad / 256), 8 * ctx->sm_count, 128, 64, &lists, st);
         if (rc) return rc;
         lists.segments *= 2;  // one list per (column segment, column part) of a row
         if ((rc = alloc_lists(ctx, n_pad, &lists, st))) return rc;
@@ -283,11 +307,30 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
         plan.ctot = lists.ctot;
         plan.segments = lists.segments;
         mark(ctx, PH_PREP);
-        if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                          nullptr, ctx->d_stats)) != cudaSuccess)
-            return cuda_fail(st, e, "knn_candidates_tc");
-        ctx->launches += 1;
+        if (order_rows) {
+            // Two passes: the priority tiles, then the tiles the tile balls
+            // cannot rule out.
+            TileLists first;
+            first.tiles = order.prio;
+            first.count = order.prio_cnt;
+            first.stride = kPrioMax;
+            if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
+                                              &first, false, order.theta, nullptr, ctx->d_stats)) != cudaSuccess)
+                return cuda_fail(st, e, "knn_candidates_tc");
+            TileLists second;
+            if ((rc = build_second_pass(ctx, A16, bf16, n, d, order, bA, bdelta, &second, st))) return rc;
+            if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
+                                              &second, true, order.theta, nullptr, ctx->d_stats)) != cudaSuccess)
+                return cuda_fail(st, e, "knn_candidates_tc");
+            ctx->launches += 2;
+        } else {
+            if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
+                                              nullptr, false, nullptr, nullptr, ctx->d_stats)) != cudaSuccess)
+                return cuda_fail(st, e, "knn_candidates_tc");
+            ctx->launches += 1;
+        }
         mark(ctx, PH_CAND);
+        perm = order.perm;
         bounds.A = bA;
         bounds.delta = bdelta;
         bounds.eps2 = beps2;
@@ -318,7 +361,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
     }
 
     const float* xr = ref ? xcentred : xwork;
-    if ((e = launch_rerank(ctx, plan, xr, xr, norm2, norm2, norm64, norm64, x, x, bounds, lists, out_idx,
+    if ((e = launch_rerank(ctx, plan, xr, xr, norm2, norm2, norm64, norm64, x, x, bounds, lists, perm, out_idx,
                            out_dist)) != cudaSuccess)
         return cuda_fail(st, e, "knn_rerank");
     ctx->launches += 2;

@@ -48,6 +48,8 @@ enum Slot : int {
     SLOT_SCAN,
     SLOT_MISC,
     SLOT_WORKQ,
+    SLOT_ORDER,         // row ordering: anchors, permutation, priority tiles
+    SLOT_PRUNE,         // tile balls and the tile lists of the second sweep pass
     SLOT_COUNT
 };
 
@@ -132,6 +134,36 @@ struct Lists {
     int cap = 0, ctot = 0, segments = 1;
 };
 
+int32_t alloc_lists(scrust_context* ctx, int64_t rows_pad, Lists* lists, scrust_status* st);
+
+// A spatial ordering of the rows of a self-kNN solve (order.cu): rows are
+// grouped into cells around anchors and each 256-row work item of the tensor
+// sweep gets the column tiles of its own and its anchors' neighbouring cells
+// to visit first.
+constexpr int kPrioMax = 64;           // priority tiles per work item
+constexpr int kAnchorNeighbours = 16;  // neighbouring anchors per anchor
+constexpr int64_t kMaxAnchors = 8192;
+struct RowOrder {
+    const uint32_t* perm = nullptr;      // sorted position -> original row
+    const uint32_t* prio = nullptr;      // [items][kPrioMax] distinct column tiles, nearest cells first
+    const uint32_t* prio_cnt = nullptr;  // [items], at least 1
+    float* theta = nullptr;              // [n_pad * 2] list thresholds between the sweep passes
+    const uint32_t* cell_of_pos = nullptr;  // [n] cell of each sorted position
+};
+// Builds the ordering.  A16/B16 and the four bound arrays (n_pad rows each)
+// are used as scratch for operands in the original row order.
+int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, const double* means,
+                        uint32_t* max_bits, bool cosine, bool bf16, void* A16, void* B16, float* bA, float* beps,
+                        float* bdelta, float* beps2, RowOrder* out, scrust_status* st);
+struct TileLists;
+// After the priority pass: the column tiles each row block still has to
+// visit, from tile bounding balls and the rows' thresholds (order.cu).
+int32_t build_second_pass(scrust_context* ctx, const void* A16, bool bf16, int64_t n, int d, const RowOrder& order,
+                          const float* bA, const float* bdelta, TileLists* out, scrust_status* st);
+// Largest solve whose second-pass tile lists (row blocks x column tiles
+// entries) the ordering accepts.
+constexpr int64_t kOrderMaxRows = 8000000;
+
 // prep.cu
 cudaError_t launch_column_means(const float* x, int64_t n, int d, bool sequential, double* means,
                                 double* partial, cudaStream_t s);
@@ -153,16 +185,28 @@ cudaError_t launch_plain_candidates(scrust_context* ctx, const KnnPlan& plan, co
 
 // knn_tensor.cu
 size_t tensor_smem_bytes();
+// Row i of the operands is input row perm[i] (i when perm is null).
 cudaError_t launch_tensor_operands(const float* x, int64_t n, int64_t n_pad, int d, const double* means,
-                                   const uint32_t* max_norm_bits, bool cosine, bool bf16, void* A16, void* B16,
-                                   float* bA, float* eps, uint32_t* max_eps_bits, uint32_t* max_bhat_bits,
-                                   cudaStream_t s);
+                                   const uint32_t* max_norm_bits, bool cosine, bool bf16, const uint32_t* perm,
+                                   void* A16, void* B16, float* bA, float* eps, uint32_t* max_eps_bits,
+                                   uint32_t* max_bhat_bits, cudaStream_t s);
 cudaError_t launch_tensor_bounds(int64_t n, const float* bA, const float* eps, const uint32_t* max_eps_bits,
                                  const uint32_t* max_bhat_bits, float* bdelta, float* beps2, cudaStream_t s);
+// Explicit column tiles per row block of the query rows.
+struct TileLists {
+    const uint32_t* tiles = nullptr;
+    const uint32_t* offset = nullptr;  // per row block; null: block * stride
+    const uint32_t* count = nullptr;   // per row block
+    int stride = 0;
+};
+// One pass of the tensor sweep.  `tiles` null: every column tile, outward
+// from the diagonal.  `resume`: lists and thresholds continue from an earlier
+// pass (counts in lists.cnt, thresholds in theta_io); theta_io, when given,
+// receives each list's threshold as its row block ends.
 cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, const void* A16, int64_t nq_pad,
                                      const void* B16, int64_t nr_pad, const float* bA, const float* bdelta,
-                                     const float* beps2, const Lists& lists, bool bf16, int* grid_out,
-                                     unsigned long long* stats);
+                                     const float* beps2, const Lists& lists, bool bf16, const TileLists* tiles,
+                                     bool resume, float* theta_io, int* grid_out, unsigned long long* stats);
 
 // Per-row bound of the candidate lists, as the rerank re-applies it: the
 // plain form's additive margin, or the tensor form's (A, delta, eps2).
@@ -173,12 +217,13 @@ struct RowBounds {
     const float* eps2 = nullptr;
 };
 
-// rerank.cu
+// rerank.cu.  With a permutation, list row s and list entry c stand for
+// input rows perm[s] and perm[c]; outputs are written in input order.
 cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float* qx,
                           const float* rx, const float* qnorm2, const float* rnorm2,
                           const double* qn64, const double* rn64, const float* qraw,
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
-                          uint32_t* out_idx, float* out_dist);
+                          const uint32_t* perm, uint32_t* out_idx, float* out_dist);
 
 // conn.cu
 cudaError_t launch_smooth_knn(scrust_context* ctx, const float* dist, int64_t n, int k,

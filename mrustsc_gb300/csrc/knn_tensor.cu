@@ -74,6 +74,14 @@ struct TensorArgs {
     uint32_t idesc;
     int* err;
     unsigned long long* stats;  // optional counters (TensorStat), null when off
+    // Explicit column tiles per work item (one column segment), or null for
+    // the outward sweep over the item's whole segment.
+    const uint32_t* tl;
+    const uint32_t* tl_off;     // per-item offsets into tl, or null: item * tl_stride
+    const uint32_t* tl_cnt;
+    int tl_stride;
+    int resume;                 // lists and thresholds continue from an earlier pass
+    float* theta_io;            // per list: the threshold when the item ends (read when resuming)
 };
 
 // Counters gathered when statistics are on (summed over all CTAs).
@@ -110,6 +118,25 @@ __device__ __forceinline__ int sweep_tile(int i, int home, int ct0, int ct1) {
     }
     return R > L ? hw + (i - m) : hw - (i - m);
 }
+
+// The column tiles of one work item in visiting order: its explicit list,
+// or the outward sweep over [ct0, ct1).  The producer, the MMA issuer and
+// the epilogue all derive the same count and sequence from it.
+struct TileOrder {
+    const uint32_t* list;
+    int count, home, ct0, ct1;
+
+    __device__ __forceinline__ TileOrder(const TensorArgs& a, int w, int qt, int ct0_, int ct1_)
+        : list(nullptr), count(ct1_ - ct0_), home(qt * ROWS / TBN), ct0(ct0_), ct1(ct1_) {
+        if (a.tl) {
+            list = a.tl + (a.tl_off ? (int64_t)a.tl_off[w] : (int64_t)w * a.tl_stride);
+            count = (int)min(a.tl_cnt[w], (uint32_t)(ct1_ - ct0_));
+        }
+    }
+    __device__ __forceinline__ int next(int it) const {
+        return list ? (int)list[it] : sweep_tile(it, home, ct0, ct1);
+    }
+};
 
 __device__ __forceinline__ float min32(const uint32_t (&v)[32]) {
     float m[11];
@@ -214,6 +241,10 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int segs = a.lists.segments;        // lists per row
     const int csegs = segs / PARTS;           // column segments
 
+    // No item carries tag 0xffffffff: shared memory left by an earlier kernel
+    // must never pass for a partner's threshold.
+    for (int i = threadIdx.x; i < HALVES * PARTS * TBM; i += blockDim.x)
+        (&theta_s[0][0][0])[i] = 0xffffffff00000000ull | 0x7f800000u;
     if (threadIdx.x == 0) {
         prefetch_tensormap(&ta);
         prefetch_tensormap(&tb);
@@ -250,6 +281,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const int qt = w / csegs, seg = w % csegs;
                 const int ct0 = seg * a.tiles_per_seg;
                 const int ct1 = min(a.col_tiles, ct0 + a.tiles_per_seg);
+                const TileOrder order(a, w, qt, ct0, ct1);
+                if (order.count == 0) continue;
                 const uint32_t ab = ac & 1, au = ac >> 1;
                 if (!mbar_wait_bounded(&aempty[ab], (au & 1) ^ 1, a.err)) {
                     ok = false;
@@ -258,8 +291,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                 mbar_arrive_expect_tx(&afull[ab], A_BYTES);
                 tma_load_2d(sA + ab * A_BYTES, &ta, 0, qt * ROWS, &afull[ab]);
                 ac++;
-                for (int it = 0; it < ct1 - ct0; ++it) {
-                    const int ct = sweep_tile(it, qt * ROWS / TBN, ct0, ct1);
+                for (int it = 0; it < order.count; ++it) {
+                    const int ct = order.next(it);
                     const uint32_t st = sc % STAGES, su = sc / STAGES;
                     const long long t0 = a.stats ? clock64() : 0;
                     if (!mbar_wait_bounded(&empty[st], (su & 1) ^ 1, a.err)) {
@@ -288,9 +321,11 @@ __global__ void __launch_bounds__(THREADS, 1)
             long long w_full = 0, w_empty = 0;
             bool ok = true;
             for (int w = blockIdx.x; w < a.items && ok; w += gridDim.x) {
-                const int seg = w % csegs;
+                const int qt = w / csegs, seg = w % csegs;
                 const int ct0 = seg * a.tiles_per_seg;
                 const int ct1 = min(a.col_tiles, ct0 + a.tiles_per_seg);
+                const TileOrder order(a, w, qt, ct0, ct1);
+                if (order.count == 0) continue;
                 const uint32_t ab = ac & 1, au = ac >> 1;
                 if (!mbar_wait_bounded(&afull[ab], au & 1, a.err)) {
                     ok = false;
@@ -298,7 +333,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
                 tc_fence_after();
                 const uint32_t a_base = smem_addr(sA + ab * A_BYTES);
-                for (int it = ct0; it < ct1 && ok; ++it) {
+                for (int it = 0; it < order.count && ok; ++it) {
                     const uint32_t st = sc % STAGES, su = sc / STAGES;
                     long long t0 = a.stats ? clock64() : 0;
                     if (!mbar_wait_bounded(&full[st], su & 1, a.err)) {
@@ -358,6 +393,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int qt = w / col_segs, seg = w % col_segs;
             const int ct0 = seg * a.tiles_per_seg;
             const int ct1 = min(a.col_tiles, ct0 + a.tiles_per_seg);
+            const TileOrder order(a, w, qt, ct0, ct1);
+            if (order.count == 0) continue;
             const int64_t row = (int64_t)qt * ROWS + h * TBM + r_local;
             const bool valid = row < a.nq;
             float th = valid ? __int_as_float(0x7f800000) : __int_as_float(0xff800000);
@@ -365,12 +402,16 @@ __global__ void __launch_bounds__(THREADS, 1)
             TensorBound bnd{0.f, 0.f, 0.f};
             if (valid) bnd = TensorBound{a.bA[row], a.bdelta[row], a.beps2[row]};
             const int64_t lslot = (row * col_segs + seg) * PARTS + part;
+            if (valid && a.resume) {
+                cnt = min(a.lists.cnt[lslot], (uint32_t)cap);  // below cap when an item ends
+                th = a.theta_io[lslot];
+            }
             uint32_t* ids = a.lists.ids + lslot * (int64_t)a.lists.ctot;
             float* vals = a.lists.vals + lslot * (int64_t)a.lists.ctot;
             const uint64_t tag = (uint64_t)(uint32_t)w << 32;
             *my_th = tag | __float_as_uint(th);
-            for (int it = 0; it < ct1 - ct0; ++it) {
-                const int ct = sweep_tile(it, qt * ROWS / TBN, ct0, ct1);
+            for (int it = 0; it < order.count; ++it) {
+                const int ct = order.next(it);
                 if (!mbar_wait_bounded(&tfull[h], tc & 1, a.err)) {
                     ok = false;
                     break;
@@ -422,7 +463,10 @@ __global__ void __launch_bounds__(THREADS, 1)
                     prune_lanes(need, a, seg * PARTS + part, row, bnd, th, cnt, n_ovf, hist_s[e]);
                 }
             }
-            if (valid && ok) a.lists.cnt[lslot] = min(cnt, (uint32_t)a.lists.ctot);
+            if (valid && ok) {
+                a.lists.cnt[lslot] = min(cnt, (uint32_t)a.lists.ctot);
+                if (a.theta_io) a.theta_io[lslot] = th;
+            }
         }
         if (a.stats) {
             unsigned long long s_app = n_app, s_ovf = n_ovf;
@@ -461,14 +505,15 @@ __device__ __forceinline__ __nv_bfloat16 to16<__nv_bfloat16>(float v) {
 __device__ __forceinline__ double f64_of(__half v) { return (double)__half2float(v); }
 __device__ __forceinline__ double f64_of(__nv_bfloat16 v) { return (double)__bfloat162float(v); }
 
-// One thread per padded row: writes A_i and B_i (64 16-bit values each), the
+// One thread per padded row: writes A_i and B_i of input row perm[i] (64 16-bit values each), the
 // quantised squared norm A = |a_hat|^2, the per-row error radius
 // eps = |a_hat - scale*c| + scale*u*|c| (+ scale*u for normalised rows), and
 // the running maxima of eps and |b_hat|.
 template <class T>
 __global__ void tensor_operands_kernel(const float* __restrict__ x, int64_t n, int64_t n_pad, int d,
                                        const double* __restrict__ means, const uint32_t* __restrict__ max_norm_bits,
-                                       int cosine, T* __restrict__ A16, T* __restrict__ B16,
+                                       int cosine, const uint32_t* __restrict__ perm, T* __restrict__ A16,
+                                       T* __restrict__ B16,
                                        float* __restrict__ bA, float* __restrict__ eps,
                                        uint32_t* __restrict__ max_eps_bits, uint32_t* __restrict__ max_bhat_bits) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -487,9 +532,10 @@ __global__ void tensor_operands_kernel(const float* __restrict__ x, int64_t n, i
         brow[t] = zero;
     }
     if (i < n) {
+        const int64_t src = perm ? (int64_t)perm[i] : i;
         double hh = 0.0, e2 = 0.0, c2 = 0.0;
         for (int t = 0; t < d; t++) {
-            const float c = __double2float_rn(__dsub_rn((double)__ldg(x + i * d + t), means[t]));
+            const float c = __double2float_rn(__dsub_rn((double)__ldg(x + src * d + t), means[t]));
             const float y = c * scale;
             const T q = to16<T>(y);
             const double qd = f64_of(q);
@@ -560,18 +606,18 @@ __global__ void tensor_bounds_kernel(int64_t n, const float* __restrict__ bA, co
 size_t tensor_smem_bytes() { return SMEM_BYTES; }
 
 cudaError_t launch_tensor_operands(const float* x, int64_t n, int64_t n_pad, int d, const double* means,
-                                   const uint32_t* max_norm_bits, bool cosine, bool bf16, void* A16, void* B16,
-                                   float* bA, float* eps, uint32_t* max_eps_bits, uint32_t* max_bhat_bits,
-                                   cudaStream_t s) {
+                                   const uint32_t* max_norm_bits, bool cosine, bool bf16, const uint32_t* perm,
+                                   void* A16, void* B16, float* bA, float* eps, uint32_t* max_eps_bits,
+                                   uint32_t* max_bhat_bits, cudaStream_t s) {
     const unsigned blocks = (unsigned)((n_pad + 127) / 128);
     if (bf16)
         tensor_operands_kernel<__nv_bfloat16><<<blocks, 128, 0, s>>>(
-            x, n, n_pad, d, means, max_norm_bits, cosine ? 1 : 0, (__nv_bfloat16*)A16, (__nv_bfloat16*)B16, bA,
-            eps, max_eps_bits, max_bhat_bits);
+            x, n, n_pad, d, means, max_norm_bits, cosine ? 1 : 0, perm, (__nv_bfloat16*)A16, (__nv_bfloat16*)B16,
+            bA, eps, max_eps_bits, max_bhat_bits);
     else
         tensor_operands_kernel<__half><<<blocks, 128, 0, s>>>(x, n, n_pad, d, means, max_norm_bits,
-                                                              cosine ? 1 : 0, (__half*)A16, (__half*)B16, bA, eps,
-                                                              max_eps_bits, max_bhat_bits);
+                                                              cosine ? 1 : 0, perm, (__half*)A16, (__half*)B16, bA,
+                                                              eps, max_eps_bits, max_bhat_bits);
     return cudaGetLastError();
 }
 
@@ -584,8 +630,8 @@ cudaError_t launch_tensor_bounds(int64_t n, const float* bA, const float* eps, c
 
 cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, const void* A16, int64_t nq_pad,
                                      const void* B16, int64_t nr_pad, const float* bA, const float* bdelta,
-                                     const float* beps2, const Lists& lists, bool bf16, int* grid_out,
-                                     unsigned long long* stats) {
+                                     const float* beps2, const Lists& lists, bool bf16, const TileLists* tiles,
+                                     bool resume, float* theta_io, int* grid_out, unsigned long long* stats) {
     if (nq_pad % ROWS || nr_pad % TBN) return cudaErrorInvalidValue;
     CUtensorMap ta, tb;
     const CUtensorMapDataType dt = bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
@@ -612,6 +658,21 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.idesc = umma_idesc_f16(TBM, TBN, bf16);
     a.err = ctx->d_err;
     a.stats = stats;
+    a.tl = nullptr;
+    a.tl_off = nullptr;
+    a.tl_cnt = nullptr;
+    a.tl_stride = 0;
+    if (tiles && tiles->tiles) {
+        // Explicit tile lists are per row block: one column segment only.
+        if (col_segs != 1 || !tiles->count) return cudaErrorInvalidValue;
+        a.tl = tiles->tiles;
+        a.tl_off = tiles->offset;
+        a.tl_cnt = tiles->count;
+        a.tl_stride = tiles->stride;
+    }
+    a.resume = resume ? 1 : 0;
+    a.theta_io = theta_io;
+    if (resume && !theta_io) return cudaErrorInvalidValue;
     cudaError_t e =
         cudaFuncSetAttribute(tensor_candidates_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
     if (e != cudaSuccess) return e;

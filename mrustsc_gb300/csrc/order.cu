@@ -1,0 +1,668 @@
+// order.cu -- a spatial ordering of the rows for the tensor sweep.
+//
+// Exactness never depends on the order in which a row meets its columns, but
+// speed does: a row's threshold only tightens once it has seen columns near
+// it, and until then every column it meets is appended to its list.  So
+// before the sweep the rows are grouped into cells around anchors (every
+// n/m-th row), the cells are laid out consecutively, and every 256-row work
+// item gets a short list of priority tiles: the tiles holding its own cells
+// and the cells of the anchors nearest to them.  The sweep visits those
+// first (knn_tensor.cu).  Nearest anchors come from the tensor candidate lists
+// of a points x anchors pass with k = 1 (an approximate assignment is enough
+// for an ordering); anchor neighbourhoods from an FP32 anchors x anchors kNN.
+//
+// The sweep then runs in two passes.  The first visits only the priority
+// tiles and leaves every list with a threshold.  Between the passes each
+// column tile gets a bounding ball of its quantised rows (centre c_T, radius
+// R_T) and each row block the largest distance U_I that can still matter:
+// the MMA value of a pair is at least |a_i - b_j|^2 - A_i - delta_i, so a
+// column j can join row i's list only while |a_i - b_j| < sqrt(theta_i + A_i
+// + delta_i).  A tile with |c_I - c_T| - R_I - R_T >= U_I cannot add to any
+// row of block I and is left out of the second pass, which visits the rest.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace scrust {
+
+namespace {
+
+// Anchor c is input row floor(c * n / m); its coordinates are copied out
+// for the anchor neighbourhoods.
+__global__ void anchors_kernel(const float* __restrict__ x, int d, int64_t n, int64_t m, uint32_t* __restrict__ src,
+                               float* __restrict__ out) {
+    const int64_t c = blockIdx.x;
+    if (c >= m) return;
+    const int64_t r = (c * n) / m;
+    if (threadIdx.x == 0) src[c] = (uint32_t)r;
+    for (int t = threadIdx.x; t < d; t += blockDim.x) out[c * d + t] = x[r * d + t];
+}
+
+// One block per anchor: its kAnchorNeighbours nearest other anchors by FP32
+// squared distance (ties to the smaller id), 0xffffffff past the last.
+constexpr int AK_THREADS = 256;
+__global__ void __launch_bounds__(AK_THREADS) anchor_knn_kernel(const float* __restrict__ anc, int64_t m, int d,
+                                                                uint32_t* __restrict__ nb) {
+    extern __shared__ float ak_dist[];
+    __shared__ float wv[AK_THREADS / 32];
+    __shared__ uint32_t wi[AK_THREADS / 32];
+    const int64_t c = blockIdx.x;
+    const float* a = anc + c * d;
+    for (int64_t j = threadIdx.x; j < m; j += AK_THREADS) {
+        const float* b = anc + j * d;
+        float s = 0.f;
+        for (int t = 0; t < d; ++t) {
+            const float df = a[t] - b[t];
+            s = fmaf(df, df, s);
+        }
+        ak_dist[j] = j == c ? __int_as_float(0x7f800000) : s;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int r = 0; r < kAnchorNeighbours; ++r) {
+        float bv = __int_as_float(0x7f800000);
+        uint32_t bi = 0xffffffffu;
+        for (int64_t j = threadIdx.x; j < m; j += AK_THREADS) {
+            const float v = ak_dist[j];
+            if (v < bv) {  // ascending j per thread: the first minimum wins
+                bv = v;
+                bi = (uint32_t)j;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov < bv || (ov == bv && oi < bi)) {
+                bv = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            wv[w] = bv;
+            wi[w] = bi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float v = wv[0];
+            uint32_t id = wi[0];
+            for (int t = 1; t < AK_THREADS / 32; ++t)
+                if (wv[t] < v || (wv[t] == v && wi[t] < id)) {
+                    v = wv[t];
+                    id = wi[t];
+                }
+            const bool found = id < (uint32_t)m && v < __int_as_float(0x7f800000);
+            nb[c * kAnchorNeighbours + r] = found ? id : 0xffffffffu;
+            if (found) ak_dist[id] = __int_as_float(0x7f800000);
+        }
+        __syncthreads();
+    }
+}
+
+// Cells are laid out in the order of a walk over the anchors: from each
+// anchor to its nearest unvisited neighbouring anchor, or, when all of them
+// have been visited, to the lowest unvisited anchor.  Consecutive cells are
+// then mostly neighbours, so a 256-row block rarely mixes far-apart cells.
+// One warp; the first kChainNb neighbours of every anchor (16-bit ids) and
+// the visited bitmap live in shared memory.  rank[a] is anchor a's place.
+constexpr int kChainNb = 12;
+__global__ void __launch_bounds__(32) anchor_chain_kernel(const uint32_t* __restrict__ nb, int m,
+                                                          uint32_t* __restrict__ rank) {
+    extern __shared__ uint32_t ch_smem[];
+    uint32_t* visited = ch_smem;                                      // (m + 31) / 32 words
+    uint16_t* nbs = reinterpret_cast<uint16_t*>(ch_smem + (m + 31) / 32);  // m * kChainNb
+    const int lane = threadIdx.x;
+    const int words = (m + 31) / 32;
+    for (int i = lane; i < words; i += 32) visited[i] = 0u;
+    for (int i = lane; i < m * kChainNb; i += 32) {
+        const uint32_t c = nb[(int64_t)(i / kChainNb) * kAnchorNeighbours + i % kChainNb];
+        nbs[i] = c < (uint32_t)m ? (uint16_t)c : (uint16_t)0xffffu;
+    }
+    __syncwarp();
+    int cur = 0, scan = 0;
+    if (lane == 0) {
+        visited[0] = 1u;
+        rank[0] = 0;
+    }
+    __syncwarp();
+    int pos = 1;
+    for (; pos < m; ++pos) {
+        bool cand = false;
+        uint32_t c = 0xffffu;
+        if (lane < kChainNb) {
+            c = nbs[cur * kChainNb + lane];
+            cand = c < (uint32_t)m && !((visited[c >> 5] >> (c & 31)) & 1u);
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, cand);
+        int next;
+        if (bal) {
+            next = (int)__shfl_sync(0xffffffffu, c, __ffs(bal) - 1);
+        } else {
+            next = -1;
+            while (next < 0) {  // some anchor is unvisited since pos < m
+                const int wd = scan + lane;
+                const uint32_t free = wd < words ? ~visited[wd] : 0u;
+                const uint32_t fb = __ballot_sync(0xffffffffu, free != 0u);
+                if (fb) {
+                    const int wl = __ffs(fb) - 1;
+                    const uint32_t fw = __shfl_sync(0xffffffffu, free, wl);
+                    next = (scan + wl) * 32 + __ffs(fw) - 1;
+                    scan += wl;
+                } else {
+                    scan += 32;
+                    if (scan >= words) break;
+                }
+            }
+            if (next < 0 || next >= m) break;  // cannot happen: the bitmap holds an unvisited anchor
+        }
+        if (lane == 0) {
+            visited[next >> 5] |= 1u << (next & 31);
+            rank[next] = (uint32_t)pos;
+        }
+        __syncwarp();
+        cur = next;
+    }
+    // Every anchor gets a rank whatever happened above.
+    if (lane == 0 && pos < m)
+        for (int a = 0; a < m; ++a)
+            if (!((visited[a >> 5] >> (a & 31)) & 1u)) {
+                visited[a >> 5] |= 1u << (a & 31);
+                rank[a] = (uint32_t)pos++;
+            }
+}
+
+// Anchor neighbourhoods renamed into walk order: row rank[a] of out holds
+// the ranks of a's neighbours.
+__global__ void relabel_neighbours_kernel(const uint32_t* __restrict__ nb, const uint32_t* __restrict__ rank, int m,
+                                          uint32_t* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)m * kAnchorNeighbours) return;
+    const int64_t a = i / kAnchorNeighbours, j = i % kAnchorNeighbours;
+    const uint32_t c = nb[i];
+    out[(int64_t)rank[a] * kAnchorNeighbours + j] = c < (uint32_t)m ? rank[c] : 0xffffffffu;
+}
+
+// Per row, the column of the smallest candidate value over its lists: an
+// approximately nearest anchor, which is all an ordering needs.
+__global__ void argmin_lists_kernel(Lists lists, int64_t n, int64_t m, const uint32_t* __restrict__ rank,
+                                    uint32_t* __restrict__ keys, unsigned long long* __restrict__ vals) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float best = __int_as_float(0x7f800000);
+    uint32_t arg = 0;
+    for (int l = 0; l < lists.segments; ++l) {
+        const int64_t slot = i * lists.segments + l;
+        const uint32_t c = min(lists.cnt[slot], (uint32_t)lists.ctot);
+        const uint32_t* ids = lists.ids + slot * (int64_t)lists.ctot;
+        const float* vs = lists.vals + slot * (int64_t)lists.ctot;
+        for (uint32_t t = 0; t < c; ++t) {
+            const float v = vs[t];
+            if (v < best) {
+                best = v;
+                arg = ids[t];
+            }
+        }
+    }
+    keys[i] = rank[arg < (uint32_t)m ? arg : (uint32_t)(m - 1)];
+    vals[i] = (unsigned long long)i;
+}
+
+__global__ void unpack_perm_kernel(const uint32_t* __restrict__ skeys, const unsigned long long* __restrict__ svals,
+                                   int64_t n, uint32_t* __restrict__ perm, uint32_t* __restrict__ cell_of_pos,
+                                   uint32_t* __restrict__ cell_count) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    perm[s] = (uint32_t)svals[s];
+    cell_of_pos[s] = skeys[s];
+    atomicAdd(cell_count + skeys[s], 1u);
+}
+
+// One warp per 256-row work item: the column tiles holding the item's own
+// cells, then those holding the cells of their nearest anchors, nearest
+// anchors first; distinct, at most kPrioMax.  The item's own tile always
+// comes first, so no list is empty.
+constexpr int kHomeMax = 8;
+__global__ void prio_tiles_kernel(const uint32_t* __restrict__ cell_of_pos, int64_t n,
+                                  const uint32_t* __restrict__ cell_start, int m,
+                                  const uint32_t* __restrict__ anchor_nb, int ka, int items, int col_tiles,
+                                  uint32_t* __restrict__ prio, uint32_t* __restrict__ prio_cnt) {
+    __shared__ uint32_t outs[4][kPrioMax];
+    __shared__ uint32_t homes[4][kHomeMax];
+    __shared__ int nhome[4];
+    const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int item = blockIdx.x * 4 + wi;
+    if (item >= items) return;
+    uint32_t* out = outs[wi];
+    const int64_t s0 = (int64_t)item * 256, s1 = min(n, s0 + 256);
+    if (lane == 0) nhome[wi] = 0;
+    __syncwarp();
+    for (int64_t b = s0; b < s1; b += 32) {
+        const int64_t sp = b + lane;
+        const bool head = sp < s1 && (sp == s0 || cell_of_pos[sp] != cell_of_pos[sp - 1]);
+        const uint32_t bal = __ballot_sync(0xffffffffu, head);
+        if (head) {
+            const int pos = nhome[wi] + __popc(bal & lanemask_lt());
+            if (pos < kHomeMax) homes[wi][pos] = cell_of_pos[sp];
+        }
+        __syncwarp();
+        if (lane == 0) nhome[wi] = min(kHomeMax, nhome[wi] + __popc(bal));
+        __syncwarp();
+    }
+    const int nh = nhome[wi];
+    int cnt = 0;
+    // Appends tile t unless present (every lane tracks cnt).
+    auto add = [&](uint32_t t) {
+        if (cnt >= kPrioMax || t >= (uint32_t)col_tiles) return;
+        const bool dup = (lane < cnt && out[lane] == t) || (lane + 32 < cnt && out[lane + 32] == t);
+        if (__any_sync(0xffffffffu, dup)) return;
+        if (lane == 0) out[cnt] = t;
+        cnt++;
+        __syncwarp();
+    };
+    add((uint32_t)item);
+    const int kk = min(ka, kAnchorNeighbours);
+    for (int j = -1; j < kk && cnt < kPrioMax; ++j) {
+        for (int hh = 0; hh < nh && cnt < kPrioMax; ++hh) {
+            const uint32_t h = homes[wi][hh];
+            const uint32_t c = j < 0 ? h : anchor_nb[(int64_t)h * ka + j];
+            if (c >= (uint32_t)m) continue;
+            const uint32_t a = cell_start[c], b = cell_start[c + 1];
+            if (b <= a) continue;
+            for (uint32_t t = a / 256; t <= (b - 1) / 256 && cnt < kPrioMax; ++t) add(t);
+        }
+    }
+    __syncwarp();
+    for (int t = lane; t < cnt; t += 32) prio[(int64_t)item * kPrioMax + t] = out[t];
+    if (lane == 0) prio_cnt[item] = (uint32_t)cnt;
+}
+
+
+__device__ __forceinline__ float op_float(__half v) { return __half2float(v); }
+__device__ __forceinline__ float op_float(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// Balls of one tile: the whole tile and each of its cell segments (runs of
+// rows of one cell; a cell lies in one region of the data, while a tile
+// may straddle two far-apart cells).  Segments past kSegMax merge into the
+// last.  Centres are stored dimension-major for coalesced pair tests.
+constexpr int kSegMax = 8;
+struct TileBalls {
+    float* centre;      // [d][tiles]
+    float* radius;      // [tiles]
+    float* reach;       // [tiles]
+    float* seg_centre;  // [kSegMax][d][tiles]
+    float* seg_radius;  // [kSegMax][tiles]
+    float* seg_reach;   // [kSegMax][tiles]
+    uint32_t* nseg;     // [tiles]
+};
+
+// One block of 256 threads per column tile (= row block, the solve being a
+// self-kNN): centres (means) and radii of the tile's quantised rows, and the
+// reach U = max over the rows of sqrt(theta + A + delta), theta being the
+// smaller of the row's two list thresholds.
+template <class T>
+__global__ void __launch_bounds__(256) tile_balls_kernel(const T* __restrict__ ops, int64_t n, int d, int tiles,
+                                                         const uint32_t* __restrict__ cell_of_pos,
+                                                         const float* __restrict__ theta, const float* __restrict__ bA,
+                                                         const float* __restrict__ bdelta, TileBalls b) {
+    __shared__ float part[8][64];
+    __shared__ float centre[64];
+    __shared__ float scentre[kSegMax][64];
+    __shared__ int sstart[kSegMax + 1];
+    __shared__ int wheads[8];
+    __shared__ unsigned long long rmax_all, rmax_seg[kSegMax];
+    __shared__ uint32_t umax_all, umax_seg[kSegMax];
+    const int tile = blockIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t j = (int64_t)tile * 256 + threadIdx.x;
+    const bool valid = j < n;
+    const int rows = (int)min((int64_t)256, n - (int64_t)tile * 256);
+    const T* row = ops + j * 64;
+    // Segment of each row: the number of run heads at or before it, less one.
+    const bool head = valid && (threadIdx.x == 0 || cell_of_pos[j] != cell_of_pos[j - 1]);
+    const uint32_t hb = __ballot_sync(0xffffffffu, head);
+    if (lane == 0) wheads[w] = __popc(hb);
+    if (threadIdx.x == 0) {
+        rmax_all = 0ull;
+        umax_all = 0u;
+    }
+    if (threadIdx.x < kSegMax) {
+        rmax_seg[threadIdx.x] = 0ull;
+        umax_seg[threadIdx.x] = 0u;
+    }
+    __syncthreads();
+    int before = 0, nheads = 0;
+    for (int q = 0; q < 8; ++q) {
+        before += q < w ? wheads[q] : 0;
+        nheads += wheads[q];
+    }
+    const int nseg = min(nheads, kSegMax);
+    const int seg = min(before + __popc(hb & lanemask_lt()) + (head ? 1 : 0) - 1, kSegMax - 1);
+    if (head && seg == before + __popc(hb & lanemask_lt())) sstart[seg] = threadIdx.x;
+    if (threadIdx.x == 0) sstart[nseg] = rows;
+    for (int t = 0; t < d; ++t) {
+        float v = valid ? op_float(row[t]) : 0.f;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) part[w][t] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < d) {
+        float sum = 0.f;
+        for (int q = 0; q < 8; ++q) sum += part[q][threadIdx.x];
+        centre[threadIdx.x] = sum / (float)rows;
+        b.centre[(int64_t)threadIdx.x * tiles + tile] = centre[threadIdx.x];
+    }
+    for (int p = threadIdx.x; p < nseg * d; p += blockDim.x) {
+        const int sg = p / d, t = p % d;
+        float sum = 0.f;
+        for (int r = sstart[sg]; r < sstart[sg + 1]; ++r) sum += op_float(ops[((int64_t)tile * 256 + r) * 64 + t]);
+        const float c = sum / (float)(sstart[sg + 1] - sstart[sg]);
+        scentre[sg][t] = c;
+        b.seg_centre[((int64_t)sg * d + t) * tiles + tile] = c;
+    }
+    __syncthreads();
+    if (valid) {
+        double r2 = 0.0, s2 = 0.0;
+        for (int t = 0; t < d; ++t) {
+            const double v = (double)op_float(row[t]);
+            const double df = v - (double)centre[t], ds = v - (double)scentre[seg][t];
+            r2 += df * df;
+            s2 += ds * ds;
+        }
+        const float th = fminf(theta[2 * j], theta[2 * j + 1]);
+        const double v = (double)th + (double)bA[j] + (double)bdelta[j];
+        const float u = isinf(th) && th > 0.f ? th : (v > 0.0 ? __double2float_ru(sqrt(v)) : 0.f);
+        // Non-negative doubles and floats order like their bit patterns.
+        atomicMax(&rmax_all, (unsigned long long)__double_as_longlong(r2));
+        atomicMax(&rmax_seg[seg], (unsigned long long)__double_as_longlong(s2));
+        atomicMax(&umax_all, __float_as_uint(u));
+        atomicMax(&umax_seg[seg], __float_as_uint(u));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        b.radius[tile] = __double2float_ru(sqrt(__longlong_as_double((long long)rmax_all)) * (1.0 + 1e-9));
+        b.reach[tile] = __uint_as_float(umax_all);
+        b.nseg[tile] = (uint32_t)nseg;
+    }
+    if (threadIdx.x < nseg) {
+        const int sg = threadIdx.x;
+        b.seg_radius[(int64_t)sg * tiles + tile] =
+            __double2float_ru(sqrt(__longlong_as_double((long long)rmax_seg[sg])) * (1.0 + 1e-9));
+        b.seg_reach[(int64_t)sg * tiles + tile] = __uint_as_float(umax_seg[sg]);
+    }
+}
+
+// Whether a ball of reach u around centre I may hold a point within u of a
+// point of ball T (conservatively true).  The f32 centre distance is within
+// 1e-5 relative plus 3e-5 absolute (centre coordinates are at most 64 in
+// magnitude); the slack covers both, and the comparison itself is in f64.
+__device__ __forceinline__ bool tile_needed(float dc2, float rI, float rT, float uI) {
+    const double dc = sqrt((double)dc2) * (1.0 - 1e-5);
+    return !(dc >= (double)rI + (double)rT + (double)uI * (1.0 + 1e-5) + 1e-4);
+}
+
+// One block per row block I: the tiles of the second pass, i.e. the tiles
+// not in I's priority list that may still add to I, in ascending order.  The
+// whole-tile balls decide first; a pair they cannot separate is tested ball
+// by ball over the cell segments.  Without `offsets` it only counts.
+__global__ void __launch_bounds__(256) tile_lists_kernel(TileBalls b, int d, int tiles,
+                                                         const uint32_t* __restrict__ prio,
+                                                         const uint32_t* __restrict__ prio_cnt,
+                                                         const uint32_t* __restrict__ offsets,
+                                                         uint32_t* __restrict__ counts, uint32_t* __restrict__ entries) {
+    __shared__ float cI[64];
+    __shared__ float sI[kSegMax][64];
+    __shared__ float srI[kSegMax], suI[kSegMax];
+    __shared__ uint32_t pl[kPrioMax];
+    __shared__ int wsum[8];
+    __shared__ int base_s;
+    const int I = blockIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int pc = (int)min(prio_cnt[I], (uint32_t)kPrioMax);
+    const int nsI = (int)min(b.nseg[I], (uint32_t)kSegMax);
+    if (threadIdx.x < d) cI[threadIdx.x] = b.centre[(int64_t)threadIdx.x * tiles + I];
+    for (int p = threadIdx.x; p < nsI * d; p += blockDim.x)
+        sI[p / d][p % d] = b.seg_centre[((int64_t)(p / d) * d + p % d) * tiles + I];
+    if (threadIdx.x < nsI) {
+        srI[threadIdx.x] = b.seg_radius[(int64_t)threadIdx.x * tiles + I];
+        suI[threadIdx.x] = b.seg_reach[(int64_t)threadIdx.x * tiles + I];
+    }
+    if (threadIdx.x < pc) pl[threadIdx.x] = prio[(int64_t)I * kPrioMax + threadIdx.x];
+    if (threadIdx.x == 0) base_s = 0;
+    __syncthreads();
+    const float rI = b.radius[I], uI = b.reach[I];
+    const uint32_t off = offsets ? offsets[I] : 0u;
+    for (int t0 = 0; t0 < tiles; t0 += 256) {
+        const int T = t0 + threadIdx.x;
+        bool keep = false;
+        if (T < tiles) {
+            bool in_prio = false;
+            for (int q = 0; q < pc; ++q) in_prio |= pl[q] == (uint32_t)T;
+            if (!in_prio) {
+                float dc2 = 0.f;
+                for (int t = 0; t < d; ++t) {
+                    const float df = cI[t] - b.centre[(int64_t)t * tiles + T];
+                    dc2 = fmaf(df, df, dc2);
+                }
+                keep = tile_needed(dc2, rI, b.radius[T], uI);
+                const int nsT = (int)min(b.nseg[T], (uint32_t)kSegMax);
+                if (keep && (nsI > 1 || nsT > 1)) {
+                    keep = false;
+                    for (int sb = 0; sb < nsT && !keep; ++sb) {
+                        const float rT = b.seg_radius[(int64_t)sb * tiles + T];
+                        for (int sa = 0; sa < nsI && !keep; ++sa) {
+                            float e2 = 0.f;
+                            for (int t = 0; t < d; ++t) {
+                                const float df = sI[sa][t] - b.seg_centre[((int64_t)sb * d + t) * tiles + T];
+                                e2 = fmaf(df, df, e2);
+                            }
+                            keep = tile_needed(e2, srI[sa], rT, suI[sa]);
+                        }
+                    }
+                }
+            }
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) wsum[w] = __popc(bal);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int q = 0; q < 8; ++q) {
+            before += q < w ? wsum[q] : 0;
+            total += wsum[q];
+        }
+        if (offsets && keep) entries[off + base_s + before + __popc(bal & lanemask_lt())] = (uint32_t)T;
+        __syncthreads();
+        if (threadIdx.x == 0) base_s += total;
+        __syncthreads();
+    }
+    if (!offsets && threadIdx.x == 0) counts[I] = (uint32_t)base_s;
+}
+
+}  // namespace
+
+namespace {
+
+size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+
+int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, const double* means,
+                        uint32_t* max_bits, bool cosine, bool bf16, void* A16, void* B16, float* bA, float* beps,
+                        float* bdelta, float* beps2, RowOrder* out, scrust_status* st) {
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaSuccess;
+    const int64_t n_pad = (n + 255) / 256 * 256;
+    const int items = (int)(n_pad / 256);
+    const int64_t m = std::min<int64_t>(std::max<int64_t>(n / 256, 2), kMaxAnchors);
+    const int64_t m_pad = (m + 255) / 256 * 256;
+    const int nblocks = radix_blocks(n);
+    const size_t scan_elems = scan_scratch_elems(std::max<int64_t>((int64_t)256 * nblocks, m + 1));
+
+    // Carve the ordering slot.
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align_up(off + bytes);
+        return o;
+    };
+    const size_t o_src = take(4 * (size_t)m), o_anc = take(4 * (size_t)m * d), o_aA = take(128 * (size_t)m_pad),
+                 o_aB = take(128 * (size_t)m_pad), o_arb = take(8 * (size_t)m_pad), o_kA = take(4 * (size_t)n),
+                 o_kB = take(4 * (size_t)n), o_vA = take(8 * (size_t)n), o_vB = take(8 * (size_t)n),
+                 o_perm = take(4 * (size_t)n), o_cell = take(4 * (size_t)n), o_ccnt = take(4 * (size_t)(m + 1)),
+                 o_cst = take(4 * (size_t)(m + 1)), o_nb = take(4 * (size_t)m * kAnchorNeighbours),
+                 o_nb2 = take(4 * (size_t)m * kAnchorNeighbours), o_rank = take(4 * (size_t)m),
+                 o_prio = take(4 * (size_t)items * kPrioMax), o_pc = take(4 * (size_t)items),
+                 o_theta = take(8 * (size_t)n_pad),
+                 o_hist = take(4 * ((size_t)256 * nblocks + 16)), o_scan = take(4 * scan_elems);
+    char* base = (char*)ws_get(ctx, SLOT_ORDER, off, &e);
+    if (!base) return cuda_fail(st, e, "ordering: workspace");
+    uint32_t* src = (uint32_t*)(base + o_src);
+    float* anc = (float*)(base + o_anc);
+    uint32_t *keysA = (uint32_t*)(base + o_kA), *keysB = (uint32_t*)(base + o_kB);
+    unsigned long long *valsA = (unsigned long long*)(base + o_vA), *valsB = (unsigned long long*)(base + o_vB);
+    uint32_t* perm = (uint32_t*)(base + o_perm);
+    uint32_t* cell_of_pos = (uint32_t*)(base + o_cell);
+    uint32_t* cell_count = (uint32_t*)(base + o_ccnt);
+    uint32_t* cell_start = (uint32_t*)(base + o_cst);
+    uint32_t* anchor_nb = (uint32_t*)(base + o_nb);
+    uint32_t* cell_nb = (uint32_t*)(base + o_nb2);
+    uint32_t* rank = (uint32_t*)(base + o_rank);
+    uint32_t* prio = (uint32_t*)(base + o_prio);
+    uint32_t* prio_cnt = (uint32_t*)(base + o_pc);
+    float* arb = (float*)(base + o_arb);
+
+    // Anchors, and both operand sets in the input order.
+    anchors_kernel<<<(unsigned)m, 64, 0, s>>>(x, d, n, m, src, anc);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchors");
+    if ((e = launch_tensor_operands(x, n, n_pad, d, means, max_bits, cosine, bf16, nullptr, A16, B16, bA, beps,
+                                    max_bits + 1, max_bits + 2, s)) != cudaSuccess ||
+        (e = launch_tensor_bounds(n, bA, beps, max_bits + 1, max_bits + 2, bdelta, beps2, s)) != cudaSuccess ||
+        (e = launch_tensor_operands(x, m, m_pad, d, means, max_bits, cosine, bf16, src, base + o_aA, base + o_aB, arb,
+                                    arb + m_pad, max_bits + 1, max_bits + 2, s)) != cudaSuccess)
+        return cuda_fail(st, e, "ordering: operands");
+    ctx->launches += 4;
+
+    // Anchor neighbourhoods and the walk that orders the cells.
+    anchor_knn_kernel<<<(unsigned)m, AK_THREADS, sizeof(float) * (size_t)m, s>>>(anc, m, d, anchor_nb);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor neighbours");
+    const size_t chain_smem = 4 * (size_t)((m + 31) / 32) + 2 * (size_t)m * kChainNb;
+    if ((e = cudaFuncSetAttribute(anchor_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)chain_smem)) != cudaSuccess)
+        return cuda_fail(st, e, "ordering: anchor walk");
+    anchor_chain_kernel<<<1, 32, chain_smem, s>>>(anchor_nb, (int)m, rank);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor walk");
+    relabel_neighbours_kernel<<<(unsigned)((m * kAnchorNeighbours + 255) / 256), 256, 0, s>>>(anchor_nb, rank, (int)m,
+                                                                                               cell_nb);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor walk");
+    ctx->launches += 3;
+
+    // Rows x anchors with k = 1 on the tensor cores.
+    KnnPlan px;
+    px.nq = n;
+    px.nr = m;
+    px.d = d;
+    px.k = 1;
+    px.self = false;
+    px.form = SCRUST_FORM_TENSOR;
+    Lists lx;
+    lx.cap = 64;
+    lx.ctot = 64 + 128;
+    lx.segments = 2;
+    int32_t rc = alloc_lists(ctx, n_pad, &lx, st);
+    if (rc) return rc;
+    px.cap = lx.cap;
+    px.ctot = lx.ctot;
+    px.segments = lx.segments;
+    if ((e = launch_tensor_candidates(ctx, px, A16, n_pad, base + o_aB, m_pad, bA, bdelta, beps2, lx, bf16, nullptr,
+                                      false, nullptr, nullptr, nullptr)) != cudaSuccess)
+        return cuda_fail(st, e, "ordering: anchor candidates");
+    argmin_lists_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(lx, n, m, rank, keysA, valsA);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: nearest anchor");
+    ctx->launches += 2;
+
+    // Stable sort of the rows by anchor: the permutation and the cells.
+    int bits = 1;
+    while (((int64_t)1 << bits) < m) bits++;
+    uint32_t* skeys = nullptr;
+    unsigned long long* svals = nullptr;
+    if ((e = radix_sort_pairs(ctx, keysA, valsA, keysB, valsB, n, bits, (uint32_t*)(base + o_hist),
+                              (uint32_t*)(base + o_scan), scan_elems, &skeys, &svals)) != cudaSuccess)
+        return cuda_fail(st, e, "ordering: sort");
+    if ((e = cudaMemsetAsync(cell_count, 0, 4 * (size_t)(m + 1), s)) != cudaSuccess)
+        return cuda_fail(st, e, "ordering: memset");
+    unpack_perm_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(skeys, svals, n, perm, cell_of_pos, cell_count);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: permutation");
+    if ((e = device_exclusive_scan(ctx, cell_count, cell_start, m + 1, (uint32_t*)(base + o_scan), scan_elems)) !=
+        cudaSuccess)
+        return cuda_fail(st, e, "ordering: cell scan");
+
+    // The priority tiles of every work item.
+    prio_tiles_kernel<<<(unsigned)((items + 3) / 4), 128, 0, s>>>(cell_of_pos, n, cell_start, (int)m, cell_nb,
+                                                                  kAnchorNeighbours, items, items, prio, prio_cnt);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: priority tiles");
+    ctx->launches += 2;
+    out->perm = perm;
+    out->prio = prio;
+    out->prio_cnt = prio_cnt;
+    out->theta = (float*)(base + o_theta);
+    out->cell_of_pos = cell_of_pos;
+    return SCRUST_OK;
+}
+
+int32_t build_second_pass(scrust_context* ctx, const void* A16, bool bf16, int64_t n, int d, const RowOrder& order,
+                          const float* bA, const float* bdelta, TileLists* out, scrust_status* st) {
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaSuccess;
+    const int tiles = (int)((n + 255) / 256);
+    const size_t scan_elems = scan_scratch_elems((int64_t)tiles + 1);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align_up(off + bytes);
+        return o;
+    };
+    const size_t o_c = take(4 * (size_t)d * tiles), o_r = take(4 * (size_t)tiles), o_u = take(4 * (size_t)tiles),
+                 o_sc = take(4 * (size_t)kSegMax * d * tiles), o_sr = take(4 * (size_t)kSegMax * tiles),
+                 o_su = take(4 * (size_t)kSegMax * tiles), o_ns = take(4 * (size_t)tiles),
+                 o_cnt = take(4 * ((size_t)tiles + 1)), o_off = take(4 * ((size_t)tiles + 1)),
+                 o_scan = take(4 * scan_elems), o_ent = take(4 * (size_t)tiles * (size_t)tiles);
+    char* base = (char*)ws_get(ctx, SLOT_PRUNE, off, &e);
+    if (!base) return cuda_fail(st, e, "pruning: workspace");
+    TileBalls balls;
+    balls.centre = (float*)(base + o_c);
+    balls.radius = (float*)(base + o_r);
+    balls.reach = (float*)(base + o_u);
+    balls.seg_centre = (float*)(base + o_sc);
+    balls.seg_radius = (float*)(base + o_sr);
+    balls.seg_reach = (float*)(base + o_su);
+    balls.nseg = (uint32_t*)(base + o_ns);
+    uint32_t* counts = (uint32_t*)(base + o_cnt);
+    uint32_t* offsets = (uint32_t*)(base + o_off);
+    uint32_t* entries = (uint32_t*)(base + o_ent);
+    if (bf16)
+        tile_balls_kernel<__nv_bfloat16><<<tiles, 256, 0, s>>>((const __nv_bfloat16*)A16, n, d, tiles,
+                                                               order.cell_of_pos, order.theta, bA, bdelta, balls);
+    else
+        tile_balls_kernel<__half><<<tiles, 256, 0, s>>>((const __half*)A16, n, d, tiles, order.cell_of_pos,
+                                                        order.theta, bA, bdelta, balls);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "pruning: tile balls");
+    if ((e = cudaMemsetAsync(counts + tiles, 0, sizeof(uint32_t), s)) != cudaSuccess)
+        return cuda_fail(st, e, "pruning: memset");
+    tile_lists_kernel<<<tiles, 256, 0, s>>>(balls, d, tiles, order.prio, order.prio_cnt, nullptr, counts, nullptr);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "pruning: tile counts");
+    if ((e = device_exclusive_scan(ctx, counts, offsets, (int64_t)tiles + 1, (uint32_t*)(base + o_scan),
+                                   scan_elems)) != cudaSuccess)
+        return cuda_fail(st, e, "pruning: scan");
+    tile_lists_kernel<<<tiles, 256, 0, s>>>(balls, d, tiles, order.prio, order.prio_cnt, offsets, counts, entries);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "pruning: tile lists");
+    ctx->launches += 3;
+    out->tiles = entries;
+    out->offset = offsets;
+    out->count = counts;
+    out->stride = 0;
+    return SCRUST_OK;
+}
+
+}  // namespace scrust

@@ -38,6 +38,7 @@ struct RerankArgs {
     const float* rraw;
     RowBounds bounds;
     Lists lists;
+    const uint32_t* perm;  // list row / list entry -> input row, or null
     int64_t nq, nr;
     int d, k, mode, metric, self;
     float gamma;
@@ -120,9 +121,13 @@ __device__ void finalize_row(const Team& team, const RerankArgs& a, int64_t q,
     team.sync();
 }
 
-__device__ void push_fallback(const RerankArgs& a, int64_t q) {
+__device__ void push_fallback(const RerankArgs& a, int64_t slot) {
     uint32_t pos = atomicAdd(a.fb_count, 1u);
-    a.fb_rows[pos] = (uint32_t)q;
+    a.fb_rows[pos] = (uint32_t)slot;
+}
+
+__device__ __forceinline__ int64_t input_row(const RerankArgs& a, int64_t s) {
+    return a.perm ? (int64_t)a.perm[s] : s;
 }
 
 __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a) {
@@ -131,24 +136,25 @@ __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a
     const int lane = threadIdx.x & 31;
     unsigned long long* A = rr_smem + (size_t)warp * 2 * RC;
     unsigned long long* B = A + RC;
-    const int64_t q = (int64_t)blockIdx.x * RR_WARPS + warp;
-    if (q >= a.nq) return;
+    const int64_t slot = (int64_t)blockIdx.x * RR_WARPS + warp;  // list row
+    if (slot >= a.nq) return;
     WarpTeam team;
-    if (a.lists.overflow[q]) {
-        if (lane == 0) push_fallback(a, q);
+    if (a.lists.overflow[slot]) {
+        if (lane == 0) push_fallback(a, slot);
         return;
     }
+    const int64_t q = input_row(a, slot);
     const int segs = a.lists.segments;
     int m0 = 0;
-    for (int s = 0; s < segs; ++s) m0 += (int)min(a.lists.cnt[q * segs + s], (uint32_t)a.lists.ctot);
+    for (int s = 0; s < segs; ++s) m0 += (int)min(a.lists.cnt[slot * segs + s], (uint32_t)a.lists.ctot);
     if (m0 > RC || m0 < a.k) {
-        if (lane == 0) push_fallback(a, q);
+        if (lane == 0) push_fallback(a, slot);
         return;
     }
     int off = 0;
     for (int s = 0; s < segs; ++s) {
-        const int c = (int)min(a.lists.cnt[q * segs + s], (uint32_t)a.lists.ctot);
-        const int64_t base = (q * segs + s) * (int64_t)a.lists.ctot;
+        const int c = (int)min(a.lists.cnt[slot * segs + s], (uint32_t)a.lists.ctot);
+        const int64_t base = (slot * segs + s) * (int64_t)a.lists.ctot;
         for (int p = lane; p < c; p += 32) {
             uint32_t id = a.lists.ids[base + p];
             float v = a.lists.vals[base + p];
@@ -157,14 +163,15 @@ __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a
                 id = 0;
                 v = __int_as_float(0x7f800000);
             }
+            if (a.perm) id = a.perm[id];
             A[off + p] = ((unsigned long long)float_key(v) << 32) | id;
         }
         off += c;
     }
     __syncwarp();
     const uint32_t kth = team_select_hi(team, A, m0, a.k);
-    const float theta = a.bounds.margin ? PlainBound{a.bounds.margin[q]}.theta(key_float(kth))
-                                        : TensorBound{a.bounds.A[q], a.bounds.delta[q], a.bounds.eps2[q]}.theta(
+    const float theta = a.bounds.margin ? PlainBound{a.bounds.margin[slot]}.theta(key_float(kth))
+                                        : TensorBound{a.bounds.A[slot], a.bounds.delta[slot], a.bounds.eps2[slot]}.theta(
                                               key_float(kth));
     int m = 0;
     for (int b0 = 0; b0 < m0; b0 += 32) {
@@ -215,7 +222,7 @@ __global__ void __launch_bounds__(FB_THREADS) rerank_fallback_kernel(RerankArgs 
         const uint32_t row = row_s;
         __syncthreads();
         if (row == 0xffffffffu) break;
-        const int64_t q = row;
+        const int64_t q = input_row(a, row);
         for (int64_t j = tid; j < a.nr; j += blockDim.x)
             sc[j] = (a.self && j == q) ? __int_as_float(0x7f800000) : compute_r(a, q, (uint32_t)j);
         __syncthreads();
@@ -300,7 +307,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
                           const float* rx, const float* qnorm2, const float* rnorm2,
                           const double* qn64, const double* rn64, const float* qraw,
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
-                          uint32_t* out_idx, float* out_dist) {
+                          const uint32_t* perm, uint32_t* out_idx, float* out_dist) {
     cudaError_t e;
     uint32_t* fb_rows = (uint32_t*)ws_get(ctx, SLOT_FALLBACK_ROWS, sizeof(uint32_t) * (size_t)plan.nq, &e);
     if (!fb_rows) return e;
@@ -318,6 +325,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.rraw = rraw;
     a.bounds = bounds;
     a.lists = lists;
+    a.perm = perm;
     a.nq = plan.nq;
     a.nr = plan.nr;
     a.d = plan.d;

@@ -18,7 +18,15 @@ from mrustsc_gb300 import synthetic
 pytestmark = pytest.mark.gpu
 
 DIST_RTOL = 1e-6
-FORMS = ["plain", "tensor"]
+FORMS = ["plain", "tensor", "tensor-ordered"]
+
+
+def kw(form):
+    """Keyword arguments of a form id: the ordered tensor form forces the row
+    ordering on, so small inputs exercise the permuted operands and rerank."""
+    if form == "tensor-ordered":
+        return {"form": "tensor", "ordering": "on"}
+    return {"form": form}
 
 
 @pytest.fixture(scope="module")
@@ -46,10 +54,10 @@ def assert_exact(oracle, x, k, idx, dist, rows=None, metric="euclidean"):
 
 @pytest.mark.parametrize("form", FORMS)
 def test_line_and_grid_known_answers(scrust, form):
-    idx, dist = scrust.knn(refdata.line(6), 2, "auto", form=form)
+    idx, dist = scrust.knn(refdata.line(6), 2, "auto", **kw(form))
     assert idx[0].tolist() == [1, 2] and dist[0].tolist() == [1.0, 2.0]
     assert idx[2].tolist() == [1, 3] and idx[5].tolist() == [4, 3]
-    idx, dist = scrust.knn(refdata.grid(3), 4, "auto", form=form)
+    idx, dist = scrust.knn(refdata.grid(3), 4, "auto", **kw(form))
     assert idx[4].tolist() == [1, 3, 5, 7]
     assert idx[0].tolist() == [1, 3, 4, 2]
     assert abs(dist[0, 2] - np.sqrt(2.0)) < 1e-6 and abs(dist[0, 3] - 2.0) < 1e-6
@@ -59,7 +67,7 @@ def test_line_and_grid_known_answers(scrust, form):
 @pytest.mark.parametrize(("n", "d", "k"), [(64, 8, 1), (100, 5, 7), (257, 3, 15), (300, 32, 16)])
 def test_random_embeddings_match_fp64(scrust, oracle, n, d, k, form):
     x = refdata.random_embedding(n, d, n)
-    idx, dist = scrust.knn(x, k, "auto", form=form)
+    idx, dist = scrust.knn(x, k, "auto", **kw(form))
     assert_exact(oracle, x, k, idx, dist)
 
 
@@ -75,25 +83,25 @@ def test_reference_snap_equals_the_metal_twin(scrust, oracle, n, d, k):
 @pytest.mark.parametrize("form", FORMS)
 def test_largest_supported_k(scrust, oracle, form):
     x = refdata.random_embedding(128 + 71, 4, 7)
-    idx, dist = scrust.knn(x, 128, "auto", form=form)
+    idx, dist = scrust.knn(x, 128, "auto", **kw(form))
     assert_exact(oracle, x, 128, idx, dist)
 
 
 @pytest.mark.parametrize("form", FORMS)
 def test_line_ties_and_forty_duplicates(scrust, form):
-    idx, dist = scrust.knn(refdata.line(50), 2, "auto", form=form)
+    idx, dist = scrust.knn(refdata.line(50), 2, "auto", **kw(form))
     assert idx[10].tolist() == [9, 11] and dist[10].tolist() == [1.0, 1.0]
     x = np.zeros((41, 2), np.float32)
     x[40, 0] = 100.0
-    idx, _ = scrust.knn(x, 3, "auto", form=form)
+    idx, _ = scrust.knn(x, 3, "auto", **kw(form))
     assert idx[5].tolist() == [0, 1, 2] and idx[0].tolist() == [1, 2, 3]
 
 
 @pytest.mark.parametrize("form", FORMS)
 def test_two_runs_are_identical(scrust, form):
     x = refdata.random_embedding(500, 6, 11)
-    a = scrust.knn(x, 9, "auto", form=form)
-    b = scrust.knn(x, 9, "auto", form=form)
+    a = scrust.knn(x, 9, "auto", **kw(form))
+    b = scrust.knn(x, 9, "auto", **kw(form))
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
 
@@ -102,7 +110,7 @@ def test_two_runs_are_identical(scrust, form):
 def test_plain_small_workload_matches_fp64(scrust, oracle, form):
     x = synthetic.plain_small(seed=0)
     for k in (15, 14):
-        idx, dist = scrust.knn(x, k, "auto", form=form)
+        idx, dist = scrust.knn(x, k, "auto", **kw(form))
         assert_exact(oracle, x, k, idx, dist)
 
 
@@ -110,6 +118,8 @@ def test_plain_small_workload_matches_fp64(scrust, oracle, form):
 def test_tensor_precisions_match_fp64(scrust, oracle, precision):
     x = synthetic.mixture(6000, 50, clusters=20, dup_frac=0.01, near_dup_frac=0.01, seed=12)
     idx, dist = scrust.knn(x, 15, "auto", form="tensor", precision=precision)
+    assert_exact(oracle, x, 15, idx, dist)
+    idx, dist = scrust.knn(x, 15, "auto", form="tensor", precision=precision, ordering="on")
     assert_exact(oracle, x, 15, idx, dist)
 
 
@@ -136,7 +146,7 @@ def test_plain_small_reference_snap_matches_twin_and_cpu_path(scrust, oracle):
 @pytest.mark.parametrize("offset", [0.0, 1e2, 1e4, 1e5])
 def test_far_from_the_origin(scrust, oracle, offset, form):
     x = (np.random.default_rng(2).normal(size=(300, 12)) + offset).astype(np.float32)
-    idx, dist = scrust.knn(x, 14, "auto", form=form)
+    idx, dist = scrust.knn(x, 14, "auto", **kw(form))
     assert_exact(oracle, x, 14, idx, dist)
 
 
@@ -144,7 +154,7 @@ def test_far_from_the_origin(scrust, oracle, offset, form):
 def test_lattice_ties_break_towards_the_smaller_index(scrust, oracle, form):
     side = 8
     lattice = np.array([[i, j] for i in range(side) for j in range(side)], dtype=np.float32)
-    idx, dist = scrust.knn(lattice, 14, "auto", form=form)
+    idx, dist = scrust.knn(lattice, 14, "auto", **kw(form))
     assert_exact(oracle, lattice, 14, idx, dist)
 
 
@@ -152,12 +162,12 @@ def test_lattice_ties_break_towards_the_smaller_index(scrust, oracle, form):
 def test_duplicates_sit_at_distance_zero(scrust, oracle, form):
     x = refdata.audit_embedding(180, 6, 5)
     x[20:30] = x[20]
-    idx, dist = scrust.knn(x, 14, "auto", form=form)
+    idx, dist = scrust.knn(x, 14, "auto", **kw(form))
     assert np.count_nonzero(dist == 0.0) == 10 * 9
     assert_exact(oracle, x, 14, idx, dist)
     x = refdata.audit_embedding(200, 6, 9)
     x[:20] = x[0]
-    idx, dist = scrust.knn(x, 14, "auto", form=form)
+    idx, dist = scrust.knn(x, 14, "auto", **kw(form))
     assert np.count_nonzero(dist[:20]) == 0
     assert_exact(oracle, x, 14, idx, dist)
 
@@ -166,7 +176,7 @@ def test_duplicates_sit_at_distance_zero(scrust, oracle, form):
 def test_many_duplicates_take_the_fallback(scrust, oracle, form):
     x = synthetic.mixture(1500, 20, clusters=5, dup_frac=0.0, seed=4)
     x[100:500] = x[100]  # 400 identical cells: far more than any candidate list holds
-    idx, dist = scrust.knn(x, 15, "auto", form=form)
+    idx, dist = scrust.knn(x, 15, "auto", **kw(form))
     assert_exact(oracle, x, 15, idx, dist)
     assert idx[100].tolist() == list(range(101, 116))
 
@@ -186,17 +196,17 @@ def test_knot_below_resolution_collapses_like_the_reference(scrust, oracle):
 @pytest.mark.parametrize("form", FORMS)
 def test_near_duplicates_and_high_dimension(scrust, oracle, form):
     x = synthetic.mixture(3000, 50, clusters=12, dup_frac=0.02, near_dup_frac=0.02, seed=8)
-    idx, dist = scrust.knn(x, 30, "auto", form=form)
+    idx, dist = scrust.knn(x, 30, "auto", **kw(form))
     assert_exact(oracle, x, 30, idx, dist)
     x = synthetic.mixture(700, 130, clusters=6, dup_frac=0.01, seed=9)
-    idx, dist = scrust.knn(x, 10, "auto", form=form)
+    idx, dist = scrust.knn(x, 10, "auto", **kw(form))
     assert_exact(oracle, x, 10, idx, dist)
 
 
 @pytest.mark.parametrize("form", FORMS)
 def test_cosine_matches_fp64_cosine(scrust, oracle, form):
     x = synthetic.mixture(2000, 50, clusters=10, dup_frac=0.01, near_dup_frac=0.01, seed=3)
-    idx, dist = scrust.knn(x, 15, "auto", metric="cosine", form=form)
+    idx, dist = scrust.knn(x, 15, "auto", metric="cosine", **kw(form))
     assert_exact(oracle, x, 15, idx, dist, metric="cosine")
 
 
@@ -211,7 +221,7 @@ def test_cosine_rejects_zero_rows(scrust):
 @pytest.mark.parametrize("form", FORMS)
 def test_scale_workload_sampled_rows_match_fp64(scrust, oracle, form):
     x = synthetic.plain_scale(seed=0)
-    idx, dist = scrust.knn(x, 30, "auto", form=form)
+    idx, dist = scrust.knn(x, 30, "auto", **kw(form))
     n = len(x)
     assert np.all(np.diff(dist, axis=1) >= 0)
     assert not np.any(idx == np.arange(n, dtype=np.uint32)[:, None])
@@ -219,5 +229,5 @@ def test_scale_workload_sampled_rows_match_fp64(scrust, oracle, form):
     dups = np.nonzero((dist[:, :1] < 1e-2).ravel())[0]
     rows = np.unique(np.concatenate([rng.choice(n, 300, replace=False), dups[:100]]))
     assert_exact(oracle, x, 30, idx, dist, rows=rows)
-    ci, cd = scrust.knn(x, 30, "auto", metric="cosine", form=form)
+    ci, cd = scrust.knn(x, 30, "auto", metric="cosine", **kw(form))
     assert_exact(oracle, x, 30, ci, cd, rows=rows[:150], metric="cosine")
