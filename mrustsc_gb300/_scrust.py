@@ -66,11 +66,12 @@ def _k(k) -> int:
 
 
 def knn(embedding, k, device, *, metric: str = "euclidean", form: str = "plain", mode: str = "exact",
-        precision: str = "fp16", ordering: str = "auto"):
+        precision: str = "fp16", ordering: str = "auto", list_capacity: int = 0, segments: int = 0):
     """Exact k nearest neighbours, self excluded, nearest first, ties to the smaller id.
 
-    `ordering` ("auto", "off", "on") controls the tensor form's row ordering,
-    which changes the speed and never the result.
+    `ordering` ("auto", "off", "on") controls the tensor form's row ordering;
+    `list_capacity` and `segments` (0 = automatic) the candidate lists.  They
+    change the speed and never the result.
     """
     x = _array2(embedding, np.float32, "embedding")
     k = _k(k)
@@ -78,7 +79,8 @@ def knn(embedding, k, device, *, metric: str = "euclidean", form: str = "plain",
     n, d = x.shape
     L = _lib.lib()
     st = _lib.Status()
-    opts = _lib.options(form=form, metric=metric, mode=mode, precision=precision, ordering=ordering)
+    opts = _lib.options(form=form, metric=metric, mode=mode, precision=precision, ordering=ordering,
+                        list_capacity=list_capacity, segments=segments)
     ctx = None
     # Argument errors are reported before a device is required, as the
     # reference validates before dispatching (neighbors.rs:41-57).

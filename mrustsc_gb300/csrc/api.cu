@@ -91,7 +91,6 @@ void mark(scrust_context* ctx, Phase p) {
 namespace {
 
 constexpr uint32_t kMaxK = 128;
-constexpr int kRerankCapacity = 1024;
 constexpr int64_t kOrderMinRows = 65536;  // automatic ordering from this many rows
 
 int32_t check_knn_args(uint64_t n, uint64_t d, uint32_t k, scrust_status* st) {
@@ -166,7 +165,7 @@ int32_t plan_lists(scrust_context* ctx, const scrust_knn_options& o, int k, int 
         segments = (int)o.segments;
     } else if (row_blocks < blocks_wanted) {
         segments = (blocks_wanted + row_blocks - 1) / row_blocks;
-        segments = std::min(segments, std::max(1, kRerankCapacity / (4 * k)));
+        segments = std::min(segments, std::max(1, kRerankUnion / (4 * k)));
     }
     segments = std::max(1, std::min(segments, col_tiles));
     const int per = (col_tiles + segments - 1) / segments;
@@ -174,6 +173,7 @@ int32_t plan_lists(scrust_context* ctx, const scrust_knn_options& o, int k, int 
     int cap = (int)o.list_capacity;
     if (cap == 0) cap = std::max(default_cap, (2 * k + 32 + 31) / 32 * 32);
     cap = std::max(cap, k + 32);
+    cap = (cap + 3) / 4 * 4;  // lists start on 16-byte boundaries
     const int ctot = cap + headroom;
     if (ctot > 512)
         return fail(st, SCRUST_INVALID_PARAMETER, "list_capacity must be at most %d, got %d", 512 - headroom, cap);
@@ -298,8 +298,11 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
         ctx->launches += 2;
         // Headroom of 128: a tensor-form list is checked once per tile, after
         // its warp has appended up to 128 columns.
-        int32_t rc =
-            plan_lists(ctx, lo, (int)k, items, (int)(n_pad / 256), 8 * ctx->sm_count, 128, 64, &lists, st);
+        // Ordered solves keep long lists (256): a row block's first tiles
+        // fill its lists before any threshold exists, and every prune is a
+        // latency the row block waits for.
+        int32_t rc = plan_lists(ctx, lo, (int)k, items, (int)(n_pad / 256), 8 * ctx->sm_count, 128,
+                                order_rows ? 256 : 64, &lists, st);
         if (rc) return rc;
         lists.segments *= 2;  // one list per (column segment, column part) of a row
         if ((rc = alloc_lists(ctx, n_pad, &lists, st))) return rc;

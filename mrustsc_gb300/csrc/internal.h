@@ -125,6 +125,13 @@ struct KnnPlan {
     int segments = 1;
 };
 
+// Keys the rerank's warp path holds per row (the union of the row's lists);
+// larger unions take the fallback.
+constexpr int kRerankUnion = 1024;
+// Lists are cut to at most max(kListFinalMin, kRerankUnion / lists per row)
+// entries when a tensor-form work item ends.
+constexpr int kListFinalMin = 64;
+
 // Candidate lists as the candidate kernels write them and the rerank reads.
 struct Lists {
     uint32_t* ids = nullptr;

@@ -57,7 +57,6 @@ constexpr uint32_t A_BYTES = ROWS * TK * 2;
 constexpr uint32_t B_BYTES = TBN * TK * 2;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr size_t SMEM_BYTES = 2 * A_BYTES + STAGES * B_BYTES + 1024;
-constexpr int kFinalPrune = 64;  // lists longer than this are pruned once more when a work item ends
 constexpr int kPartCols = TBN / PARTS;  // columns one epilogue warp drains per tile
 
 struct TensorArgs {
@@ -80,6 +79,7 @@ struct TensorArgs {
     const uint32_t* tl_off;     // per-item offsets into tl, or null: item * tl_stride
     const uint32_t* tl_cnt;
     int tl_stride;
+    int final_cap;              // lists longer than this are pruned once more when an item ends
     int resume;                 // lists and thresholds continue from an earlier pass
     float* theta_io;            // per list: the threshold when the item ends (read when resuming)
 };
@@ -190,6 +190,112 @@ __device__ __forceinline__ void test_chunk(const uint32_t (&v)[32], int64_t colb
         append_chunk(v, colbase, th, chunk_valid(colbase, a.nr, a.self != 0, row), ids, vals, cnt);
 }
 
+// The K smallest values a lane has met (k <= K), ascending, in registers.
+// With it a lane's threshold follows its k-th smallest value chunk by chunk,
+// so its lists only receive columns inside the current bound and a prune is
+// a compaction, never a selection.
+template <int K>
+struct TopK {
+    float v[K];
+    __device__ __forceinline__ void reset() {
+#pragma unroll
+        for (int j = 0; j < K; j++) v[j] = __int_as_float(0x7f800000);
+    }
+    // x below v[K-1]: shifts the larger entries up by one (independent
+    // selects, no dependent chain).
+    __device__ __forceinline__ void insert(float x) {
+        bool gt[K];
+#pragma unroll
+        for (int j = 0; j < K; j++) gt[j] = v[j] > x;
+#pragma unroll
+        for (int j = K - 1; j > 0; j--) v[j] = gt[j - 1] ? v[j - 1] : (gt[j] ? x : v[j]);
+        v[0] = gt[0] ? x : v[0];
+    }
+    __device__ __forceinline__ float kth(int k) const {
+        float r = v[0];
+#pragma unroll
+        for (int j = 1; j < K; j++) r = (j == k - 1) ? v[j] : r;
+        return r;
+    }
+};
+
+__device__ __forceinline__ float pick32(const uint32_t (&v)[32], int j) {
+    float x = f_of(v[0]);
+#pragma unroll
+    for (int q = 1; q < 32; q++) x = (j == q) ? f_of(v[q]) : x;
+    return x;
+}
+
+// test_chunk with a register top-K: the chunk's columns below the K-th
+// smallest so far enter it, the threshold follows, then survivors append.
+template <int K>
+__device__ __forceinline__ void test_chunk_topk(const uint32_t (&v)[32], int64_t colbase, float& th, int64_t row,
+                                                const TensorArgs& a, uint32_t* ids, float* vals, uint32_t& cnt,
+                                                TopK<K>& top, const TensorBound& bnd) {
+    const float m = min32(v);
+    const uint32_t valid = chunk_valid(colbase, a.nr, a.self != 0, row);
+    if (__any_sync(0xffffffffu, m < top.v[K - 1])) {
+        const float lim = top.v[K - 1];
+        uint32_t want = 0;
+#pragma unroll
+        for (int j = 0; j < 32; j++) want |= (f_of(v[j]) < lim) ? (1u << j) : 0u;
+        want &= valid;
+        if (want) {
+            const float old = top.kth(a.k);
+            while (want) {
+                const int j = __ffs(want) - 1;
+                want &= want - 1;
+                const float x = pick32(v, j);
+                if (x < top.v[K - 1]) top.insert(x);
+            }
+            const float kth = top.kth(a.k);
+            if (kth < old) th = fminf(th, bnd.theta_f32(kth));
+        }
+    }
+    if (__any_sync(0xffffffffu, m < th)) append_chunk(v, colbase, th, valid, ids, vals, cnt);
+}
+
+// Drops, in place, the entries of a lane's list at or above theta; eight
+// entries are read before any is written back.
+__device__ __forceinline__ uint32_t compact_lane(uint32_t* ids, float* vals, uint32_t cnt, float theta) {
+    uint32_t out = 0;
+#pragma unroll 1
+    for (uint32_t e0 = 0; e0 < cnt; e0 += 8) {
+        float x[8];
+        uint32_t id[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const bool in = e0 + q < cnt;
+            x[q] = in ? vals[e0 + q] : __int_as_float(0x7f800000);
+            id[q] = in ? ids[e0 + q] : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            if (x[q] < theta) {
+                ids[out] = id[q];
+                vals[out] = x[q];
+                out++;
+            }
+        }
+    }
+    return out;
+}
+
+// Applies a prune result to a lane's registers: a list that keeps `cap` or
+// more entries inside its own threshold overflows to the exact fallback.
+__device__ __forceinline__ void take_prune(const PruneResult& r, const TensorArgs& a, int64_t row, float& th,
+                                           uint32_t& cnt, uint32_t& n_ovf) {
+    if ((int)r.cnt >= a.lists.cap) {
+        a.lists.overflow[row] = 1u;
+        th = __int_as_float(0xff800000);
+        cnt = 0;
+        n_ovf++;
+    } else {
+        th = r.theta;
+        cnt = r.cnt;
+    }
+}
+
 // Prunes, with the whole warp, the lists of the lanes set in `need`; each
 // lane keeps its own threshold and count in registers.
 __device__ __forceinline__ void prune_lanes(uint32_t need, const TensorArgs& a, int seg, int64_t row,
@@ -208,20 +314,13 @@ __device__ __forceinline__ void prune_lanes(uint32_t need, const TensorArgs& a, 
         const int64_t off = (lrow * segs + seg) * (int64_t)a.lists.ctot;  // seg: list slot within the row
         const PruneResult r =
             prune_core(a.lists.ids + off, a.lists.vals + off, min(lc, (uint32_t)a.lists.ctot), a.k, lb, lth, hist);
-        if (lane == l) {
-            if ((int)r.cnt >= a.lists.cap) {
-                a.lists.overflow[row] = 1u;
-                th = __int_as_float(0xff800000);
-                cnt = 0;
-                n_ovf++;
-            } else {
-                th = r.theta;
-                cnt = r.cnt;
-            }
-        }
+        if (lane == l) take_prune(r, a, row, th, cnt, n_ovf);
     }
 }
 
+// TOPK = K (k <= K, K = 1 or 16): thresholds from a register top-K per lane
+// (TopK); TOPK = 0: from warp-cooperative selections over the lists.
+template <int TOPK>
 __global__ void __launch_bounds__(THREADS, 1)
     tensor_candidates_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
                              TensorArgs a) {
@@ -388,6 +487,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         volatile unsigned long long* other_th = &theta_s[h][part ^ 1][r_local];
         uint32_t tc = 0;
         uint32_t n_app = 0, n_prune = 0, n_ovf = 0;
+        long long c_prune = 0, c_wait = 0;
         bool ok = true;
         for (int w = blockIdx.x; w < a.items && ok; w += gridDim.x) {
             const int qt = w / col_segs, seg = w % col_segs;
@@ -410,12 +510,16 @@ __global__ void __launch_bounds__(THREADS, 1)
             float* vals = a.lists.vals + lslot * (int64_t)a.lists.ctot;
             const uint64_t tag = (uint64_t)(uint32_t)w << 32;
             *my_th = tag | __float_as_uint(th);
+            TopK<(TOPK > 0 ? TOPK : 1)> top;
+            if constexpr (TOPK > 0) top.reset();
             for (int it = 0; it < order.count; ++it) {
                 const int ct = order.next(it);
+                const long long w0 = a.stats ? clock64() : 0;
                 if (!mbar_wait_bounded(&tfull[h], tc & 1, a.err)) {
                     ok = false;
                     break;
                 }
+                if (a.stats) c_wait += clock64() - w0;
                 tc_fence_after();
                 // The partner part's threshold bounds this row just as well.
                 const unsigned long long o = *other_th;
@@ -423,6 +527,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const int64_t col0 = (int64_t)ct * TBN + part * kPartCols;
                 const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(h * TBN + part * kPartCols);
                 const uint32_t before = cnt;
+                const float th_before = th;
                 {
                     // Four 32-column chunks; each TMEM load overlaps the
                     // previous chunk's threshold test.
@@ -430,15 +535,19 @@ __global__ void __launch_bounds__(THREADS, 1)
                     tmem_ld32(tbase, va);
                     tmem_ld_wait(va);
                     tmem_ld32(tbase + 32, vb);
-                    test_chunk(va, col0, th, row, a, ids, vals, cnt);
+                    if constexpr (TOPK > 0) test_chunk_topk(va, col0, th, row, a, ids, vals, cnt, top, bnd);
+                    else test_chunk(va, col0, th, row, a, ids, vals, cnt);
                     tmem_ld_wait(vb);
                     tmem_ld32(tbase + 64, va);
-                    test_chunk(vb, col0 + 32, th, row, a, ids, vals, cnt);
+                    if constexpr (TOPK > 0) test_chunk_topk(vb, col0 + 32, th, row, a, ids, vals, cnt, top, bnd);
+                    else test_chunk(vb, col0 + 32, th, row, a, ids, vals, cnt);
                     tmem_ld_wait(va);
                     tmem_ld32(tbase + 96, vb);
-                    test_chunk(va, col0 + 64, th, row, a, ids, vals, cnt);
+                    if constexpr (TOPK > 0) test_chunk_topk(va, col0 + 64, th, row, a, ids, vals, cnt, top, bnd);
+                    else test_chunk(va, col0 + 64, th, row, a, ids, vals, cnt);
                     tmem_ld_wait(vb);
-                    test_chunk(vb, col0 + 96, th, row, a, ids, vals, cnt);
+                    if constexpr (TOPK > 0) test_chunk_topk(vb, col0 + 96, th, row, a, ids, vals, cnt, top, bnd);
+                    else test_chunk(vb, col0 + 96, th, row, a, ids, vals, cnt);
                 }
                 // Release the accumulator before any prune, so the tensor
                 // core refills it while this warp prunes.
@@ -448,19 +557,37 @@ __global__ void __launch_bounds__(THREADS, 1)
                 n_app += cnt - before;
                 const uint32_t need = __ballot_sync(0xffffffffu, cnt >= (uint32_t)cap);
                 if (need) {
+                    const long long p0 = a.stats ? clock64() : 0;
                     n_prune += __popc(need);
-                    prune_lanes(need, a, seg * PARTS + part, row, bnd, th, cnt, n_ovf, hist_s[e]);
-                    *my_th = tag | __float_as_uint(th);
+                    if constexpr (TOPK > 0) {
+                        if (cnt >= (uint32_t)cap)
+                            take_prune(PruneResult{th, compact_lane(ids, vals, min(cnt, (uint32_t)a.lists.ctot), th)},
+                                       a, row, th, cnt, n_ovf);
+                        __syncwarp();
+                    } else {
+                        prune_lanes(need, a, seg * PARTS + part, row, bnd, th, cnt, n_ovf, hist_s[e]);
+                    }
+                    if (a.stats) c_prune += clock64() - p0;
                 }
+                if (__any_sync(0xffffffffu, th != th_before)) *my_th = tag | __float_as_uint(th);
                 tc++;
             }
-            // A last prune keeps every finished list short, so the union of a
-            // row's lists stays within the rerank's capacity.
+            // A last prune keeps every finished list short enough for the
+            // union of a row's lists to fit the rerank.
             if (ok) {
-                const uint32_t need = __ballot_sync(0xffffffffu, cnt > (uint32_t)kFinalPrune);
+                const uint32_t need = __ballot_sync(0xffffffffu, cnt > (uint32_t)a.final_cap);
                 if (need) {
+                    const long long p0 = a.stats ? clock64() : 0;
                     n_prune += __popc(need);
-                    prune_lanes(need, a, seg * PARTS + part, row, bnd, th, cnt, n_ovf, hist_s[e]);
+                    if constexpr (TOPK > 0) {
+                        if (cnt > (uint32_t)a.final_cap)
+                            take_prune(PruneResult{th, compact_lane(ids, vals, min(cnt, (uint32_t)a.lists.ctot), th)},
+                                       a, row, th, cnt, n_ovf);
+                        __syncwarp();
+                    } else {
+                        prune_lanes(need, a, seg * PARTS + part, row, bnd, th, cnt, n_ovf, hist_s[e]);
+                    }
+                    if (a.stats) c_prune += clock64() - p0;
                 }
             }
             if (valid && ok) {
@@ -478,6 +605,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                 atomicAdd(a.stats + TS_APPENDS, s_app);
                 atomicAdd(a.stats + TS_OVERFLOWS, s_ovf);
                 atomicAdd(a.stats + TS_PRUNES, (unsigned long long)n_prune);
+                atomicAdd(a.stats + TS_PRUNE_CYCLES, (unsigned long long)c_prune);
+                atomicAdd(a.stats + TS_EPI_WAIT, (unsigned long long)c_wait);
             }
         }
     }
@@ -653,6 +782,8 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.tiles_per_seg = (a.col_tiles + col_segs - 1) / col_segs;
     if ((a.col_tiles + a.tiles_per_seg - 1) / a.tiles_per_seg != col_segs) return cudaErrorInvalidValue;
     if (lists.ctot < lists.cap + kPartCols || lists.ctot > 32 * kListMaxEntriesPerLane) return cudaErrorInvalidValue;
+    // The rerank takes the union of a row's lists: up to kRerankUnion keys.
+    a.final_cap = std::max(kListFinalMin, kRerankUnion / lists.segments);
     if (lists.segments % PARTS) return cudaErrorInvalidValue;
     a.items = (int)(nq_pad / ROWS) * (lists.segments / PARTS);
     a.idesc = umma_idesc_f16(TBM, TBN, bf16);
@@ -673,12 +804,13 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.resume = resume ? 1 : 0;
     a.theta_io = theta_io;
     if (resume && !theta_io) return cudaErrorInvalidValue;
-    cudaError_t e =
-        cudaFuncSetAttribute(tensor_candidates_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+    auto kern = a.k == 1 ? tensor_candidates_kernel<1> : a.k <= 16 ? tensor_candidates_kernel<16>
+                                                                   : tensor_candidates_kernel<0>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
     if (e != cudaSuccess) return e;
     const int grid = std::min(a.items, ctx->sm_count);
     if (grid_out) *grid_out = grid;
-    tensor_candidates_kernel<<<grid, THREADS, SMEM_BYTES, ctx->stream>>>(ta, tb, a);
+    kern<<<grid, THREADS, SMEM_BYTES, ctx->stream>>>(ta, tb, a);
     return cudaGetLastError();
 }
 

@@ -37,6 +37,14 @@ struct TensorBound {
         const double th = r * r + (double)delta - (double)A;
         return __double2float_ru(th + 1e-6 * fabs(th) + 1e-30);
     }
+    // The same bound in f32 with every step rounded towards +inf, then
+    // raised past itself: never at or below the exact bound.
+    __device__ __forceinline__ float theta_f32(float kth) const {
+        const float q = __fadd_ru(fmaxf(0.f, __fadd_ru(kth, A)), delta);
+        const float r = __fadd_ru(__fsqrt_ru(q), eps2);
+        const float th = __fsub_ru(__fadd_ru(__fmul_ru(r, r), delta), A);
+        return __fadd_ru(__fadd_ru(th, __fmul_ru(fabsf(th), 1e-6f)), 1e-30f);
+    }
 };
 
 struct PruneResult {

@@ -403,81 +403,128 @@ __device__ __forceinline__ bool tile_needed(float dc2, float rI, float rT, float
     return !(dc >= (double)rI + (double)rT + (double)uI * (1.0 + 1e-5) + 1e-4);
 }
 
-// One block per row block I: the tiles of the second pass, i.e. the tiles
-// not in I's priority list that may still add to I, in ascending order.  The
-// whole-tile balls decide first; a pair they cannot separate is tested ball
-// by ball over the cell segments.  Without `offsets` it only counts.
-__global__ void __launch_bounds__(256) tile_lists_kernel(TileBalls b, int d, int tiles,
-                                                         const uint32_t* __restrict__ prio,
-                                                         const uint32_t* __restrict__ prio_cnt,
-                                                         const uint32_t* __restrict__ offsets,
-                                                         uint32_t* __restrict__ counts, uint32_t* __restrict__ entries) {
-    __shared__ float cI[64];
-    __shared__ float sI[kSegMax][64];
-    __shared__ float srI[kSegMax], suI[kSegMax];
-    __shared__ uint32_t pl[kPrioMax];
-    __shared__ int wsum[8];
-    __shared__ int base_s;
-    const int I = blockIdx.x;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int pc = (int)min(prio_cnt[I], (uint32_t)kPrioMax);
-    const int nsI = (int)min(b.nseg[I], (uint32_t)kSegMax);
-    if (threadIdx.x < d) cI[threadIdx.x] = b.centre[(int64_t)threadIdx.x * tiles + I];
-    for (int p = threadIdx.x; p < nsI * d; p += blockDim.x)
-        sI[p / d][p % d] = b.seg_centre[((int64_t)(p / d) * d + p % d) * tiles + I];
-    if (threadIdx.x < nsI) {
-        srI[threadIdx.x] = b.seg_radius[(int64_t)threadIdx.x * tiles + I];
-        suI[threadIdx.x] = b.seg_reach[(int64_t)threadIdx.x * tiles + I];
+// The cell-segment balls of all tiles, one row each (centres padded to 64
+// dimensions with zeros), in tile order.
+__global__ void flatten_segments_kernel(TileBalls b, int d, int tiles, const uint32_t* __restrict__ seg_off,
+                                        float* __restrict__ fc, float* __restrict__ fr, float* __restrict__ fu,
+                                        uint32_t* __restrict__ fo) {
+    const int T = blockIdx.x;
+    const int ns = (int)min(b.nseg[T], (uint32_t)kSegMax);
+    const uint32_t o = seg_off[T];
+    for (int p = threadIdx.x; p < ns * 64; p += blockDim.x) {
+        const int sg = p / 64, t = p % 64;
+        fc[(int64_t)(o + sg) * 64 + t] = t < d ? b.seg_centre[((int64_t)sg * d + t) * tiles + T] : 0.f;
     }
-    if (threadIdx.x < pc) pl[threadIdx.x] = prio[(int64_t)I * kPrioMax + threadIdx.x];
-    if (threadIdx.x == 0) base_s = 0;
-    __syncthreads();
-    const float rI = b.radius[I], uI = b.reach[I];
-    const uint32_t off = offsets ? offsets[I] : 0u;
-    for (int t0 = 0; t0 < tiles; t0 += 256) {
-        const int T = t0 + threadIdx.x;
-        bool keep = false;
-        if (T < tiles) {
-            bool in_prio = false;
-            for (int q = 0; q < pc; ++q) in_prio |= pl[q] == (uint32_t)T;
-            if (!in_prio) {
-                float dc2 = 0.f;
-                for (int t = 0; t < d; ++t) {
-                    const float df = cI[t] - b.centre[(int64_t)t * tiles + T];
-                    dc2 = fmaf(df, df, dc2);
+    if (threadIdx.x < ns) {
+        fr[o + threadIdx.x] = b.seg_radius[(int64_t)threadIdx.x * tiles + T];
+        fu[o + threadIdx.x] = b.seg_reach[(int64_t)threadIdx.x * tiles + T];
+        fo[o + threadIdx.x] = (uint32_t)T;
+    }
+}
+
+// All pairs of segment balls, 64 x 64 per block step, 4 x 4 per thread:
+// when segment i (of row block owner[i]) may reach segment j (of tile
+// owner[j]), bit (owner[i], owner[j]) of the reach bitmap is set.  The
+// segment count S is read on the device; blocks stride over the block pairs.
+constexpr int SP = 64;
+__global__ void __launch_bounds__(256) segment_pairs_kernel(const float* __restrict__ fc, const float* __restrict__ fr,
+                                                            const float* __restrict__ fu,
+                                                            const uint32_t* __restrict__ fo,
+                                                            const uint32_t* __restrict__ S_ptr, int d, int words,
+                                                            uint32_t* __restrict__ bitmap) {
+    __shared__ __align__(16) float As[64][SP];
+    __shared__ __align__(16) float Bs[64][SP];
+    const int S = (int)*S_ptr;
+    const int nb = (S + SP - 1) / SP;
+    const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+    for (int64_t bp = blockIdx.x; bp < (int64_t)nb * nb; bp += gridDim.x) {
+        const int i0 = (int)(bp / nb) * SP, j0 = (int)(bp % nb) * SP;
+        __syncthreads();
+        for (int p = threadIdx.x; p < SP * 64; p += blockDim.x) {
+            const int r = p / 64, t = p % 64;
+            As[t][r] = i0 + r < S ? fc[(int64_t)(i0 + r) * 64 + t] : 0.f;
+            Bs[t][r] = j0 + r < S ? fc[(int64_t)(j0 + r) * 64 + t] : 0.f;
+        }
+        __syncthreads();
+        float acc[4][4] = {};
+        for (int t = 0; t < d; ++t) {
+            const float4 a4 = *reinterpret_cast<const float4*>(&As[t][ty * 4]);
+            const float4 b4 = *reinterpret_cast<const float4*>(&Bs[t][tx * 4]);
+            const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float df = av[p] - bv[q];
+                    acc[p][q] = fmaf(df, df, acc[p][q]);
                 }
-                keep = tile_needed(dc2, rI, b.radius[T], uI);
-                const int nsT = (int)min(b.nseg[T], (uint32_t)kSegMax);
-                if (keep && (nsI > 1 || nsT > 1)) {
-                    keep = false;
-                    for (int sb = 0; sb < nsT && !keep; ++sb) {
-                        const float rT = b.seg_radius[(int64_t)sb * tiles + T];
-                        for (int sa = 0; sa < nsI && !keep; ++sa) {
-                            float e2 = 0.f;
-                            for (int t = 0; t < d; ++t) {
-                                const float df = sI[sa][t] - b.seg_centre[((int64_t)sb * d + t) * tiles + T];
-                                e2 = fmaf(df, df, e2);
-                            }
-                            keep = tile_needed(e2, srI[sa], rT, suI[sa]);
-                        }
-                    }
+        }
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            const int i = i0 + ty * 4 + p;
+            if (i >= S) continue;
+            const float ri = fr[i], ui = fu[i];
+            const uint32_t oi = fo[i];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = j0 + tx * 4 + q;
+                if (j >= S) continue;
+                if (tile_needed(acc[p][q], ri, fr[j], ui)) {
+                    const uint32_t oj = fo[j];
+                    atomicOr(bitmap + (int64_t)oi * words + (oj >> 5), 1u << (oj & 31));
                 }
             }
         }
-        const uint32_t bal = __ballot_sync(0xffffffffu, keep);
-        if (lane == 0) wsum[w] = __popc(bal);
+    }
+}
+
+// One block per row block I: the tiles of its reach bitmap row that are not
+// in its priority list, ascending, at entries[I * tiles ...].
+__global__ void __launch_bounds__(256) tile_lists_kernel(const uint32_t* __restrict__ bitmap, int words, int tiles,
+                                                         const uint32_t* __restrict__ prio,
+                                                         const uint32_t* __restrict__ prio_cnt,
+                                                         uint32_t* __restrict__ counts, uint32_t* __restrict__ entries) {
+    extern __shared__ uint32_t in_prio[];  // words
+    __shared__ int wsum[8];
+    const int I = blockIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int pc = (int)min(prio_cnt[I], (uint32_t)kPrioMax);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) in_prio[i] = 0u;
+    __syncthreads();
+    if (threadIdx.x < pc) {
+        const uint32_t t = prio[(int64_t)I * kPrioMax + threadIdx.x];
+        if (t < (uint32_t)tiles) atomicOr(&in_prio[t >> 5], 1u << (t & 31));
+    }
+    __syncthreads();
+    const uint32_t* row = bitmap + (int64_t)I * words;
+    uint32_t* out = entries + (int64_t)I * tiles;
+    int base = 0;
+    for (int w0 = 0; w0 < words; w0 += 256) {
+        const int wd = w0 + threadIdx.x;
+        uint32_t bits = wd < words ? row[wd] & ~in_prio[wd] : 0u;
+        int c = __popc(bits);
+        int incl = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) wsum[w] = incl;
         __syncthreads();
         int before = 0, total = 0;
         for (int q = 0; q < 8; ++q) {
             before += q < w ? wsum[q] : 0;
             total += wsum[q];
         }
-        if (offsets && keep) entries[off + base_s + before + __popc(bal & lanemask_lt())] = (uint32_t)T;
-        __syncthreads();
-        if (threadIdx.x == 0) base_s += total;
+        int pos = base + before + incl - c;
+        while (bits) {
+            const int bt = __ffs(bits) - 1;
+            bits &= bits - 1;
+            out[pos++] = (uint32_t)(wd * 32 + bt);
+        }
+        base += total;
         __syncthreads();
     }
-    if (!offsets && threadIdx.x == 0) counts[I] = (uint32_t)base_s;
+    if (threadIdx.x == 0) counts[I] = (uint32_t)base;
 }
 
 }  // namespace
@@ -567,8 +614,8 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     px.self = false;
     px.form = SCRUST_FORM_TENSOR;
     Lists lx;
-    lx.cap = 64;
-    lx.ctot = 64 + 128;
+    lx.cap = 256;
+    lx.ctot = 256 + 128;
     lx.segments = 2;
     int32_t rc = alloc_lists(ctx, n_pad, &lx, st);
     if (rc) return rc;
@@ -616,18 +663,22 @@ int32_t build_second_pass(scrust_context* ctx, const void* A16, bool bf16, int64
     cudaStream_t s = ctx->stream;
     cudaError_t e = cudaSuccess;
     const int tiles = (int)((n + 255) / 256);
-    const size_t scan_elems = scan_scratch_elems((int64_t)tiles + 1);
     size_t off = 0;
     auto take = [&](size_t bytes) {
         const size_t o = off;
         off = align_up(off + bytes);
         return o;
     };
+    const int words = (tiles + 31) / 32;
+    const int64_t smax = (int64_t)tiles * kSegMax;
+    const size_t scan_elems = scan_scratch_elems((int64_t)tiles + 1);
     const size_t o_c = take(4 * (size_t)d * tiles), o_r = take(4 * (size_t)tiles), o_u = take(4 * (size_t)tiles),
                  o_sc = take(4 * (size_t)kSegMax * d * tiles), o_sr = take(4 * (size_t)kSegMax * tiles),
-                 o_su = take(4 * (size_t)kSegMax * tiles), o_ns = take(4 * (size_t)tiles),
-                 o_cnt = take(4 * ((size_t)tiles + 1)), o_off = take(4 * ((size_t)tiles + 1)),
-                 o_scan = take(4 * scan_elems), o_ent = take(4 * (size_t)tiles * (size_t)tiles);
+                 o_su = take(4 * (size_t)kSegMax * tiles), o_ns = take(4 * ((size_t)tiles + 1)),
+                 o_so = take(4 * ((size_t)tiles + 1)), o_fc = take(4 * 64 * (size_t)smax), o_fr = take(4 * (size_t)smax),
+                 o_fu = take(4 * (size_t)smax), o_fo = take(4 * (size_t)smax), o_scan = take(4 * scan_elems),
+                 o_bm = take(4 * (size_t)tiles * words), o_cnt = take(4 * ((size_t)tiles + 1)),
+                 o_ent = take(4 * (size_t)tiles * (size_t)tiles);
     char* base = (char*)ws_get(ctx, SLOT_PRUNE, off, &e);
     if (!base) return cuda_fail(st, e, "pruning: workspace");
     TileBalls balls;
@@ -638,9 +689,17 @@ int32_t build_second_pass(scrust_context* ctx, const void* A16, bool bf16, int64
     balls.seg_radius = (float*)(base + o_sr);
     balls.seg_reach = (float*)(base + o_su);
     balls.nseg = (uint32_t*)(base + o_ns);
+    uint32_t* seg_off = (uint32_t*)(base + o_so);
+    float* fc = (float*)(base + o_fc);
+    float* fr = (float*)(base + o_fr);
+    float* fu = (float*)(base + o_fu);
+    uint32_t* fo = (uint32_t*)(base + o_fo);
+    uint32_t* bitmap = (uint32_t*)(base + o_bm);
     uint32_t* counts = (uint32_t*)(base + o_cnt);
-    uint32_t* offsets = (uint32_t*)(base + o_off);
     uint32_t* entries = (uint32_t*)(base + o_ent);
+    if ((e = cudaMemsetAsync(balls.nseg + tiles, 0, sizeof(uint32_t), s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(bitmap, 0, 4 * (size_t)tiles * words, s)) != cudaSuccess)
+        return cuda_fail(st, e, "pruning: memset");
     if (bf16)
         tile_balls_kernel<__nv_bfloat16><<<tiles, 256, 0, s>>>((const __nv_bfloat16*)A16, n, d, tiles,
                                                                order.cell_of_pos, order.theta, bA, bdelta, balls);
@@ -648,20 +707,24 @@ int32_t build_second_pass(scrust_context* ctx, const void* A16, bool bf16, int64
         tile_balls_kernel<__half><<<tiles, 256, 0, s>>>((const __half*)A16, n, d, tiles, order.cell_of_pos,
                                                         order.theta, bA, bdelta, balls);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "pruning: tile balls");
-    if ((e = cudaMemsetAsync(counts + tiles, 0, sizeof(uint32_t), s)) != cudaSuccess)
-        return cuda_fail(st, e, "pruning: memset");
-    tile_lists_kernel<<<tiles, 256, 0, s>>>(balls, d, tiles, order.prio, order.prio_cnt, nullptr, counts, nullptr);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "pruning: tile counts");
-    if ((e = device_exclusive_scan(ctx, counts, offsets, (int64_t)tiles + 1, (uint32_t*)(base + o_scan),
+    if ((e = device_exclusive_scan(ctx, balls.nseg, seg_off, (int64_t)tiles + 1, (uint32_t*)(base + o_scan),
                                    scan_elems)) != cudaSuccess)
-        return cuda_fail(st, e, "pruning: scan");
-    tile_lists_kernel<<<tiles, 256, 0, s>>>(balls, d, tiles, order.prio, order.prio_cnt, offsets, counts, entries);
+        return cuda_fail(st, e, "pruning: segment scan");
+    flatten_segments_kernel<<<tiles, 64, 0, s>>>(balls, d, tiles, seg_off, fc, fr, fu, fo);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "pruning: segments");
+    segment_pairs_kernel<<<8 * ctx->sm_count, 256, 0, s>>>(fc, fr, fu, fo, seg_off + tiles, d, words, bitmap);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "pruning: segment pairs");
+    const size_t lists_smem = 4 * (size_t)words;
+    if ((e = cudaFuncSetAttribute(tile_lists_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lists_smem)) !=
+        cudaSuccess)
+        return cuda_fail(st, e, "pruning: tile lists");
+    tile_lists_kernel<<<tiles, 256, lists_smem, s>>>(bitmap, words, tiles, order.prio, order.prio_cnt, counts, entries);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "pruning: tile lists");
     ctx->launches += 3;
     out->tiles = entries;
-    out->offset = offsets;
+    out->offset = nullptr;
     out->count = counts;
-    out->stride = 0;
+    out->stride = tiles;
     return SCRUST_OK;
 }
 

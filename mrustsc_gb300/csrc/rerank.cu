@@ -22,7 +22,7 @@ namespace scrust {
 namespace {
 
 constexpr int RR_WARPS = 4;
-constexpr int RC = 1024;      // keys per warp
+constexpr int RC = kRerankUnion;  // keys per warp
 constexpr int FB_CAP = 4096;  // keys per fallback block
 constexpr int FB_THREADS = 256;
 constexpr int FB_BLOCKS = 32;

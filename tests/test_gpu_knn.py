@@ -123,6 +123,24 @@ def test_tensor_precisions_match_fp64(scrust, oracle, precision):
     assert_exact(oracle, x, 15, idx, dist)
 
 
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("k,cap", [(15, 47), (24, 60), (40, 90)])
+def test_small_list_capacity_forces_prunes(scrust, oracle, form, k, cap):
+    """Short lists prune after nearly every tile: both prune paths (one list
+    per lane for k <= 32, one list per warp above) and the overflow path."""
+    x = synthetic.mixture(5000, 30, clusters=10, dup_frac=0.01, seed=21)
+    idx, dist = scrust.knn(x, k, "auto", list_capacity=cap, **kw(form))
+    assert_exact(oracle, x, k, idx, dist)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_explicit_segments(scrust, oracle, form):
+    x = synthetic.mixture(3000, 20, clusters=6, dup_frac=0.01, seed=22)
+    for segments in (1, 2, 3):
+        idx, dist = scrust.knn(x, 12, "auto", segments=segments, **kw(form))
+        assert_exact(oracle, x, 12, idx, dist)
+
+
 def test_plain_small_reference_snap_matches_twin_and_cpu_path(scrust, oracle):
     x = synthetic.plain_small(seed=1)
     idx, dist = scrust.knn(x, 15, "auto", mode="reference_snap")
