@@ -43,7 +43,7 @@ FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustain
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--form", choices=["plain", "tensor"], default=None)
@@ -78,7 +78,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
         except Exception:
             self.proc = None
@@ -258,7 +258,7 @@ def run_ours(args):
     clocks.start()
     launches0 = L.scrust_cuda_launch_count(ctx)
     phases = []
-    buf = (ctypes.c_float * 4)()
+    buf = (ctypes.c_float * 6)()
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
     total_ms = 0.0
@@ -268,7 +268,7 @@ def run_ours(args):
         end.record(stream)
         end.synchronize()
         total_ms += start.elapsed_time(end)
-        got = L.scrust_cuda_phase_times(ctx, buf, 4)
+        got = L.scrust_cuda_phase_times(ctx, buf, 6)
         phases.append([buf[i] for i in range(got)])
     torch.cuda.synchronize()
     launches = int(L.scrust_cuda_launch_count(ctx) - launches0)
@@ -283,17 +283,35 @@ def run_ours(args):
         torch.distributed.barrier()
     value = world * n / (ms_step / 1e3)
 
-    ph = np.array(phases) if phases and len(phases[0]) == 4 else np.zeros((1, 4))
+    ph = np.array(phases) if phases and len(phases[0]) == 6 else np.zeros((1, 6))
     ph_mean = ph.mean(0)
     cand_ms = float(ph_mean[1])
     pk, pk_kind = peaks()
-    flops = 2.0 * n * n * d
     if form == "tensor":
-        achieved = flops / (cand_ms / 1e3) / 1e12
+        # The dominant kernel is the tensor sweep (knn_candidates_tc): its two
+        # passes are timed by the library's events on its stream (the
+        # candidates phase less the building of the second pass's tile
+        # lists).  Its unit of work is one (256-row block, 256-column tile)
+        # pair, 2 * 256 * 256 * d algorithmic flops; the pairs it computes are
+        # counted by the kernel's own counters in one extra, untimed step.
+        sweep_ms = cand_ms - float(ph_mean[5]) if ph_mean[4] > 0 else cand_ms
+        out = (ctypes.c_uint64 * 16)()
+        L.scrust_cuda_kernel_stats(ctx, 1, out, 16)
+        step()
+        _lib.check(L.scrust_cuda_synchronize(ctx, ctypes.byref(st)), st)
+        L.scrust_cuda_kernel_stats(ctx, 0, out, 16)
+        tiles = int(out[8])
+        blocks = (n + 255) // 256
+        flops = tiles * 2.0 * 256 * 256 * d
+        achieved = flops / (sweep_ms / 1e3) / 1e12
         roof = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                 "frac": achieved / pk["bf16_tflops"], "traffic": None,
-                "kernel": "knn_candidates_tc", "peak_source": pk_kind}
+                "kernel": "tensor_candidates_kernel (knn_candidates_tc), both sweep passes",
+                "kernel_ms": sweep_ms, "units": "(256-row block, 256-column tile) pairs computed",
+                "units_per_step": tiles, "flops_per_unit": 2 * 256 * 256 * d,
+                "brute_force_units": blocks * blocks, "peak_source": f"bf16 burst, {pk_kind}"}
     else:
+        flops = 2.0 * n * n * d
         sm_count = torch.cuda.get_device_properties(local).multi_processor_count
         fp32_peak = sm_count * 128 * 2 * float(pk.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
         achieved = flops / (cand_ms / 1e3) / 1e12
@@ -310,7 +328,9 @@ def run_ours(args):
                        "mode": "exact", "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (200 MB embedding, >1 GB candidate lists per step)"},
             "phases_ms": {"prep": float(ph_mean[0]), "candidates": float(ph_mean[1]),
-                          "rerank": float(ph_mean[2]), "connectivities": float(ph_mean[3])},
+                          "rerank": float(ph_mean[2]), "connectivities": float(ph_mean[3]),
+                          "candidates_first_pass": float(ph_mean[4]),
+                          "candidates_tile_lists": float(ph_mean[5])},
             "gpu_launches": launches, "roofline": roof, "clocks": clk}
 
     if rank == 0 and not args.no_recall:

@@ -211,7 +211,9 @@ SCRUST_API int32_t scrust_cuda_smooth_knn_distances_noalloc(const float* distanc
 /* Phase timing.  When enabled, each kNN / connectivities call records CUDA
  * events on the context stream around its phases; scrust_cuda_phase_times
  * writes the last call's milliseconds (after a synchronise) in the order
- * prep, candidates, rerank, connectivities and returns how many it wrote. */
+ * prep, candidates, rerank, connectivities, then two parts of candidates in
+ * an ordered tensor-form solve (its first sweep pass and the building of the
+ * second pass's tile lists; 0 otherwise), and returns how many it wrote. */
 SCRUST_API void scrust_cuda_set_timing(scrust_context* context, int32_t enable);
 SCRUST_API int32_t scrust_cuda_phase_times(scrust_context* context, float* ms, int32_t max_phases);
 

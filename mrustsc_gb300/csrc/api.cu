@@ -84,7 +84,7 @@ void mark(scrust_context* ctx, Phase p) {
     if (!ctx->timing) return;
     if (!ctx->ev[p] && cudaEventCreate(&ctx->ev[p]) != cudaSuccess) return;
     if (p == PH_START)
-        for (int i = 0; i < 5; i++) ctx->ev_recorded[i] = false;
+        for (int i = 0; i < 7; i++) ctx->ev_recorded[i] = false;
     if (cudaEventRecord(ctx->ev[p], ctx->stream) == cudaSuccess) ctx->ev_recorded[p] = true;
 }
 
@@ -265,6 +265,8 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
     Lists lists;
     RowBounds bounds;
     const uint32_t* perm = nullptr;  // rows of the lists -> input rows (tensor form with ordering)
+    const float* rerank_xs = nullptr;
+    const float* rerank_theta = nullptr;
     if (tensor) {
         const bool bf16 = o.precision == SCRUST_PRECISION_BF16;
         void* A16 = ws_get(ctx, SLOT_A16, (size_t)n_pad * 64 * 2, &e);
@@ -320,8 +322,10 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
             if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
                                               &first, false, order.theta, nullptr, ctx->d_stats)) != cudaSuccess)
                 return cuda_fail(st, e, "knn_candidates_tc");
+            mark(ctx, PH_PASS1);
             TileLists second;
             if ((rc = build_second_pass(ctx, A16, bf16, n, d, order, bA, bdelta, &second, st))) return rc;
+            mark(ctx, PH_LISTS);
             if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
                                               &second, true, order.theta, nullptr, ctx->d_stats)) != cudaSuccess)
                 return cuda_fail(st, e, "knn_candidates_tc");
@@ -334,6 +338,15 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
         }
         mark(ctx, PH_CAND);
         perm = order.perm;
+        if (order_rows) {
+            float* xs = (float*)ws_get(ctx, SLOT_XSORTED, sizeof(float) * (size_t)n * d, &e);
+            if (!xs) return cuda_fail(st, e, "workspace");
+            if ((e = launch_gather_rows(xwork, order.perm, n, d, xs, s)) != cudaSuccess)
+                return cuda_fail(st, e, "gather rows");
+            ctx->launches += 1;
+            rerank_xs = xs;
+            rerank_theta = order.theta;
+        }
         bounds.A = bA;
         bounds.delta = bdelta;
         bounds.eps2 = beps2;
@@ -364,8 +377,8 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
     }
 
     const float* xr = ref ? xcentred : xwork;
-    if ((e = launch_rerank(ctx, plan, xr, xr, norm2, norm2, norm64, norm64, x, x, bounds, lists, perm, out_idx,
-                           out_dist)) != cudaSuccess)
+    if ((e = launch_rerank(ctx, plan, xr, xr, norm2, norm2, norm64, norm64, x, x, bounds, lists, perm, rerank_xs,
+                           rerank_theta, out_idx, out_dist)) != cudaSuccess)
         return cuda_fail(st, e, "knn_rerank");
     ctx->launches += 2;
     mark(ctx, PH_RERANK);
@@ -801,6 +814,18 @@ int32_t scrust_cuda_phase_times(scrust_context* ctx, float* ms, int32_t max_phas
         if (ctx->ev_recorded[p] && cudaEventElapsedTime(&t, ctx->ev[prev], ctx->ev[p]) == cudaSuccess) {
             prev = p;
         } else {
+            cudaGetLastError();
+            t = 0.f;
+        }
+        ms[written++] = t;
+    }
+    // Inside the candidates phase of an ordered solve: the first sweep pass
+    // and the building of the second pass's tile lists.
+    const int sub[2][2] = {{PH_PREP, PH_PASS1}, {PH_PASS1, PH_LISTS}};
+    for (int i = 0; i < 2 && written < max_phases; ++i) {
+        float t = 0.f;
+        if (!(ctx->ev_recorded[sub[i][0]] && ctx->ev_recorded[sub[i][1]] &&
+              cudaEventElapsedTime(&t, ctx->ev[sub[i][0]], ctx->ev[sub[i][1]]) == cudaSuccess)) {
             cudaGetLastError();
             t = 0.f;
         }

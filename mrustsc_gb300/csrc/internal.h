@@ -50,6 +50,7 @@ enum Slot : int {
     SLOT_WORKQ,
     SLOT_ORDER,         // row ordering: anchors, permutation, priority tiles
     SLOT_PRUNE,         // tile balls and the tile lists of the second sweep pass
+    SLOT_XSORTED,       // working rows in list order (ordered solves)
     SLOT_COUNT
 };
 
@@ -82,8 +83,8 @@ struct scrust_context {
     uint64_t launches = 0;              // kernels enqueued so far
     unsigned long long* d_stats = nullptr;  // kernel counters when statistics are on (16 words)
     bool timing = false;
-    cudaEvent_t ev[5] = {};             // phase boundaries: prep | candidates | rerank | connectivities
-    bool ev_recorded[5] = {};
+    cudaEvent_t ev[7] = {};             // phase boundaries: prep | candidates | rerank | connectivities,
+    bool ev_recorded[7] = {};           // and inside candidates: first sweep pass | second-pass tile lists
 };
 
 struct scrust_csr {
@@ -100,7 +101,7 @@ struct scrust_csr {
 namespace scrust {
 
 // Phase boundary events (no-ops unless timing is enabled).
-enum Phase { PH_START = 0, PH_PREP = 1, PH_CAND = 2, PH_RERANK = 3, PH_CONN = 4 };
+enum Phase { PH_START = 0, PH_PREP = 1, PH_CAND = 2, PH_RERANK = 3, PH_CONN = 4, PH_PASS1 = 5, PH_LISTS = 6 };
 void mark(scrust_context* ctx, Phase p);
 
 // Status helpers.
@@ -225,12 +226,17 @@ struct RowBounds {
 };
 
 // rerank.cu.  With a permutation, list row s and list entry c stand for
-// input rows perm[s] and perm[c]; outputs are written in input order.
+// input rows perm[s] and perm[c]; outputs are written in input order.  With
+// xs (the working rows in list order) and theta (each list's threshold at
+// the end of the candidate pass) as well, no selection is needed.
 cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float* qx,
                           const float* rx, const float* qnorm2, const float* rnorm2,
                           const double* qn64, const double* rn64, const float* qraw,
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
-                          const uint32_t* perm, uint32_t* out_idx, float* out_dist);
+                          const uint32_t* perm, const float* xs, const float* theta, uint32_t* out_idx,
+                          float* out_dist);
+// order.cu: rows of x in list order, xs[s] = x[perm[s]].
+cudaError_t launch_gather_rows(const float* x, const uint32_t* perm, int64_t n, int d, float* xs, cudaStream_t s);
 
 // conn.cu
 cudaError_t launch_smooth_knn(scrust_context* ctx, const float* dist, int64_t n, int k,

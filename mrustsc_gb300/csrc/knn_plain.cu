@@ -55,7 +55,6 @@ __global__ void __launch_bounds__(THREADS, 2)
     __shared__ float thr_s[BM];
     __shared__ uint32_t cnt_s[BM];
     __shared__ float margin_s[BM];
-    __shared__ uint32_t hist_s[THREADS / 32][256];
 
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
@@ -189,7 +188,7 @@ __global__ void __launch_bounds__(THREADS, 2)
                     const int64_t lbase = (row * a.lists.segments + seg) * (int64_t)a.lists.ctot;
                     prune_list(a.lists.ids + lbase, a.lists.vals + lbase, min(c, (uint32_t)a.lists.ctot), a.k,
                                a.lists.cap, PlainBound{margin_s[lr]}, &thr_s[lr], &cnt_s[lr],
-                               a.lists.overflow + row, hist_s[warp]);
+                               a.lists.overflow + row);
                 }
             }
         }

@@ -300,7 +300,7 @@ __device__ __forceinline__ void take_prune(const PruneResult& r, const TensorArg
 // lane keeps its own threshold and count in registers.
 __device__ __forceinline__ void prune_lanes(uint32_t need, const TensorArgs& a, int seg, int64_t row,
                                             const TensorBound& bnd, float& th, uint32_t& cnt,
-                                            uint32_t& n_ovf, uint32_t* hist) {
+                                            uint32_t& n_ovf) {
     const int lane = threadIdx.x & 31;
     const int segs = a.lists.segments;
     while (need) {
@@ -313,7 +313,7 @@ __device__ __forceinline__ void prune_lanes(uint32_t need, const TensorArgs& a, 
         const int64_t lrow = __shfl_sync(0xffffffffu, row, l);
         const int64_t off = (lrow * segs + seg) * (int64_t)a.lists.ctot;  // seg: list slot within the row
         const PruneResult r =
-            prune_core(a.lists.ids + off, a.lists.vals + off, min(lc, (uint32_t)a.lists.ctot), a.k, lb, lth, hist);
+            prune_core(a.lists.ids + off, a.lists.vals + off, min(lc, (uint32_t)a.lists.ctot), a.k, lb, lth);
         if (lane == l) take_prune(r, a, row, th, cnt, n_ovf);
     }
 }
@@ -332,7 +332,6 @@ __global__ void __launch_bounds__(THREADS, 1)
     __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], afull[2], aempty[2], tfull[HALVES],
         tempty[HALVES];
     __shared__ uint32_t tmem_slot;
-    __shared__ uint32_t hist_s[EPI_WARPS][256];
     __shared__ unsigned long long theta_s[HALVES][PARTS][TBM];
 
     const int warp = threadIdx.x >> 5;
@@ -565,7 +564,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                        a, row, th, cnt, n_ovf);
                         __syncwarp();
                     } else {
-                        prune_lanes(need, a, seg * PARTS + part, row, bnd, th, cnt, n_ovf, hist_s[e]);
+                        prune_lanes(need, a, seg * PARTS + part, row, bnd, th, cnt, n_ovf);
                     }
                     if (a.stats) c_prune += clock64() - p0;
                 }
@@ -585,7 +584,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                        a, row, th, cnt, n_ovf);
                         __syncwarp();
                     } else {
-                        prune_lanes(need, a, seg * PARTS + part, row, bnd, th, cnt, n_ovf, hist_s[e]);
+                        prune_lanes(need, a, seg * PARTS + part, row, bnd, th, cnt, n_ovf);
                     }
                     if (a.stats) c_prune += clock64() - p0;
                 }

@@ -54,12 +54,10 @@ struct PruneResult {
 
 // Prunes one row's list with the whole warp: theta <- min(old, bound.theta(k-th
 // smallest value)), entries at or above theta dropped (compacted in place).
-// The k-th smallest comes from a four-pass 8-bit radix select over a
-// 256-bin histogram `hist` in shared memory owned by this warp.  Every lane
-// returns the same result.
+// Every lane returns the same result.
 template <class Bound>
 __device__ PruneResult prune_core(uint32_t* ids, float* vals, uint32_t cnt, int k, const Bound& bound,
-                                  float theta_old, uint32_t* hist) {
+                                  float theta_old) {
     // Fewer than k entries: there is no k-th smallest to bound the row by.
     if ((int)cnt < k) return PruneResult{theta_old, cnt};
     const int lane = threadIdx.x & 31;
@@ -76,54 +74,39 @@ __device__ PruneResult prune_core(uint32_t* ids, float* vals, uint32_t cnt, int 
             id[e] = 0xffffffffu;
         }
     }
-    const int live = ((int)cnt + 31) / 32;  // entry slots that can hold data
-    uint32_t prefix = 0, decided = 0;
+    // k-th smallest key by binary radix selection over the bits below the
+    // keys' common prefix; each step is one warp-wide count.
+    uint32_t kmin = 0xffffffffu, kmax = 0u;
+#pragma unroll
+    for (int e = 0; e < kListMaxEntriesPerLane; e++) {
+        if (e * 32 + lane < (int)cnt) {
+            const uint32_t key = float_key(v[e]);
+            kmin = min(kmin, key);
+            kmax = max(kmax, key);
+        }
+    }
+    kmin = __reduce_min_sync(0xffffffffu, kmin);
+    kmax = __reduce_max_sync(0xffffffffu, kmax);
+    const uint32_t diff = kmin ^ kmax;
+    const int top = diff ? 31 - __clz(diff) : -1;
+    const uint32_t low = top >= 0 ? (uint32_t)((2ull << top) - 1ull) : 0u;
+    uint32_t prefix = kmin & ~low, decided = ~low;
     int rank = k;
 #pragma unroll 1
-    for (int pass = 0; pass < 4; ++pass) {
-        const int shift = 24 - 8 * pass;
-#pragma unroll
-        for (int b = 0; b < 8; b++) hist[lane * 8 + b] = 0;
-        __syncwarp();
+    for (int bit = top; bit >= 0; --bit) {
+        const uint32_t b = 1u << bit;
+        int c0 = 0;
 #pragma unroll
         for (int e = 0; e < kListMaxEntriesPerLane; e++) {
-            if (e < live && e * 32 + lane < (int)cnt) {
-                const uint32_t key = float_key(v[e]);
-                if ((key & decided) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
-            }
+            const uint32_t key = float_key(v[e]);
+            c0 += (e * 32 + lane < (int)cnt) && ((key & decided) == prefix) && !(key & b);
         }
-        __syncwarp();
-        uint32_t c[8];
-        uint32_t own = 0;
-#pragma unroll
-        for (int b = 0; b < 8; b++) {
-            c[b] = hist[lane * 8 + b];
-            own += c[b];
+        const int total = __reduce_add_sync(0xffffffffu, c0);
+        if (rank > total) {
+            rank -= total;
+            prefix |= b;
         }
-        uint32_t incl = own;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        const int L = __ffs(__ballot_sync(0xffffffffu, (int)incl >= rank)) - 1;
-        uint32_t digit = 0;
-        int new_rank = 0;
-        if (lane == L) {
-            int r = rank - (int)(incl - own);
-            int b = 0;
-            for (; b < 7; b++) {
-                if ((int)c[b] >= r) break;
-                r -= (int)c[b];
-            }
-            digit = (uint32_t)(lane * 8 + b);
-            new_rank = r;
-        }
-        digit = __shfl_sync(0xffffffffu, digit, L);
-        rank = __shfl_sync(0xffffffffu, new_rank, L);
-        prefix |= digit << shift;
-        decided |= 255u << shift;
-        __syncwarp();
+        decided |= b;
     }
     const float theta = fminf(theta_old, bound.theta(key_float(prefix)));
     uint32_t out = 0;
@@ -148,8 +131,8 @@ __device__ PruneResult prune_core(uint32_t* ids, float* vals, uint32_t cnt, int 
 // *overflow_flag raised, so the exact fallback finishes it.
 template <class Bound>
 __device__ void prune_list(uint32_t* ids, float* vals, uint32_t cnt, int k, int cap, const Bound& bound,
-                           float* thr, uint32_t* cnt_out, uint32_t* overflow_flag, uint32_t* hist) {
-    const PruneResult r = prune_core(ids, vals, cnt, k, bound, *thr, hist);
+                           float* thr, uint32_t* cnt_out, uint32_t* overflow_flag) {
+    const PruneResult r = prune_core(ids, vals, cnt, k, bound, *thr);
     if ((threadIdx.x & 31) == 0) {
         if ((int)r.cnt >= cap) {
             *overflow_flag = 1u;

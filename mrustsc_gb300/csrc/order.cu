@@ -527,7 +527,20 @@ __global__ void __launch_bounds__(256) tile_lists_kernel(const uint32_t* __restr
     if (threadIdx.x == 0) counts[I] = (uint32_t)base;
 }
 
+__global__ void gather_rows_kernel(const float* __restrict__ x, const uint32_t* __restrict__ perm, int64_t n, int d,
+                                   float* __restrict__ xs) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * d) return;
+    const int64_t s = i / d, t = i % d;
+    xs[i] = x[(int64_t)perm[s] * d + t];
+}
+
 }  // namespace
+
+cudaError_t launch_gather_rows(const float* x, const uint32_t* perm, int64_t n, int d, float* xs, cudaStream_t s) {
+    gather_rows_kernel<<<(unsigned)((n * d + 255) / 256), 256, 0, s>>>(x, perm, n, d, xs);
+    return cudaGetLastError();
+}
 
 namespace {
 

@@ -39,6 +39,8 @@ struct RerankArgs {
     RowBounds bounds;
     Lists lists;
     const uint32_t* perm;  // list row / list entry -> input row, or null
+    const float* xs;       // working rows in list order (ordered solves), or null
+    const float* theta;    // per list: its threshold when the candidate pass ended, or null
     int64_t nq, nr;
     int d, k, mode, metric, self;
     float gamma;
@@ -198,6 +200,70 @@ __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a
     finalize_row(team, a, q, B, m, reinterpret_cast<double*>(A));
 }
 
+// Ordered solves: the candidate pass left every list with a threshold no
+// smaller than the final one, so the rerank needs no selection.  A warp per
+// list row keeps the entries below the smaller of its lists' thresholds,
+// measures them on the working rows laid out in list order (neighbouring
+// rows share candidates, which stay in cache), and finishes as above with
+// input ids.  More than RS_KEYS survivors go to the fallback.
+constexpr int RS_WARPS = 8;
+constexpr int RS_KEYS = 256;
+__global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs a) {
+    extern __shared__ unsigned long long rs_smem[];
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    unsigned long long* keys = rs_smem + (size_t)warp * 2 * RS_KEYS;
+    double* dbl = reinterpret_cast<double*>(keys + RS_KEYS);
+    const int64_t slot = (int64_t)blockIdx.x * RS_WARPS + warp;
+    if (slot >= a.nq) return;
+    WarpTeam team;
+    if (a.lists.overflow[slot]) {
+        if (lane == 0) push_fallback(a, slot);
+        return;
+    }
+    const int segs = a.lists.segments;
+    float theta = __int_as_float(0x7f800000);
+    for (int l = 0; l < segs; ++l) theta = fminf(theta, a.theta[slot * segs + l]);
+    const float* xq = a.xs + slot * a.d;
+    int m = 0;
+    for (int l = 0; l < segs; ++l) {
+        const int c = (int)min(a.lists.cnt[slot * segs + l], (uint32_t)a.lists.ctot);
+        const int64_t base = (slot * segs + l) * (int64_t)a.lists.ctot;
+        for (int b0 = 0; b0 < c; b0 += 32) {
+            const int p = b0 + lane;
+            bool keep = false;
+            uint32_t id = 0;
+            if (p < c) {
+                id = a.lists.ids[base + p];
+                if ((int64_t)id >= a.nr) {  // never written by a candidate kernel: refuse to read it
+                    atomicExch(a.err + DERR_CANDIDATES, 1);
+                } else {
+                    keep = a.lists.vals[base + p] < theta;
+                }
+            }
+            const uint32_t ballot = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                const int pos = m + __popc(ballot & lanemask_lt());
+                if (pos < RS_KEYS) {
+                    const float r = dist2_f32(xq, a.xs + (int64_t)id * a.d, a.d);
+                    keys[pos] = ((unsigned long long)float_key(r) << 32) | a.perm[id];
+                }
+            }
+            m += __popc(ballot);
+        }
+    }
+    if (m > RS_KEYS || m < a.k) {
+        if (lane == 0) push_fallback(a, slot);
+        return;
+    }
+    __syncwarp();
+    const int P = next_pow2(m);
+    for (int p = m + lane; p < P; p += 32) keys[p] = ~0ull;
+    __syncwarp();
+    team_bitonic_sort(team, keys, P);
+    finalize_row(team, a, input_row(a, slot), keys, m, dbl);
+}
+
 // One block per row, over every reference row: used for rows whose
 // candidate lists overflowed (many cells within the margin, e.g. duplicates).
 __global__ void __launch_bounds__(FB_THREADS) rerank_fallback_kernel(RerankArgs a) {
@@ -307,7 +373,8 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
                           const float* rx, const float* qnorm2, const float* rnorm2,
                           const double* qn64, const double* rn64, const float* qraw,
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
-                          const uint32_t* perm, uint32_t* out_idx, float* out_dist) {
+                          const uint32_t* perm, const float* xs, const float* theta, uint32_t* out_idx,
+                          float* out_dist) {
     cudaError_t e;
     uint32_t* fb_rows = (uint32_t*)ws_get(ctx, SLOT_FALLBACK_ROWS, sizeof(uint32_t) * (size_t)plan.nq, &e);
     if (!fb_rows) return e;
@@ -326,6 +393,8 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.bounds = bounds;
     a.lists = lists;
     a.perm = perm;
+    a.xs = xs;
+    a.theta = theta;
     a.nq = plan.nq;
     a.nr = plan.nr;
     a.d = plan.d;
@@ -343,11 +412,17 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.err = ctx->d_err;
     e = cudaMemsetAsync(ctx->d_counter, 0, 2 * sizeof(uint32_t), ctx->stream);
     if (e != cudaSuccess) return e;
-    const size_t smem_w = (size_t)RR_WARPS * 2 * RC * sizeof(unsigned long long);
-    e = cudaFuncSetAttribute(rerank_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_w);
-    if (e != cudaSuccess) return e;
-    const unsigned blocks = (unsigned)((plan.nq + RR_WARPS - 1) / RR_WARPS);
-    rerank_warp_kernel<<<blocks, RR_WARPS * 32, smem_w, ctx->stream>>>(a);
+    if (xs && theta && perm) {
+        const size_t smem_s = (size_t)RS_WARPS * 2 * RS_KEYS * sizeof(unsigned long long);
+        const unsigned blocks = (unsigned)((plan.nq + RS_WARPS - 1) / RS_WARPS);
+        rerank_sorted_kernel<<<blocks, RS_WARPS * 32, smem_s, ctx->stream>>>(a);
+    } else {
+        const size_t smem_w = (size_t)RR_WARPS * 2 * RC * sizeof(unsigned long long);
+        e = cudaFuncSetAttribute(rerank_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_w);
+        if (e != cudaSuccess) return e;
+        const unsigned blocks = (unsigned)((plan.nq + RR_WARPS - 1) / RR_WARPS);
+        rerank_warp_kernel<<<blocks, RR_WARPS * 32, smem_w, ctx->stream>>>(a);
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const size_t smem_f = (size_t)FB_CAP * (sizeof(unsigned long long) + sizeof(double));
     e = cudaFuncSetAttribute(rerank_fallback_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
