@@ -319,6 +319,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
             first.tiles = order.prio;
             first.count = order.prio_cnt;
             first.stride = kPrioMax;
+            first.order = order.prio_order;
             if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
                                               &first, false, order.theta, nullptr, ctx->d_stats)) != cudaSuccess)
                 return cuda_fail(st, e, "knn_candidates_tc");

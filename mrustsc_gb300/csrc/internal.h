@@ -153,6 +153,7 @@ constexpr int kAnchorNeighbours = 16;  // neighbouring anchors per anchor
 constexpr int64_t kMaxAnchors = 8192;
 struct RowOrder {
     const uint32_t* perm = nullptr;      // sorted position -> original row
+    const uint32_t* prio_order = nullptr;  // row blocks by decreasing priority-tile count
     const uint32_t* prio = nullptr;      // [items][kPrioMax] distinct column tiles, nearest cells first
     const uint32_t* prio_cnt = nullptr;  // [items], at least 1
     float* theta = nullptr;              // [n_pad * 2] list thresholds between the sweep passes
@@ -206,15 +207,19 @@ struct TileLists {
     const uint32_t* offset = nullptr;  // per row block; null: block * stride
     const uint32_t* count = nullptr;   // per row block
     int stride = 0;
+    const uint32_t* order = nullptr;   // row blocks by decreasing count, or null
 };
 // One pass of the tensor sweep.  `tiles` null: every column tile, outward
 // from the diagonal.  `resume`: lists and thresholds continue from an earlier
 // pass (counts in lists.cnt, thresholds in theta_io); theta_io, when given,
-// receives each list's threshold as its row block ends.
+// receives each list's threshold as its row block ends.  `argmin_out` (k = 1
+// only): no lists; per (row, column part) the smallest value and its column,
+// packed as float_key << 32 | column.
 cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, const void* A16, int64_t nq_pad,
                                      const void* B16, int64_t nr_pad, const float* bA, const float* bdelta,
                                      const float* beps2, const Lists& lists, bool bf16, const TileLists* tiles,
-                                     bool resume, float* theta_io, int* grid_out, unsigned long long* stats);
+                                     bool resume, float* theta_io, int* grid_out, unsigned long long* stats,
+                                     unsigned long long* argmin_out = nullptr);
 
 // Per-row bound of the candidate lists, as the rerank re-applies it: the
 // plain form's additive margin, or the tensor form's (A, delta, eps2).

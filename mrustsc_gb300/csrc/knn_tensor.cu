@@ -79,6 +79,10 @@ struct TensorArgs {
     const uint32_t* tl_off;     // per-item offsets into tl, or null: item * tl_stride
     const uint32_t* tl_cnt;
     int tl_stride;
+    const uint32_t* item_order; // items by decreasing work, dealt out in a snake, or null: round robin
+    // k = 1 without lists: per (row, part) the smallest MMA value and its
+    // column, packed as float_key << 32 | column; null otherwise.
+    unsigned long long* argmin_out;
     int final_cap;              // lists longer than this are pruned once more when an item ends
     int resume;                 // lists and thresholds continue from an earlier pass
     float* theta_io;            // per list: the threshold when the item ends (read when resuming)
@@ -137,6 +141,18 @@ struct TileOrder {
         return list ? (int)list[it] : sweep_tile(it, home, ct0, ct1);
     }
 };
+
+// The j-th work item of this CTA, or -1.  Round robin over the items; with
+// an item order (items by decreasing work) a snake over it: the CTAs take
+// the heaviest items first, alternately in forward and reverse CTA order,
+// which balances the CTAs' totals.  Every role of the CTA derives the same
+// sequence.
+__device__ __forceinline__ int item_at(const TensorArgs& a, int j) {
+    const int G = gridDim.x, c = blockIdx.x;
+    const int64_t pos = (int64_t)j * G + (a.item_order && (j & 1) ? G - 1 - c : c);
+    if (pos >= a.items) return -1;
+    return a.item_order ? (int)a.item_order[pos] : (int)pos;
+}
 
 __device__ __forceinline__ float min32(const uint32_t (&v)[32]) {
     float m[11];
@@ -226,20 +242,44 @@ __device__ __forceinline__ float pick32(const uint32_t (&v)[32], int j) {
     return x;
 }
 
-// test_chunk with a register top-K: the chunk's columns below the K-th
-// smallest so far enter it, the threshold follows, then survivors append.
+// A chunk's columns below the lane's K-th smallest so far enter its top-K,
+// and the threshold follows the k-th smallest.  Returns the chunk minimum.
+// Appending is left to a second look at the tile, once the whole tile has
+// tightened the threshold.
 template <int K>
-__device__ __forceinline__ void test_chunk_topk(const uint32_t (&v)[32], int64_t colbase, float& th, int64_t row,
-                                                const TensorArgs& a, uint32_t* ids, float* vals, uint32_t& cnt,
-                                                TopK<K>& top, const TensorBound& bnd) {
+__device__ __forceinline__ float topk_chunk(const uint32_t (&v)[32], int64_t colbase, float& th, int64_t row,
+                                            const TensorArgs& a, TopK<K>& top, const TensorBound& bnd,
+                                            uint32_t& best) {
     const float m = min32(v);
-    const uint32_t valid = chunk_valid(colbase, a.nr, a.self != 0, row);
+    if constexpr (K == 1) {
+        // The chunk minimum is the only candidate; its column is kept too.
+        if (__any_sync(0xffffffffu, m < top.v[0])) {
+            const uint32_t valid = chunk_valid(colbase, a.nr, a.self != 0, row);
+            float mv = m;
+            if (valid != 0xffffffffu) {
+                mv = __int_as_float(0x7f800000);
+#pragma unroll
+                for (int j = 0; j < 32; j++)
+                    if ((valid >> j) & 1u) mv = fminf(mv, f_of(v[j]));
+            }
+            if (mv < top.v[0]) {
+                int jj = 0;
+#pragma unroll
+                for (int j = 31; j >= 0; j--)
+                    if (((valid >> j) & 1u) && f_of(v[j]) == mv) jj = j;
+                top.v[0] = mv;
+                best = (uint32_t)(colbase + jj);
+                th = fminf(th, bnd.theta_f32(mv));
+            }
+        }
+        return m;
+    }
     if (__any_sync(0xffffffffu, m < top.v[K - 1])) {
         const float lim = top.v[K - 1];
         uint32_t want = 0;
 #pragma unroll
         for (int j = 0; j < 32; j++) want |= (f_of(v[j]) < lim) ? (1u << j) : 0u;
-        want &= valid;
+        want &= chunk_valid(colbase, a.nr, a.self != 0, row);
         if (want) {
             const float old = top.kth(a.k);
             while (want) {
@@ -252,7 +292,7 @@ __device__ __forceinline__ void test_chunk_topk(const uint32_t (&v)[32], int64_t
             if (kth < old) th = fminf(th, bnd.theta_f32(kth));
         }
     }
-    if (__any_sync(0xffffffffu, m < th)) append_chunk(v, colbase, th, valid, ids, vals, cnt);
+    return m;
 }
 
 // Drops, in place, the entries of a lane's list at or above theta; eight
@@ -375,7 +415,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             uint32_t sc = 0, ac = 0;
             long long w_tma = 0;
             bool ok = true;
-            for (int w = blockIdx.x; w < a.items && ok; w += gridDim.x) {
+            for (int j = 0, w; ok && (w = item_at(a, j)) >= 0; ++j) {
                 const int qt = w / csegs, seg = w % csegs;
                 const int ct0 = seg * a.tiles_per_seg;
                 const int ct1 = min(a.col_tiles, ct0 + a.tiles_per_seg);
@@ -418,7 +458,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             uint32_t sc = 0, ac = 0, tc = 0;
             long long w_full = 0, w_empty = 0;
             bool ok = true;
-            for (int w = blockIdx.x; w < a.items && ok; w += gridDim.x) {
+            for (int j = 0, w; ok && (w = item_at(a, j)) >= 0; ++j) {
                 const int qt = w / csegs, seg = w % csegs;
                 const int ct0 = seg * a.tiles_per_seg;
                 const int ct1 = min(a.col_tiles, ct0 + a.tiles_per_seg);
@@ -488,7 +528,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         uint32_t n_app = 0, n_prune = 0, n_ovf = 0;
         long long c_prune = 0, c_wait = 0;
         bool ok = true;
-        for (int w = blockIdx.x; w < a.items && ok; w += gridDim.x) {
+        for (int j = 0, w; ok && (w = item_at(a, j)) >= 0; ++j) {
             const int qt = w / col_segs, seg = w % col_segs;
             const int ct0 = seg * a.tiles_per_seg;
             const int ct1 = min(a.col_tiles, ct0 + a.tiles_per_seg);
@@ -511,6 +551,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             *my_th = tag | __float_as_uint(th);
             TopK<(TOPK > 0 ? TOPK : 1)> top;
             if constexpr (TOPK > 0) top.reset();
+            uint32_t best = 0xffffffffu;
             for (int it = 0; it < order.count; ++it) {
                 const int ct = order.next(it);
                 const long long w0 = a.stats ? clock64() : 0;
@@ -527,26 +568,51 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(h * TBN + part * kPartCols);
                 const uint32_t before = cnt;
                 const float th_before = th;
-                {
+                if constexpr (TOPK > 0) {
+                    // First look: the tile's columns update the top-K and the
+                    // threshold.  Second look: chunks holding columns below
+                    // the tightened threshold are read again and appended.
+                    uint32_t va[32], vb[32];
+                    float cm[4];
+                    tmem_ld32(tbase, va);
+                    tmem_ld_wait(va);
+                    tmem_ld32(tbase + 32, vb);
+                    cm[0] = topk_chunk(va, col0, th, row, a, top, bnd, best);
+                    tmem_ld_wait(vb);
+                    tmem_ld32(tbase + 64, va);
+                    cm[1] = topk_chunk(vb, col0 + 32, th, row, a, top, bnd, best);
+                    tmem_ld_wait(va);
+                    tmem_ld32(tbase + 96, vb);
+                    cm[2] = topk_chunk(va, col0 + 64, th, row, a, top, bnd, best);
+                    tmem_ld_wait(vb);
+                    cm[3] = topk_chunk(vb, col0 + 96, th, row, a, top, bnd, best);
+                    const unsigned long long o2 = *other_th;
+                    if ((o2 & 0xffffffff00000000ull) == tag) th = fminf(th, __uint_as_float((uint32_t)o2));
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        if (!a.argmin_out && __any_sync(0xffffffffu, cm[c] < th)) {
+                            tmem_ld32(tbase + 32 * c, va);
+                            tmem_ld_wait(va);
+                            append_chunk(va, col0 + 32 * c, th,
+                                         chunk_valid(col0 + 32 * c, a.nr, a.self != 0, row), ids, vals, cnt);
+                        }
+                    }
+                } else {
                     // Four 32-column chunks; each TMEM load overlaps the
                     // previous chunk's threshold test.
                     uint32_t va[32], vb[32];
                     tmem_ld32(tbase, va);
                     tmem_ld_wait(va);
                     tmem_ld32(tbase + 32, vb);
-                    if constexpr (TOPK > 0) test_chunk_topk(va, col0, th, row, a, ids, vals, cnt, top, bnd);
-                    else test_chunk(va, col0, th, row, a, ids, vals, cnt);
+                    test_chunk(va, col0, th, row, a, ids, vals, cnt);
                     tmem_ld_wait(vb);
                     tmem_ld32(tbase + 64, va);
-                    if constexpr (TOPK > 0) test_chunk_topk(vb, col0 + 32, th, row, a, ids, vals, cnt, top, bnd);
-                    else test_chunk(vb, col0 + 32, th, row, a, ids, vals, cnt);
+                    test_chunk(vb, col0 + 32, th, row, a, ids, vals, cnt);
                     tmem_ld_wait(va);
                     tmem_ld32(tbase + 96, vb);
-                    if constexpr (TOPK > 0) test_chunk_topk(va, col0 + 64, th, row, a, ids, vals, cnt, top, bnd);
-                    else test_chunk(va, col0 + 64, th, row, a, ids, vals, cnt);
+                    test_chunk(va, col0 + 64, th, row, a, ids, vals, cnt);
                     tmem_ld_wait(vb);
-                    if constexpr (TOPK > 0) test_chunk_topk(vb, col0 + 96, th, row, a, ids, vals, cnt, top, bnd);
-                    else test_chunk(vb, col0 + 96, th, row, a, ids, vals, cnt);
+                    test_chunk(vb, col0 + 96, th, row, a, ids, vals, cnt);
                 }
                 // Release the accumulator before any prune, so the tensor
                 // core refills it while this warp prunes.
@@ -588,6 +654,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                     }
                     if (a.stats) c_prune += clock64() - p0;
                 }
+            }
+            if (a.argmin_out) {
+                if (valid && ok)
+                    a.argmin_out[row * PARTS + part] =
+                        ((unsigned long long)float_key(top.v[0]) << 32) | (unsigned long long)best;
+                continue;
             }
             if (valid && ok) {
                 a.lists.cnt[lslot] = min(cnt, (uint32_t)a.lists.ctot);
@@ -759,7 +831,8 @@ cudaError_t launch_tensor_bounds(int64_t n, const float* bA, const float* eps, c
 cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, const void* A16, int64_t nq_pad,
                                      const void* B16, int64_t nr_pad, const float* bA, const float* bdelta,
                                      const float* beps2, const Lists& lists, bool bf16, const TileLists* tiles,
-                                     bool resume, float* theta_io, int* grid_out, unsigned long long* stats) {
+                                     bool resume, float* theta_io, int* grid_out, unsigned long long* stats,
+                                     unsigned long long* argmin_out) {
     if (nq_pad % ROWS || nr_pad % TBN) return cudaErrorInvalidValue;
     CUtensorMap ta, tb;
     const CUtensorMapDataType dt = bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
@@ -792,6 +865,7 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.tl_off = nullptr;
     a.tl_cnt = nullptr;
     a.tl_stride = 0;
+    a.item_order = nullptr;
     if (tiles && tiles->tiles) {
         // Explicit tile lists are per row block: one column segment only.
         if (col_segs != 1 || !tiles->count) return cudaErrorInvalidValue;
@@ -799,9 +873,12 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
         a.tl_off = tiles->offset;
         a.tl_cnt = tiles->count;
         a.tl_stride = tiles->stride;
+        a.item_order = tiles->order;
     }
     a.resume = resume ? 1 : 0;
     a.theta_io = theta_io;
+    a.argmin_out = argmin_out;
+    if (argmin_out && (plan.k != 1 || resume)) return cudaErrorInvalidValue;
     if (resume && !theta_io) return cudaErrorInvalidValue;
     auto kern = a.k == 1 ? tensor_candidates_kernel<1> : a.k <= 16 ? tensor_candidates_kernel<16>
                                                                    : tensor_candidates_kernel<0>;

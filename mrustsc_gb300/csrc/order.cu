@@ -31,6 +31,8 @@ namespace scrust {
 
 namespace {
 
+size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
+
 // Anchor c is input row floor(c * n / m); its coordinates are copied out
 // for the anchor neighbourhoods.
 __global__ void anchors_kernel(const float* __restrict__ x, int d, int64_t n, int64_t m, uint32_t* __restrict__ src,
@@ -185,27 +187,16 @@ __global__ void relabel_neighbours_kernel(const uint32_t* __restrict__ nb, const
     out[(int64_t)rank[a] * kAnchorNeighbours + j] = c < (uint32_t)m ? rank[c] : 0xffffffffu;
 }
 
-// Per row, the column of the smallest candidate value over its lists: an
-// approximately nearest anchor, which is all an ordering needs.
-__global__ void argmin_lists_kernel(Lists lists, int64_t n, int64_t m, const uint32_t* __restrict__ rank,
-                                    uint32_t* __restrict__ keys, unsigned long long* __restrict__ vals) {
+// Per row, the nearer of its two column parts' nearest anchors (an
+// approximately nearest anchor, which is all an ordering needs), as the
+// anchor's walk rank, with the row as payload.
+__global__ void nearest_anchor_kernel(const unsigned long long* __restrict__ best, int64_t n, int64_t m,
+                                      const uint32_t* __restrict__ rank, uint32_t* __restrict__ keys,
+                                      unsigned long long* __restrict__ vals) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float best = __int_as_float(0x7f800000);
-    uint32_t arg = 0;
-    for (int l = 0; l < lists.segments; ++l) {
-        const int64_t slot = i * lists.segments + l;
-        const uint32_t c = min(lists.cnt[slot], (uint32_t)lists.ctot);
-        const uint32_t* ids = lists.ids + slot * (int64_t)lists.ctot;
-        const float* vs = lists.vals + slot * (int64_t)lists.ctot;
-        for (uint32_t t = 0; t < c; ++t) {
-            const float v = vs[t];
-            if (v < best) {
-                best = v;
-                arg = ids[t];
-            }
-        }
-    }
+    const unsigned long long b = min(best[2 * i], best[2 * i + 1]);
+    const uint32_t arg = (uint32_t)b;
     keys[i] = rank[arg < (uint32_t)m ? arg : (uint32_t)(m - 1)];
     vals[i] = (unsigned long long)i;
 }
@@ -527,6 +518,21 @@ __global__ void __launch_bounds__(256) tile_lists_kernel(const uint32_t* __restr
     if (threadIdx.x == 0) counts[I] = (uint32_t)base;
 }
 
+// Keys that sort row blocks by decreasing count (stable, so ties keep
+// block order).
+__global__ void work_keys_kernel(const uint32_t* __restrict__ counts, int items, uint32_t* __restrict__ keys,
+                                 unsigned long long* __restrict__ vals) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= items) return;
+    keys[i] = 0xffffu - min(counts[i], 0xffffu);
+    vals[i] = (unsigned long long)i;
+}
+
+__global__ void narrow_kernel(const unsigned long long* __restrict__ vals, int items, uint32_t* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < items) out[i] = (uint32_t)vals[i];
+}
+
 __global__ void gather_rows_kernel(const float* __restrict__ x, const uint32_t* __restrict__ perm, int64_t n, int d,
                                    float* __restrict__ xs) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -537,16 +543,46 @@ __global__ void gather_rows_kernel(const float* __restrict__ x, const uint32_t* 
 
 }  // namespace
 
+// Row blocks sorted by decreasing count into `order`; scratch holds
+// work_order_scratch(items) bytes.
+size_t work_order_scratch(int items) {
+    const int nb = radix_blocks(items);
+    return align_up(4 * (size_t)items) * 2 + align_up(8 * (size_t)items) * 2 + align_up(4 * ((size_t)256 * nb + 16)) +
+           align_up(4 * scan_scratch_elems((int64_t)256 * nb));
+}
+
+cudaError_t sort_by_work(scrust_context* ctx, const uint32_t* counts, int items, char* scratch, uint32_t* order) {
+    const int nb = radix_blocks(items);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char* p = scratch + off;
+        off += align_up(bytes);
+        return p;
+    };
+    uint32_t* kA = (uint32_t*)take(4 * (size_t)items);
+    uint32_t* kB = (uint32_t*)take(4 * (size_t)items);
+    unsigned long long* vA = (unsigned long long*)take(8 * (size_t)items);
+    unsigned long long* vB = (unsigned long long*)take(8 * (size_t)items);
+    uint32_t* hist = (uint32_t*)take(4 * ((size_t)256 * nb + 16));
+    const size_t scan_elems = scan_scratch_elems((int64_t)256 * nb);
+    uint32_t* scan = (uint32_t*)take(4 * scan_elems);
+    work_keys_kernel<<<(items + 255) / 256, 256, 0, ctx->stream>>>(counts, items, kA, vA);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    uint32_t* ks = nullptr;
+    unsigned long long* vs = nullptr;
+    if ((e = radix_sort_pairs(ctx, kA, vA, kB, vB, items, 16, hist, scan, scan_elems, &ks, &vs)) != cudaSuccess)
+        return e;
+    narrow_kernel<<<(items + 255) / 256, 256, 0, ctx->stream>>>(vs, items, order);
+    ctx->launches += 2;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_gather_rows(const float* x, const uint32_t* perm, int64_t n, int d, float* xs, cudaStream_t s) {
     gather_rows_kernel<<<(unsigned)((n * d + 255) / 256), 256, 0, s>>>(x, perm, n, d, xs);
     return cudaGetLastError();
 }
 
-namespace {
-
-size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
-
-}  // namespace
 
 int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, const double* means,
                         uint32_t* max_bits, bool cosine, bool bf16, void* A16, void* B16, float* bA, float* beps,
@@ -574,7 +610,9 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
                  o_cst = take(4 * (size_t)(m + 1)), o_nb = take(4 * (size_t)m * kAnchorNeighbours),
                  o_nb2 = take(4 * (size_t)m * kAnchorNeighbours), o_rank = take(4 * (size_t)m),
                  o_prio = take(4 * (size_t)items * kPrioMax), o_pc = take(4 * (size_t)items),
-                 o_theta = take(8 * (size_t)n_pad),
+                 o_theta = take(8 * (size_t)n_pad), o_po = take(4 * (size_t)items),
+                 o_best = take(16 * (size_t)n_pad),
+                 o_ws = take(work_order_scratch(items)),
                  o_hist = take(4 * ((size_t)256 * nblocks + 16)), o_scan = take(4 * scan_elems);
     char* base = (char*)ws_get(ctx, SLOT_ORDER, off, &e);
     if (!base) return cuda_fail(st, e, "ordering: workspace");
@@ -618,7 +656,8 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor walk");
     ctx->launches += 3;
 
-    // Rows x anchors with k = 1 on the tensor cores.
+    // Rows x anchors with k = 1 on the tensor cores, keeping only each row's
+    // nearest anchor.
     KnnPlan px;
     px.nq = n;
     px.nr = m;
@@ -626,19 +665,18 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     px.k = 1;
     px.self = false;
     px.form = SCRUST_FORM_TENSOR;
-    Lists lx;
-    lx.cap = 256;
-    lx.ctot = 256 + 128;
+    Lists lx;  // no storage: the pass keeps no lists
+    lx.cap = 64;
+    lx.ctot = 64 + 128;
     lx.segments = 2;
-    int32_t rc = alloc_lists(ctx, n_pad, &lx, st);
-    if (rc) return rc;
     px.cap = lx.cap;
     px.ctot = lx.ctot;
     px.segments = lx.segments;
+    unsigned long long* best = (unsigned long long*)(base + o_best);
     if ((e = launch_tensor_candidates(ctx, px, A16, n_pad, base + o_aB, m_pad, bA, bdelta, beps2, lx, bf16, nullptr,
-                                      false, nullptr, nullptr, nullptr)) != cudaSuccess)
+                                      false, nullptr, nullptr, nullptr, best)) != cudaSuccess)
         return cuda_fail(st, e, "ordering: anchor candidates");
-    argmin_lists_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(lx, n, m, rank, keysA, valsA);
+    nearest_anchor_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(best, n, m, rank, keysA, valsA);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: nearest anchor");
     ctx->launches += 2;
 
@@ -663,9 +701,12 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
                                                                   kAnchorNeighbours, items, items, prio, prio_cnt);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: priority tiles");
     ctx->launches += 2;
+    if ((e = sort_by_work(ctx, prio_cnt, items, base + o_ws, (uint32_t*)(base + o_po))) != cudaSuccess)
+        return cuda_fail(st, e, "ordering: work order");
     out->perm = perm;
     out->prio = prio;
     out->prio_cnt = prio_cnt;
+    out->prio_order = (const uint32_t*)(base + o_po);
     out->theta = (float*)(base + o_theta);
     out->cell_of_pos = cell_of_pos;
     return SCRUST_OK;
@@ -691,6 +732,7 @@ int32_t build_second_pass(scrust_context* ctx, const void* A16, bool bf16, int64
                  o_so = take(4 * ((size_t)tiles + 1)), o_fc = take(4 * 64 * (size_t)smax), o_fr = take(4 * (size_t)smax),
                  o_fu = take(4 * (size_t)smax), o_fo = take(4 * (size_t)smax), o_scan = take(4 * scan_elems),
                  o_bm = take(4 * (size_t)tiles * words), o_cnt = take(4 * ((size_t)tiles + 1)),
+                 o_wo = take(4 * (size_t)tiles), o_ws = take(work_order_scratch(tiles)),
                  o_ent = take(4 * (size_t)tiles * (size_t)tiles);
     char* base = (char*)ws_get(ctx, SLOT_PRUNE, off, &e);
     if (!base) return cuda_fail(st, e, "pruning: workspace");
@@ -734,10 +776,13 @@ int32_t build_second_pass(scrust_context* ctx, const void* A16, bool bf16, int64
     tile_lists_kernel<<<tiles, 256, lists_smem, s>>>(bitmap, words, tiles, order.prio, order.prio_cnt, counts, entries);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "pruning: tile lists");
     ctx->launches += 3;
+    if ((e = sort_by_work(ctx, counts, tiles, base + o_ws, (uint32_t*)(base + o_wo))) != cudaSuccess)
+        return cuda_fail(st, e, "pruning: work order");
     out->tiles = entries;
     out->offset = nullptr;
     out->count = counts;
     out->stride = tiles;
+    out->order = (const uint32_t*)(base + o_wo);
     return SCRUST_OK;
 }
 
