@@ -293,11 +293,16 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
                                          beps2, &order, st);
             if (rc) return rc;
         }
-        if ((e = launch_tensor_operands(xwork, n, n_pad, d, means, max_bits, cosine, bf16, order.perm, A16, B16, bA,
-                                        beps, max_bits + 1, max_bits + 2, s)) != cudaSuccess ||
-            (e = launch_tensor_bounds(n, bA, beps, max_bits + 1, max_bits + 2, bdelta, beps2, s)) != cudaSuccess)
-            return cuda_fail(st, e, "tensor operands");
-        ctx->launches += 2;
+        // An ordered solve has its operands in list order already.
+        if (!order_rows) {
+            if ((e = launch_tensor_operands(xwork, n, n_pad, d, means, max_bits, cosine, bf16, nullptr, A16, B16, bA,
+                                            beps, max_bits + 1, max_bits + 2, s)) != cudaSuccess)
+                return cuda_fail(st, e, "tensor operands");
+            ctx->launches += 1;
+        }
+        if ((e = launch_tensor_bounds(n, bA, beps, max_bits + 1, max_bits + 2, bdelta, beps2, s)) != cudaSuccess)
+            return cuda_fail(st, e, "tensor bounds");
+        ctx->launches += 1;
         // Headroom of 128: a tensor-form list is checked once per tile, after
         // its warp has appended up to 128 columns.
         // Ordered solves keep long lists (256): a row block's first tiles

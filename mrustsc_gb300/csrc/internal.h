@@ -159,8 +159,9 @@ struct RowOrder {
     float* theta = nullptr;              // [n_pad * 2] list thresholds between the sweep passes
     const uint32_t* cell_of_pos = nullptr;  // [n] cell of each sorted position
 };
-// Builds the ordering.  A16/B16 and the four bound arrays (n_pad rows each)
-// are used as scratch for operands in the original row order.
+// Builds the ordering and leaves the tensor operands A16/B16 and their row
+// terms bA/beps (n_pad rows each) in list order; bdelta/beps2 serve as
+// scratch (the caller computes the list-order bounds afterwards).
 int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, const double* means,
                         uint32_t* max_bits, bool cosine, bool bf16, void* A16, void* B16, float* bA, float* beps,
                         float* bdelta, float* beps2, RowOrder* out, scrust_status* st);

@@ -518,6 +518,36 @@ __global__ void __launch_bounds__(256) tile_lists_kernel(const uint32_t* __restr
     if (threadIdx.x == 0) counts[I] = (uint32_t)base;
 }
 
+// Operand rows (128 bytes each) and their per-row terms moved into list
+// order; padding rows are zero like the operand kernel writes them.
+__global__ void gather_operands_kernel(const uint4* __restrict__ A0, const uint4* __restrict__ B0,
+                                       const float* __restrict__ bA0, const float* __restrict__ eps0,
+                                       const uint32_t* __restrict__ perm, int64_t n, int64_t n_pad,
+                                       uint4* __restrict__ A16, uint4* __restrict__ B16, float* __restrict__ bA,
+                                       float* __restrict__ eps) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_pad) return;
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    if (s < n) {
+        const int64_t r = perm[s];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            A16[s * 8 + q] = A0[r * 8 + q];
+            B16[s * 8 + q] = B0[r * 8 + q];
+        }
+        bA[s] = bA0[r];
+        eps[s] = eps0[r];
+    } else {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            A16[s * 8 + q] = z;
+            B16[s * 8 + q] = z;
+        }
+        bA[s] = 0.f;
+        eps[s] = 0.f;
+    }
+}
+
 // Keys that sort row blocks by decreasing count (stable, so ties keep
 // block order).
 __global__ void work_keys_kernel(const uint32_t* __restrict__ counts, int items, uint32_t* __restrict__ keys,
@@ -611,7 +641,8 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
                  o_nb2 = take(4 * (size_t)m * kAnchorNeighbours), o_rank = take(4 * (size_t)m),
                  o_prio = take(4 * (size_t)items * kPrioMax), o_pc = take(4 * (size_t)items),
                  o_theta = take(8 * (size_t)n_pad), o_po = take(4 * (size_t)items),
-                 o_best = take(16 * (size_t)n_pad),
+                 o_best = take(16 * (size_t)n_pad), o_A0 = take(128 * (size_t)n_pad),
+                 o_B0 = take(128 * (size_t)n_pad), o_bA0 = take(4 * (size_t)n_pad), o_eps0 = take(4 * (size_t)n_pad),
                  o_ws = take(work_order_scratch(items)),
                  o_hist = take(4 * ((size_t)256 * nblocks + 16)), o_scan = take(4 * scan_elems);
     char* base = (char*)ws_get(ctx, SLOT_ORDER, off, &e);
@@ -634,9 +665,13 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     // Anchors, and both operand sets in the input order.
     anchors_kernel<<<(unsigned)m, 64, 0, s>>>(x, d, n, m, src, anc);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchors");
-    if ((e = launch_tensor_operands(x, n, n_pad, d, means, max_bits, cosine, bf16, nullptr, A16, B16, bA, beps,
+    void* A0 = base + o_A0;
+    void* B0 = base + o_B0;
+    float* bA0 = (float*)(base + o_bA0);
+    float* eps0 = (float*)(base + o_eps0);
+    if ((e = launch_tensor_operands(x, n, n_pad, d, means, max_bits, cosine, bf16, nullptr, A0, B0, bA0, eps0,
                                     max_bits + 1, max_bits + 2, s)) != cudaSuccess ||
-        (e = launch_tensor_bounds(n, bA, beps, max_bits + 1, max_bits + 2, bdelta, beps2, s)) != cudaSuccess ||
+        (e = launch_tensor_bounds(n, bA0, eps0, max_bits + 1, max_bits + 2, bdelta, beps2, s)) != cudaSuccess ||
         (e = launch_tensor_operands(x, m, m_pad, d, means, max_bits, cosine, bf16, src, base + o_aA, base + o_aB, arb,
                                     arb + m_pad, max_bits + 1, max_bits + 2, s)) != cudaSuccess)
         return cuda_fail(st, e, "ordering: operands");
@@ -673,7 +708,7 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     px.ctot = lx.ctot;
     px.segments = lx.segments;
     unsigned long long* best = (unsigned long long*)(base + o_best);
-    if ((e = launch_tensor_candidates(ctx, px, A16, n_pad, base + o_aB, m_pad, bA, bdelta, beps2, lx, bf16, nullptr,
+    if ((e = launch_tensor_candidates(ctx, px, A0, n_pad, base + o_aB, m_pad, bA0, bdelta, beps2, lx, bf16, nullptr,
                                       false, nullptr, nullptr, nullptr, best)) != cudaSuccess)
         return cuda_fail(st, e, "ordering: anchor candidates");
     nearest_anchor_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(best, n, m, rank, keysA, valsA);
@@ -703,6 +738,11 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     ctx->launches += 2;
     if ((e = sort_by_work(ctx, prio_cnt, items, base + o_ws, (uint32_t*)(base + o_po))) != cudaSuccess)
         return cuda_fail(st, e, "ordering: work order");
+    // The operands in list order (bounds follow in the caller).
+    gather_operands_kernel<<<(unsigned)((n_pad + 127) / 128), 128, 0, s>>>(
+        (const uint4*)A0, (const uint4*)B0, bA0, eps0, perm, n, n_pad, (uint4*)A16, (uint4*)B16, bA, beps);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: operands");
+    ctx->launches += 1;
     out->perm = perm;
     out->prio = prio;
     out->prio_cnt = prio_cnt;
