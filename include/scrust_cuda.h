@@ -208,6 +208,40 @@ SCRUST_API int32_t scrust_cuda_smooth_knn_distances_noalloc(const float* distanc
                                                             float* sigmas, float* rhos, void* stream,
                                                             scrust_status* status);
 
+/* ---- Batches of independent samples (no reference counterpart) ----
+ *
+ * `n_samples` independent self-kNN solves in one tensor-form sweep.  The
+ * samples' rows are concatenated in `embedding` (device pointer, sum(n_s) x
+ * d f32); `row_offsets` (host, n_samples + 1 entries, starting at 0) gives
+ * each sample's rows.  Outputs are sum(n_s) x k, in the same row order, with
+ * neighbour ids relative to the sample's first row.  Each sample's result
+ * is bit-identical to a solve of that sample alone.  Exact mode only; d at
+ * most 61; every sample needs more than k cells. */
+typedef struct scrust_batch_plan scrust_batch_plan;
+/* Host pointers: uploads, solves, downloads and reports device errors. */
+SCRUST_API int32_t scrust_cuda_knn_batch(scrust_context* context, const float* embedding, const uint64_t* row_offsets,
+                                         uint32_t n_samples, uint64_t d, uint32_t k,
+                                         const scrust_knn_options* options, uint32_t* out_indices,
+                                         float* out_distances, scrust_status* status);
+SCRUST_API int32_t scrust_cuda_knn_batch_device(scrust_context* context, const float* embedding,
+                                                const uint64_t* row_offsets, uint32_t n_samples, uint64_t d,
+                                                uint32_t k, const scrust_knn_options* options,
+                                                uint32_t* out_indices, float* out_distances, scrust_status* status);
+/* A plan fixes the layout and the device buffers, autotunes the list
+ * capacity (when options->list_capacity is 0) and the operand precision on
+ * this batch, and captures the whole solve in a CUDA graph.  Each launch is
+ * one graph launch on the context stream. */
+SCRUST_API scrust_batch_plan* scrust_cuda_batch_plan_create(scrust_context* context, const uint64_t* row_offsets,
+                                                            uint32_t n_samples, uint64_t d, uint32_t k,
+                                                            const scrust_knn_options* options,
+                                                            const float* embedding, uint32_t* out_indices,
+                                                            float* out_distances, scrust_status* status);
+SCRUST_API int32_t scrust_cuda_batch_plan_launch(scrust_batch_plan* plan, scrust_status* status);
+/* The autotuner's choice and its time for one batch; returns 0 for NULL. */
+SCRUST_API int32_t scrust_cuda_batch_plan_choice(const scrust_batch_plan* plan, uint32_t* list_capacity,
+                                                 int32_t* precision, float* tuned_ms);
+SCRUST_API void scrust_cuda_batch_plan_destroy(scrust_batch_plan* plan);
+
 /* Phase timing.  When enabled, each kNN / connectivities call records CUDA
  * events on the context stream around its phases; scrust_cuda_phase_times
  * writes the last call's milliseconds (after a synchronise) in the order

@@ -112,6 +112,16 @@ _SIGNATURES = {
     "scrust_cuda_launch_count": (ctypes.c_uint64, [_P]),
     "scrust_cuda_kernel_stats": (ctypes.c_int32, [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64),
                                                    ctypes.c_int32]),
+    "scrust_cuda_knn_batch": (ctypes.c_int32, [_P, _P, _P, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32,
+                                                ctypes.POINTER(KnnOptions), _P, _P, ctypes.POINTER(Status)]),
+    "scrust_cuda_knn_batch_device": (ctypes.c_int32, [_P, _P, _P, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32,
+                                                       ctypes.POINTER(KnnOptions), _P, _P, ctypes.POINTER(Status)]),
+    "scrust_cuda_batch_plan_create": (_P, [_P, _P, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32,
+                                           ctypes.POINTER(KnnOptions), _P, _P, _P, ctypes.POINTER(Status)]),
+    "scrust_cuda_batch_plan_launch": (ctypes.c_int32, [_P, ctypes.POINTER(Status)]),
+    "scrust_cuda_batch_plan_choice": (ctypes.c_int32, [_P, ctypes.POINTER(ctypes.c_uint32),
+                                                        ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float)]),
+    "scrust_cuda_batch_plan_destroy": (None, [_P]),
     "scrust_cuda_version": (ctypes.c_char_p, []),
 }
 

@@ -149,3 +149,39 @@ def neighbors_graph(embedding, k, device="auto", *, metric: str = "euclidean", f
                                        ctypes.byref(st))
     _lib.check(rc, st)
     return idx, dist, _lib.csr_host_arrays(out)
+
+
+def knn_batch(embeddings, k, device, *, metric: str = "euclidean", precision: str = "fp16",
+              list_capacity: int = 0):
+    """Exact kNN of several independent samples in one tensor-form sweep.
+
+    `embeddings` is a sequence of (n_s, d) f32 arrays with the same d.  Returns
+    one (indices, distances) pair per sample, ids local to the sample; each is
+    bit-identical to `knn(embeddings[s], k, device, form="tensor")`.
+    """
+    mats = [_array2(e, np.float32, "embedding") for e in embeddings]
+    if not mats:
+        raise _lib.ScrustValueError(_lib.SHAPE, "expected at least one sample")
+    d = mats[0].shape[1]
+    if any(m.shape[1] != d for m in mats):
+        raise _lib.ScrustValueError(_lib.SHAPE, "expected every sample to have the same number of dimensions")
+    k = _k(k)
+    dev = _device_index(device)
+    offsets = np.zeros(len(mats) + 1, dtype=np.uint64)
+    offsets[1:] = np.cumsum([m.shape[0] for m in mats])
+    x = np.ascontiguousarray(np.concatenate(mats, axis=0)) if len(mats) > 1 else mats[0]
+    n = int(offsets[-1])
+    L = _lib.lib()
+    st = _lib.Status()
+    opts = _lib.options(form="tensor", metric=metric, precision=precision, list_capacity=list_capacity)
+    # Argument errors are reported before a device is required.
+    valid = 0 < d <= 61 and 0 < k <= 128 and all(m.shape[0] > k for m in mats)
+    ctx = _lib.context(dev) if valid else None
+    idx = np.empty((n, k), dtype=np.uint32)
+    dist = np.empty((n, k), dtype=np.float32)
+    rc = L.scrust_cuda_knn_batch(ctx, _lib.ptr(x) if x.size else None, _lib.ptr(offsets), len(mats), d, k,
+                                 ctypes.byref(opts), _lib.ptr(idx) if idx.size else None,
+                                 _lib.ptr(dist) if dist.size else None, ctypes.byref(st))
+    _lib.check(rc, st)
+    return [(idx[int(offsets[s]):int(offsets[s + 1])], dist[int(offsets[s]):int(offsets[s + 1])])
+            for s in range(len(mats))]

@@ -63,6 +63,19 @@ void* ws_get(scrust_context* ctx, Slot slot, size_t bytes, cudaError_t* err) {
     return ws.ptr[slot];
 }
 
+cudaError_t set_smem_limit(scrust_context* ctx, const void* func, int bytes) {
+    for (auto& pr : ctx->smem_limits)
+        if (pr.first == func) {
+            if (pr.second >= bytes) return cudaSuccess;
+            const cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            if (e == cudaSuccess) pr.second = bytes;
+            return e;
+        }
+    const cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) ctx->smem_limits.emplace_back(func, bytes);
+    return e;
+}
+
 bool encode_2d(scrust_context* ctx, CUtensorMap* map, CUtensorMapDataType dtype, void* base,
                uint64_t inner, uint64_t outer, uint64_t row_bytes, uint32_t box_inner,
                uint32_t box_outer, CUtensorMapSwizzle swizzle) {
@@ -86,6 +99,27 @@ void mark(scrust_context* ctx, Phase p) {
     if (p == PH_START)
         for (int i = 0; i < 7; i++) ctx->ev_recorded[i] = false;
     if (cudaEventRecord(ctx->ev[p], ctx->stream) == cudaSuccess) ctx->ev_recorded[p] = true;
+}
+
+// Maps the device error block to a status, then clears it.
+int32_t collect_device_errors(scrust_context* ctx, scrust_status* st) {
+    int h[DERR_COUNT] = {0};
+    cudaError_t e = cudaMemcpyAsync(h, ctx->d_err, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(st, e, "synchronize");
+    bool any = false;
+    for (int i = 0; i < DERR_COUNT; i++) any |= h[i] != 0;
+    if (!any) return ok(st);
+    cudaMemsetAsync(ctx->d_err, 0, sizeof(int) * DERR_COUNT, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    if (h[DERR_ZERO_ROW])
+        return fail(st, SCRUST_SHAPE, "expected rows with a non-zero norm for the cosine metric, got an all-zero row");
+    if (h[DERR_BAD_INDEX]) return fail(st, SCRUST_SHAPE, "expected neighbour ids below n, got an out-of-range neighbour id");
+    if (h[DERR_TIMEOUT]) return fail(st, SCRUST_TIMEOUT, "CUDA kernel knn: a bounded device wait ran out");
+    if (h[DERR_TIE_OVERFLOW])
+        return fail(st, SCRUST_KERNEL,
+                    "CUDA kernel knn_rerank: more than 4096 cells are equidistant from one cell within f32 resolution");
+    return fail(st, SCRUST_KERNEL, "CUDA kernel knn_rerank: inconsistent candidate set");
 }
 
 namespace {
@@ -128,26 +162,6 @@ int32_t check_options(const scrust_knn_options* o, scrust_status* st) {
     return SCRUST_OK;
 }
 
-// Maps the device error block to a status, then clears it.
-int32_t collect_device_errors(scrust_context* ctx, scrust_status* st) {
-    int h[DERR_COUNT] = {0};
-    cudaError_t e = cudaMemcpyAsync(h, ctx->d_err, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(st, e, "synchronize");
-    bool any = false;
-    for (int i = 0; i < DERR_COUNT; i++) any |= h[i] != 0;
-    if (!any) return ok(st);
-    cudaMemsetAsync(ctx->d_err, 0, sizeof(int) * DERR_COUNT, ctx->stream);
-    cudaStreamSynchronize(ctx->stream);
-    if (h[DERR_ZERO_ROW])
-        return fail(st, SCRUST_SHAPE, "expected rows with a non-zero norm for the cosine metric, got an all-zero row");
-    if (h[DERR_BAD_INDEX]) return fail(st, SCRUST_SHAPE, "expected neighbour ids below n, got an out-of-range neighbour id");
-    if (h[DERR_TIMEOUT]) return fail(st, SCRUST_TIMEOUT, "CUDA kernel knn: a bounded device wait ran out");
-    if (h[DERR_TIE_OVERFLOW])
-        return fail(st, SCRUST_KERNEL,
-                    "CUDA kernel knn_rerank: more than 4096 cells are equidistant from one cell within f32 resolution");
-    return fail(st, SCRUST_KERNEL, "CUDA kernel knn_rerank: inconsistent candidate set");
-}
 
 struct KnnBuffers {
     const float* xr = nullptr;   // rows the rerank measures

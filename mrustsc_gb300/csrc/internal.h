@@ -51,6 +51,8 @@ enum Slot : int {
     SLOT_ORDER,         // row ordering: anchors, permutation, priority tiles
     SLOT_PRUNE,         // tile balls and the tile lists of the second sweep pass
     SLOT_XSORTED,       // working rows in list order (ordered solves)
+    SLOT_BATCH,         // batch layout maps, work order, thresholds
+    SLOT_BATCH_TABLE,   // batch sample table
     SLOT_COUNT
 };
 
@@ -85,6 +87,7 @@ struct scrust_context {
     bool timing = false;
     cudaEvent_t ev[7] = {};             // phase boundaries: prep | candidates | rerank | connectivities,
     bool ev_recorded[7] = {};           // and inside candidates: first sweep pass | second-pass tile lists
+    std::vector<std::pair<const void*, int>> smem_limits;  // dynamic shared memory limits already set
 };
 
 struct scrust_csr {
@@ -104,10 +107,17 @@ namespace scrust {
 enum Phase { PH_START = 0, PH_PREP = 1, PH_CAND = 2, PH_RERANK = 3, PH_CONN = 4, PH_PASS1 = 5, PH_LISTS = 6 };
 void mark(scrust_context* ctx, Phase p);
 
+// Maps the device error block to a status, then clears it (synchronises).
+int32_t collect_device_errors(scrust_context* ctx, scrust_status* st);
+
 // Status helpers.
 int32_t fail(scrust_status* st, int32_t code, const char* fmt, ...);
 int32_t ok(scrust_status* st);
 int32_t cuda_fail(scrust_status* st, cudaError_t e, const char* what);
+
+// Raises a kernel's dynamic shared memory limit once per context (so that
+// launches can be captured into a CUDA graph afterwards).
+cudaError_t set_smem_limit(scrust_context* ctx, const void* func, int bytes);
 
 // Workspace access (may cudaMalloc; call with the context lock held).
 void* ws_get(scrust_context* ctx, Slot slot, size_t bytes, cudaError_t* err);
@@ -209,6 +219,10 @@ struct TileLists {
     const uint32_t* count = nullptr;   // per row block
     int stride = 0;
     const uint32_t* order = nullptr;   // row blocks by decreasing count, or null
+    // Without explicit tiles: per row block the column tile range [x, y) it
+    // sweeps (a batch of independent solves laid out block-diagonally), or null.
+    const uint2* range = nullptr;
+    const uint32_t* row_map = nullptr;  // query row -> input row, 0xffffffff for padding; null: identity
 };
 // One pass of the tensor sweep.  `tiles` null: every column tile, outward
 // from the diagonal.  `resume`: lists and thresholds continue from an earlier
@@ -234,14 +248,22 @@ struct RowBounds {
 // rerank.cu.  With a permutation, list row s and list entry c stand for
 // input rows perm[s] and perm[c]; outputs are written in input order.  With
 // xs (the working rows in list order) and theta (each list's threshold at
-// the end of the candidate pass) as well, no selection is needed.
+// the end of the candidate pass) as well, no selection is needed.  List rows
+// whose perm entry is 0xffffffff are padding and skipped.  row_lo/row_hi
+// (per input row) confine a batch's solves: ids are reported relative to
+// row_lo and the fallback scans [row_lo, row_hi).
 cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float* qx,
                           const float* rx, const float* qnorm2, const float* rnorm2,
                           const double* qn64, const double* rn64, const float* qraw,
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
                           const uint32_t* perm, const float* xs, const float* theta, uint32_t* out_idx,
-                          float* out_dist);
-// order.cu: rows of x in list order, xs[s] = x[perm[s]].
+                          float* out_dist, const uint32_t* row_lo = nullptr, const uint32_t* row_hi = nullptr);
+// order.cu: row blocks sorted by decreasing count (stable) into `order`;
+// `scratch` holds work_order_scratch(items) bytes.
+size_t work_order_scratch(int items);
+cudaError_t sort_by_work(scrust_context* ctx, const uint32_t* counts, int items, char* scratch, uint32_t* order);
+// order.cu: rows of x in list order, xs[s] = x[perm[s]] (zeros where perm
+// holds 0xffffffff).
 cudaError_t launch_gather_rows(const float* x, const uint32_t* perm, int64_t n, int d, float* xs, cudaStream_t s);
 
 // conn.cu

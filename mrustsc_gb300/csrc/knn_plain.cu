@@ -239,8 +239,7 @@ cudaError_t launch_plain_candidates(scrust_context* ctx, const KnnPlan& plan, co
     if ((a.col_tiles + a.tiles_per_seg - 1) / a.tiles_per_seg != lists.segments) return cudaErrorInvalidValue;
     a.err = ctx->d_err;
     const size_t smem = plain_smem_bytes(dp);
-    cudaError_t e = cudaFuncSetAttribute(plain_candidates_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = set_smem_limit(ctx, (const void*)plain_candidates_kernel, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((unsigned)(nq_pad / BM), (unsigned)lists.segments);
     plain_candidates_kernel<<<grid, THREADS, smem, ctx->stream>>>(tq, tr, a);

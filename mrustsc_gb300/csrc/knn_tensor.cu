@@ -80,6 +80,8 @@ struct TensorArgs {
     const uint32_t* tl_cnt;
     int tl_stride;
     const uint32_t* item_order; // items by decreasing work, dealt out in a snake, or null: round robin
+    const uint2* item_range;    // per item its column tiles [x, y) (one column segment), or null
+    const uint32_t* row_map;    // per query row its input row, 0xffffffff for padding; null: all rows real
     // k = 1 without lists: per (row, part) the smallest MMA value and its
     // column, packed as float_key << 32 | column; null otherwise.
     unsigned long long* argmin_out;
@@ -417,8 +419,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             bool ok = true;
             for (int j = 0, w; ok && (w = item_at(a, j)) >= 0; ++j) {
                 const int qt = w / csegs, seg = w % csegs;
-                const int ct0 = seg * a.tiles_per_seg;
-                const int ct1 = min(a.col_tiles, ct0 + a.tiles_per_seg);
+                const int ct0 = a.item_range ? (int)a.item_range[w].x : seg * a.tiles_per_seg;
+                const int ct1 = a.item_range ? (int)a.item_range[w].y : min(a.col_tiles, ct0 + a.tiles_per_seg);
                 const TileOrder order(a, w, qt, ct0, ct1);
                 if (order.count == 0) continue;
                 const uint32_t ab = ac & 1, au = ac >> 1;
@@ -460,8 +462,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             bool ok = true;
             for (int j = 0, w; ok && (w = item_at(a, j)) >= 0; ++j) {
                 const int qt = w / csegs, seg = w % csegs;
-                const int ct0 = seg * a.tiles_per_seg;
-                const int ct1 = min(a.col_tiles, ct0 + a.tiles_per_seg);
+                const int ct0 = a.item_range ? (int)a.item_range[w].x : seg * a.tiles_per_seg;
+                const int ct1 = a.item_range ? (int)a.item_range[w].y : min(a.col_tiles, ct0 + a.tiles_per_seg);
                 const TileOrder order(a, w, qt, ct0, ct1);
                 if (order.count == 0) continue;
                 const uint32_t ab = ac & 1, au = ac >> 1;
@@ -530,12 +532,12 @@ __global__ void __launch_bounds__(THREADS, 1)
         bool ok = true;
         for (int j = 0, w; ok && (w = item_at(a, j)) >= 0; ++j) {
             const int qt = w / col_segs, seg = w % col_segs;
-            const int ct0 = seg * a.tiles_per_seg;
-            const int ct1 = min(a.col_tiles, ct0 + a.tiles_per_seg);
+            const int ct0 = a.item_range ? (int)a.item_range[w].x : seg * a.tiles_per_seg;
+            const int ct1 = a.item_range ? (int)a.item_range[w].y : min(a.col_tiles, ct0 + a.tiles_per_seg);
             const TileOrder order(a, w, qt, ct0, ct1);
             if (order.count == 0) continue;
             const int64_t row = (int64_t)qt * ROWS + h * TBM + r_local;
-            const bool valid = row < a.nq;
+            const bool valid = row < a.nq && (!a.row_map || a.row_map[row] != 0xffffffffu);
             float th = valid ? __int_as_float(0x7f800000) : __int_as_float(0xff800000);
             uint32_t cnt = 0;
             TensorBound bnd{0.f, 0.f, 0.f};
@@ -705,7 +707,8 @@ __device__ __forceinline__ __nv_bfloat16 to16<__nv_bfloat16>(float v) {
 __device__ __forceinline__ double f64_of(__half v) { return (double)__half2float(v); }
 __device__ __forceinline__ double f64_of(__nv_bfloat16 v) { return (double)__bfloat162float(v); }
 
-// One thread per padded row: writes A_i and B_i of input row perm[i] (64 16-bit values each), the
+// One thread per padded row: writes A_i and B_i of input row perm[i] (a
+// padding row where perm[i] is 0xffffffff or i >= n) (64 16-bit values each), the
 // quantised squared norm A = |a_hat|^2, the per-row error radius
 // eps = |a_hat - scale*c| + scale*u*|c| (+ scale*u for normalised rows), and
 // the running maxima of eps and |b_hat|.
@@ -731,7 +734,8 @@ __global__ void tensor_operands_kernel(const float* __restrict__ x, int64_t n, i
         arow[t] = zero;
         brow[t] = zero;
     }
-    if (i < n) {
+    const bool real = i < n && (!perm || perm[i] != 0xffffffffu);
+    if (real) {
         const int64_t src = perm ? (int64_t)perm[i] : i;
         double hh = 0.0, e2 = 0.0, c2 = 0.0;
         for (int t = 0; t < d; t++) {
@@ -767,6 +771,11 @@ __global__ void tensor_operands_kernel(const float* __restrict__ x, int64_t n, i
         atomicMax(max_eps_bits, __float_as_uint(epf));
         atomicMax(max_bhat_bits, __float_as_uint(__double2float_ru(sqrt(hh))));
     } else {
+        // Padding: a reference row whose value against any query is +inf,
+        // so it can never become a candidate (and a query row with the same
+        // ones as a real row, so that no product is 0 * inf).
+        brow[d] = to16<T>(__int_as_float(0x7f800000));
+        arow[d] = arow[d + 1] = arow[d + 2] = to16<T>(1.0f);
         bA[i] = 0.f;
         eps[i] = 0.f;
     }
@@ -866,6 +875,10 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.tl_cnt = nullptr;
     a.tl_stride = 0;
     a.item_order = nullptr;
+    a.item_range = tiles ? tiles->range : nullptr;
+    a.row_map = tiles ? tiles->row_map : nullptr;
+    if (tiles && !tiles->tiles) a.item_order = tiles->order;
+    if (a.item_range && lists.segments != PARTS) return cudaErrorInvalidValue;
     if (tiles && tiles->tiles) {
         // Explicit tile lists are per row block: one column segment only.
         if (col_segs != 1 || !tiles->count) return cudaErrorInvalidValue;
@@ -882,7 +895,7 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     if (resume && !theta_io) return cudaErrorInvalidValue;
     auto kern = a.k == 1 ? tensor_candidates_kernel<1> : a.k <= 16 ? tensor_candidates_kernel<16>
                                                                    : tensor_candidates_kernel<0>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+    cudaError_t e = set_smem_limit(ctx, (const void*)kern, (int)SMEM_BYTES);
     if (e != cudaSuccess) return e;
     const int grid = std::min(a.items, ctx->sm_count);
     if (grid_out) *grid_out = grid;

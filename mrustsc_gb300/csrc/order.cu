@@ -568,7 +568,8 @@ __global__ void gather_rows_kernel(const float* __restrict__ x, const uint32_t* 
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n * d) return;
     const int64_t s = i / d, t = i % d;
-    xs[i] = x[(int64_t)perm[s] * d + t];
+    const uint32_t r = perm[s];
+    xs[i] = r == 0xffffffffu ? 0.f : x[(int64_t)r * d + t];
 }
 
 }  // namespace
@@ -681,8 +682,7 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     anchor_knn_kernel<<<(unsigned)m, AK_THREADS, sizeof(float) * (size_t)m, s>>>(anc, m, d, anchor_nb);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor neighbours");
     const size_t chain_smem = 4 * (size_t)((m + 31) / 32) + 2 * (size_t)m * kChainNb;
-    if ((e = cudaFuncSetAttribute(anchor_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)chain_smem)) != cudaSuccess)
+    if ((e = set_smem_limit(ctx, (const void*)anchor_chain_kernel, (int)chain_smem)) != cudaSuccess)
         return cuda_fail(st, e, "ordering: anchor walk");
     anchor_chain_kernel<<<1, 32, chain_smem, s>>>(anchor_nb, (int)m, rank);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor walk");
@@ -810,7 +810,7 @@ int32_t build_second_pass(scrust_context* ctx, const void* A16, bool bf16, int64
     segment_pairs_kernel<<<8 * ctx->sm_count, 256, 0, s>>>(fc, fr, fu, fo, seg_off + tiles, d, words, bitmap);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "pruning: segment pairs");
     const size_t lists_smem = 4 * (size_t)words;
-    if ((e = cudaFuncSetAttribute(tile_lists_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lists_smem)) !=
+    if ((e = set_smem_limit(ctx, (const void*)tile_lists_kernel, (int)lists_smem)) !=
         cudaSuccess)
         return cuda_fail(st, e, "pruning: tile lists");
     tile_lists_kernel<<<tiles, 256, lists_smem, s>>>(bitmap, words, tiles, order.prio, order.prio_cnt, counts, entries);

@@ -40,6 +40,8 @@ struct RerankArgs {
     Lists lists;
     const uint32_t* perm;  // list row / list entry -> input row, or null
     const float* xs;       // working rows in list order (ordered solves), or null
+    const uint32_t* row_lo;  // per input row: first row of its solve (a batch of solves), or null
+    const uint32_t* row_hi;  // per input row: end of its solve
     const float* theta;    // per list: its threshold when the candidate pass ended, or null
     int64_t nq, nr;
     int d, k, mode, metric, self;
@@ -116,7 +118,7 @@ __device__ void finalize_row(const Team& team, const RerankArgs& a, int64_t q,
                 dist = __double2float_rn(dbl[p]);
             else
                 dist = sqrtf(key_r(keys[p]));
-            a.out_idx[q * k + pos] = id;
+            a.out_idx[q * k + pos] = a.row_lo ? id - a.row_lo[q] : id;
             a.out_dist[q * k + pos] = dist;
         }
     }
@@ -139,7 +141,7 @@ __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a
     unsigned long long* A = rr_smem + (size_t)warp * 2 * RC;
     unsigned long long* B = A + RC;
     const int64_t slot = (int64_t)blockIdx.x * RR_WARPS + warp;  // list row
-    if (slot >= a.nq) return;
+    if (slot >= a.nq || (a.perm && a.perm[slot] == 0xffffffffu)) return;
     WarpTeam team;
     if (a.lists.overflow[slot]) {
         if (lane == 0) push_fallback(a, slot);
@@ -215,7 +217,7 @@ __global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs
     unsigned long long* keys = rs_smem + (size_t)warp * 2 * RS_KEYS;
     double* dbl = reinterpret_cast<double*>(keys + RS_KEYS);
     const int64_t slot = (int64_t)blockIdx.x * RS_WARPS + warp;
-    if (slot >= a.nq) return;
+    if (slot >= a.nq || a.perm[slot] == 0xffffffffu) return;  // padding of a batch layout
     WarpTeam team;
     if (a.lists.overflow[slot]) {
         if (lane == 0) push_fallback(a, slot);
@@ -289,8 +291,10 @@ __global__ void __launch_bounds__(FB_THREADS) rerank_fallback_kernel(RerankArgs 
         __syncthreads();
         if (row == 0xffffffffu) break;
         const int64_t q = input_row(a, row);
+        // The columns of the row's own solve: [lo, hi) of the input rows.
+        const int64_t lo = a.row_lo ? (int64_t)a.row_lo[q] : 0, hi = a.row_lo ? (int64_t)a.row_hi[q] : a.nr;
         for (int64_t j = tid; j < a.nr; j += blockDim.x)
-            sc[j] = (a.self && j == q) ? __int_as_float(0x7f800000) : compute_r(a, q, (uint32_t)j);
+            sc[j] = (a.self && j == q) || j < lo || j >= hi ? __int_as_float(0x7f800000) : compute_r(a, q, (uint32_t)j);
         __syncthreads();
         // k-th smallest of the row: four 8-bit radix passes.
         if (tid == 0) {
@@ -374,7 +378,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
                           const double* qn64, const double* rn64, const float* qraw,
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
                           const uint32_t* perm, const float* xs, const float* theta, uint32_t* out_idx,
-                          float* out_dist) {
+                          float* out_dist, const uint32_t* row_lo, const uint32_t* row_hi) {
     cudaError_t e;
     uint32_t* fb_rows = (uint32_t*)ws_get(ctx, SLOT_FALLBACK_ROWS, sizeof(uint32_t) * (size_t)plan.nq, &e);
     if (!fb_rows) return e;
@@ -395,6 +399,8 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.perm = perm;
     a.xs = xs;
     a.theta = theta;
+    a.row_lo = row_lo;
+    a.row_hi = row_hi;
     a.nq = plan.nq;
     a.nr = plan.nr;
     a.d = plan.d;
@@ -418,14 +424,14 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
         rerank_sorted_kernel<<<blocks, RS_WARPS * 32, smem_s, ctx->stream>>>(a);
     } else {
         const size_t smem_w = (size_t)RR_WARPS * 2 * RC * sizeof(unsigned long long);
-        e = cudaFuncSetAttribute(rerank_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_w);
+        e = set_smem_limit(ctx, (const void*)rerank_warp_kernel, (int)smem_w);
         if (e != cudaSuccess) return e;
         const unsigned blocks = (unsigned)((plan.nq + RR_WARPS - 1) / RR_WARPS);
         rerank_warp_kernel<<<blocks, RR_WARPS * 32, smem_w, ctx->stream>>>(a);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const size_t smem_f = (size_t)FB_CAP * (sizeof(unsigned long long) + sizeof(double));
-    e = cudaFuncSetAttribute(rerank_fallback_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
+    e = set_smem_limit(ctx, (const void*)rerank_fallback_kernel, (int)smem_f);
     if (e != cudaSuccess) return e;
     rerank_fallback_kernel<<<FB_BLOCKS, FB_THREADS, smem_f, ctx->stream>>>(a);
     return cudaGetLastError();
