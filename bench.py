@@ -52,6 +52,10 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-recall", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--workload", choices=["precision", "batching", "serving", "scale"], default="precision",
+                   help="precision: the 1M x 50 graph build (default); batching: 64 samples in one graph launch "
+                        "against 64 sequential plain launches; serving: the resident-atlas query service; "
+                        "scale: 100k x 50, k = 30, Euclidean and cosine")
     return p.parse_args()
 
 
@@ -383,10 +387,184 @@ def run_ours(args):
     return 0
 
 
+# --------------------------------------------------------------------------- batching
+
+def run_batching(args):
+    """64 samples (sizes log-uniform in [500, 50,000], 4-20 clusters each, k = 15): one CUDA-graph
+    launch of the batched tensor sweep, against 64 sequential plain-form launches on the same data."""
+    import torch
+
+    from mrustsc_gb300 import _lib, build, synthetic
+
+    build.build()
+    L = _lib.lib()
+    k, d = 15, 50
+    samples = synthetic.batch_samples(seed=0)
+    sizes = [len(x) for x in samples]
+    x = np.concatenate(samples)
+    n = len(x)
+    offsets = np.zeros(len(samples) + 1, dtype=np.uint64)
+    offsets[1:] = np.cumsum(sizes)
+    ctx = _lib.context(0)
+    stream = torch.cuda.ExternalStream(L.scrust_cuda_context_stream(ctx))
+    xd = torch.from_numpy(x).cuda()
+    idx = torch.empty((n, k), dtype=torch.int32, device="cuda")
+    dst = torch.empty((n, k), dtype=torch.float32, device="cuda")
+    st = _lib.Status()
+    opts = _lib.options(form="tensor")
+    t0 = time.perf_counter()
+    plan = L.scrust_cuda_batch_plan_create(ctx, _lib.ptr(offsets), len(samples), d, k, ctypes.byref(opts),
+                                           xd.data_ptr(), idx.data_ptr(), dst.data_ptr(), ctypes.byref(st))
+    if not plan:
+        raise RuntimeError(st.message.decode())
+    plan_s = time.perf_counter() - t0
+    cap, prec, tuned = ctypes.c_uint32(), ctypes.c_int32(), ctypes.c_float()
+    L.scrust_cuda_batch_plan_choice(plan, ctypes.byref(cap), ctypes.byref(prec), ctypes.byref(tuned))
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / steps
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    launches0 = L.scrust_cuda_launch_count(ctx)
+    ms_graph = timed(lambda: _lib.check(L.scrust_cuda_batch_plan_launch(plan, ctypes.byref(st)), st),
+                     args.steps, args.warmup)
+    launches = int(L.scrust_cuda_launch_count(ctx) - launches0)
+    clk = clocks.stop()
+    graph_idx = idx.clone()
+
+    plain = _lib.options(form="plain")
+    views = [(xd[int(offsets[s]):int(offsets[s + 1])], idx[int(offsets[s]):int(offsets[s + 1])],
+              dst[int(offsets[s]):int(offsets[s + 1])]) for s in range(len(samples))]
+
+    def sequential(o):
+        def run():
+            for xs, ii, dd in views:
+                _lib.check(L.scrust_cuda_knn_device(ctx, xs.data_ptr(), len(xs), d, k, ctypes.byref(o),
+                                                    ii.data_ptr(), dd.data_ptr(), ctypes.byref(st)), st)
+        return run
+
+    seq_steps = max(1, min(args.steps, 3))
+    ms_plain = timed(sequential(plain), seq_steps, 1)
+    same = bool((graph_idx == idx).all().item())
+    ms_tensor_seq = timed(sequential(opts), seq_steps, 1)
+    L.scrust_cuda_batch_plan_destroy(plan)
+
+    # e2e through the host-pointer batch call: upload, solve, download.
+    ih = np.empty((n, k), np.uint32)
+    dh = np.empty((n, k), np.float32)
+    xh = np.ascontiguousarray(x)
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        _lib.check(L.scrust_cuda_knn_batch(ctx, xh.ctypes.data, _lib.ptr(offsets), len(samples), d, k,
+                                           ctypes.byref(opts), ih.ctypes.data, dh.ctypes.data, ctypes.byref(st)), st)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    flops = sum(2.0 * m * m * d for m in sizes)
+    line = {"metric": "batched kNN cells/s (64 samples, one CUDA-graph launch)", "value": n / (ms_graph / 1e3),
+            "unit": "cells/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_graph,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16" if prec.value == 0 else "bf16",
+            "data": "synthetic",
+            "config": {"workload": "batching_64_samples_k15", "samples": len(samples), "cells": n, "dims": d, "k": k,
+                       "sizes": "log-uniform [500, 50000], seed 0", "sum_2n2d_flop": flops,
+                       "l2": "inputs and lists larger than L2"},
+            "comparator": {"sequential_plain_ms": ms_plain, "sequential_tensor_ms": ms_tensor_seq,
+                           "speedup_vs_sequential_plain": ms_plain / ms_graph,
+                           "results_identical_to_sequential_plain": same},
+            "autotuner": {"list_capacity": cap.value, "precision": "fp16" if prec.value == 0 else "bf16",
+                          "tuned_ms": tuned.value, "plan_create_s": plan_s},
+            "gpu_launches": launches, "clocks": clk,
+            "e2e": {"value": n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": n * d * 4,
+                    "d2h_bytes_per_step": n * k * 8, "ms_per_step": e2e_s * 1e3}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------------- plain scale (100k, k = 30)
+
+def run_scale(args):
+    """100,000 x 50, k = 30, 40 clusters, 0.5% duplicates and 0.5% near-duplicates: the graph build
+    (kNN + connectivities) for the Euclidean and the cosine metric, plain and tensor forms."""
+    import torch
+
+    from mrustsc_gb300 import _lib, build, synthetic
+
+    build.build()
+    L = _lib.lib()
+    n, d, k = 100_000, 50, 30
+    x = synthetic.plain_scale(seed=0, n=n)
+    ctx = _lib.context(0)
+    stream = torch.cuda.ExternalStream(L.scrust_cuda_context_stream(ctx))
+    xd = torch.from_numpy(x).cuda()
+    idx = torch.empty((n, k), dtype=torch.int32, device="cuda")
+    dst = torch.empty((n, k), dtype=torch.float32, device="cuda")
+    st = _lib.Status()
+    csr = ctypes.c_void_p()
+    res = {}
+    clocks = ClockSampler(0)
+    clocks.start()
+    for metric in ("euclidean", "cosine"):
+        outs = {}
+        for form in ("plain", "tensor"):
+            o = _lib.options(form=form, metric=metric)
+
+            def step():
+                _lib.check(L.scrust_cuda_neighbors_graph_device(ctx, xd.data_ptr(), n, d, k, ctypes.byref(o),
+                                                                idx.data_ptr(), dst.data_ptr(), ctypes.byref(csr),
+                                                                ctypes.byref(st)), st)
+                L.scrust_csr_free(csr)
+
+            for _ in range(args.warmup):
+                step()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            steps = max(1, min(args.steps, 10))
+            a.record(stream)
+            for _ in range(steps):
+                step()
+            b.record(stream)
+            b.synchronize()
+            ms = a.elapsed_time(b) / steps
+            outs[form] = idx.clone()
+            res[f"{metric}_{form}"] = {"cells_per_s": n / (ms / 1e3), "ms_per_step": ms}
+        res[f"{metric}_forms_identical"] = bool((outs["plain"] == outs["tensor"]).all().item())
+    clk = clocks.stop()
+    best = res["euclidean_tensor"]
+    line = {"metric": "kNN-graph cells/s at 100k x 50, k = 30", "value": best["cells_per_s"], "unit": "cells/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": best["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16", "data": "synthetic",
+            "config": {"workload": "plain_scale_100k_x50_k30", "n_cells": n, "dims": d, "k": k, "clusters": 40,
+                       "dup_frac": 0.005, "near_dup_frac": 0.005},
+            "results": res, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_serving(args):
+    from mrustsc_gb300 import serving
+
+    return serving.bench_main(args)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batching":
+        return run_batching(args)
+    if args.workload == "serving":
+        return run_serving(args)
+    if args.workload == "scale":
+        return run_scale(args)
     return run_ours(args)
 
 

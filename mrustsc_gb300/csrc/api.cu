@@ -125,7 +125,7 @@ int32_t collect_device_errors(scrust_context* ctx, scrust_status* st) {
 namespace {
 
 constexpr uint32_t kMaxK = 128;
-constexpr int64_t kOrderMinRows = 65536;  // automatic ordering from this many rows
+constexpr int64_t kOrderMinRows = 1024;  // automatic ordering from this many rows
 
 int32_t check_knn_args(uint64_t n, uint64_t d, uint32_t k, scrust_status* st) {
     if (n == 0 || d == 0)
@@ -299,8 +299,12 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
                                 (o.ordering == SCRUST_ORDERING_ON     ? (o.segments <= 1)
                                  : o.ordering == SCRUST_ORDERING_AUTO ? (o.segments <= 1 && n >= kOrderMinRows)
                                                                       : false);
+        // One column segment (two column parts) unless asked otherwise: every
+        // list then sees all of its row's columns, its threshold is the row's
+        // own, and the rerank needs no selection.
         scrust_knn_options lo = o;
-        if (order_rows) lo.segments = 1;
+        if (order_rows || o.segments == 0) lo.segments = 1;
+        const bool keep_theta = lo.segments == 1;
         RowOrder order;
         if (order_rows) {
             int32_t rc = build_row_order(ctx, xwork, n, d, means, max_bits, cosine, bf16, A16, B16, bA, beps, bdelta,
@@ -351,8 +355,15 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
                 return cuda_fail(st, e, "knn_candidates_tc");
             ctx->launches += 2;
         } else {
+            float* theta = nullptr;
+            if (keep_theta) {
+                theta = (float*)ws_get(ctx, SLOT_THETA, sizeof(float) * 2 * (size_t)n_pad, &e);
+                if (!theta) return cuda_fail(st, e, "workspace");
+                rerank_xs = xwork;
+                rerank_theta = theta;
+            }
             if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                              nullptr, false, nullptr, nullptr, ctx->d_stats)) != cudaSuccess)
+                                              nullptr, false, theta, nullptr, ctx->d_stats)) != cudaSuccess)
                 return cuda_fail(st, e, "knn_candidates_tc");
             ctx->launches += 1;
         }

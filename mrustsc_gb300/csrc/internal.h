@@ -53,6 +53,7 @@ enum Slot : int {
     SLOT_XSORTED,       // working rows in list order (ordered solves)
     SLOT_BATCH,         // batch layout maps, work order, thresholds
     SLOT_BATCH_TABLE,   // batch sample table
+    SLOT_THETA,         // list thresholds of an unordered tensor-form solve
     SLOT_COUNT
 };
 

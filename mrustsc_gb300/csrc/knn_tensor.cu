@@ -360,8 +360,8 @@ __device__ __forceinline__ void prune_lanes(uint32_t need, const TensorArgs& a, 
     }
 }
 
-// TOPK = K (k <= K, K = 1 or 16): thresholds from a register top-K per lane
-// (TopK); TOPK = 0: from warp-cooperative selections over the lists.
+// TOPK = K (k <= K, K = 1, 16 or 32): thresholds from a register top-K per
+// lane (TopK); TOPK = 0: from warp-cooperative selections over the lists.
 template <int TOPK>
 __global__ void __launch_bounds__(THREADS, 1)
     tensor_candidates_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
@@ -574,20 +574,31 @@ __global__ void __launch_bounds__(THREADS, 1)
                     // First look: the tile's columns update the top-K and the
                     // threshold.  Second look: chunks holding columns below
                     // the tightened threshold are read again and appended.
-                    uint32_t va[32], vb[32];
+                    uint32_t va[32];
                     float cm[4];
-                    tmem_ld32(tbase, va);
-                    tmem_ld_wait(va);
-                    tmem_ld32(tbase + 32, vb);
-                    cm[0] = topk_chunk(va, col0, th, row, a, top, bnd, best);
-                    tmem_ld_wait(vb);
-                    tmem_ld32(tbase + 64, va);
-                    cm[1] = topk_chunk(vb, col0 + 32, th, row, a, top, bnd, best);
-                    tmem_ld_wait(va);
-                    tmem_ld32(tbase + 96, vb);
-                    cm[2] = topk_chunk(va, col0 + 64, th, row, a, top, bnd, best);
-                    tmem_ld_wait(vb);
-                    cm[3] = topk_chunk(vb, col0 + 96, th, row, a, top, bnd, best);
+                    if constexpr (TOPK <= 16) {
+                        uint32_t vb[32];
+                        tmem_ld32(tbase, va);
+                        tmem_ld_wait(va);
+                        tmem_ld32(tbase + 32, vb);
+                        cm[0] = topk_chunk(va, col0, th, row, a, top, bnd, best);
+                        tmem_ld_wait(vb);
+                        tmem_ld32(tbase + 64, va);
+                        cm[1] = topk_chunk(vb, col0 + 32, th, row, a, top, bnd, best);
+                        tmem_ld_wait(va);
+                        tmem_ld32(tbase + 96, vb);
+                        cm[2] = topk_chunk(va, col0 + 64, th, row, a, top, bnd, best);
+                        tmem_ld_wait(vb);
+                        cm[3] = topk_chunk(vb, col0 + 96, th, row, a, top, bnd, best);
+                    } else {
+                        // A top-32 leaves no registers for a second chunk in flight.
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            tmem_ld32(tbase + 32 * c, va);
+                            tmem_ld_wait(va);
+                            cm[c] = topk_chunk(va, col0 + 32 * c, th, row, a, top, bnd, best);
+                        }
+                    }
                     const unsigned long long o2 = *other_th;
                     if ((o2 & 0xffffffff00000000ull) == tag) th = fminf(th, __uint_as_float((uint32_t)o2));
 #pragma unroll
@@ -893,8 +904,10 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.argmin_out = argmin_out;
     if (argmin_out && (plan.k != 1 || resume)) return cudaErrorInvalidValue;
     if (resume && !theta_io) return cudaErrorInvalidValue;
-    auto kern = a.k == 1 ? tensor_candidates_kernel<1> : a.k <= 16 ? tensor_candidates_kernel<16>
-                                                                   : tensor_candidates_kernel<0>;
+    auto kern = a.k == 1    ? tensor_candidates_kernel<1>
+                : a.k <= 16 ? tensor_candidates_kernel<16>
+                : a.k <= 32 ? tensor_candidates_kernel<32>
+                            : tensor_candidates_kernel<0>;
     cudaError_t e = set_smem_limit(ctx, (const void*)kern, (int)SMEM_BYTES);
     if (e != cudaSuccess) return e;
     const int grid = std::min(a.items, ctx->sm_count);

@@ -202,12 +202,13 @@ __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a
     finalize_row(team, a, q, B, m, reinterpret_cast<double*>(A));
 }
 
-// Ordered solves: the candidate pass left every list with a threshold no
+// Tensor-form solves: the candidate pass left every list with a threshold no
 // smaller than the final one, so the rerank needs no selection.  A warp per
 // list row keeps the entries below the smaller of its lists' thresholds,
-// measures them on the working rows laid out in list order (neighbouring
-// rows share candidates, which stay in cache), and finishes as above with
-// input ids.  More than RS_KEYS survivors go to the fallback.
+// measures them on the working rows laid out in list order (for an ordered
+// solve neighbouring rows share candidates, which stay in cache), and
+// finishes as above with input ids.  More than RS_KEYS survivors go to the
+// fallback.
 constexpr int RS_WARPS = 8;
 constexpr int RS_KEYS = 256;
 __global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs a) {
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs
     unsigned long long* keys = rs_smem + (size_t)warp * 2 * RS_KEYS;
     double* dbl = reinterpret_cast<double*>(keys + RS_KEYS);
     const int64_t slot = (int64_t)blockIdx.x * RS_WARPS + warp;
-    if (slot >= a.nq || a.perm[slot] == 0xffffffffu) return;  // padding of a batch layout
+    if (slot >= a.nq || (a.perm && a.perm[slot] == 0xffffffffu)) return;  // padding of a batch layout
     WarpTeam team;
     if (a.lists.overflow[slot]) {
         if (lane == 0) push_fallback(a, slot);
@@ -248,7 +249,7 @@ __global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs
                 const int pos = m + __popc(ballot & lanemask_lt());
                 if (pos < RS_KEYS) {
                     const float r = dist2_f32(xq, a.xs + (int64_t)id * a.d, a.d);
-                    keys[pos] = ((unsigned long long)float_key(r) << 32) | a.perm[id];
+                    keys[pos] = ((unsigned long long)float_key(r) << 32) | (uint32_t)input_row(a, id);
                 }
             }
             m += __popc(ballot);
@@ -418,7 +419,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.err = ctx->d_err;
     e = cudaMemsetAsync(ctx->d_counter, 0, 2 * sizeof(uint32_t), ctx->stream);
     if (e != cudaSuccess) return e;
-    if (xs && theta && perm) {
+    if (xs && theta) {
         const size_t smem_s = (size_t)RS_WARPS * 2 * RS_KEYS * sizeof(unsigned long long);
         const unsigned blocks = (unsigned)((plan.nq + RS_WARPS - 1) / RS_WARPS);
         rerank_sorted_kernel<<<blocks, RS_WARPS * 32, smem_s, ctx->stream>>>(a);
