@@ -242,6 +242,39 @@ SCRUST_API int32_t scrust_cuda_batch_plan_choice(const scrust_batch_plan* plan, 
                                                  int32_t* precision, float* tuned_ms);
 SCRUST_API void scrust_cuda_batch_plan_destroy(scrust_batch_plan* plan);
 
+/* ---- Query service over a resident atlas (no reference counterpart) ----
+ *
+ * The atlas (host pointer, m x d f32, d <= 61) is uploaded once and stays in
+ * HBM.  Requests of any number of query cells are submitted from any thread
+ * and answered by a scheduler thread that admits them into batches (at most
+ * `max_batch_cells` cells, 0 = 65536) while one of `n_slots` slots (0 = 2)
+ * and the memory budget (`budget_bytes`, 0 = 150 GiB, atlas included) allow;
+ * batches on different slots overlap on the GPU.  Each request gets its k
+ * nearest atlas cells (exact, FP64-equal lists, no self-exclusion) and the
+ * rows of its directed connectivities (smooth_knn sigma/rho and exp weights
+ * per row, columns ascending, no symmetrisation) as a host CSR of q rows by
+ * m columns.  A request's result does not depend on its batch.  Exact
+ * Euclidean only. */
+typedef struct scrust_server scrust_server;
+SCRUST_API scrust_server* scrust_serve_create(int32_t device, const float* atlas, uint64_t m, uint64_t d, uint32_t k,
+                                              const scrust_knn_options* options, uint64_t budget_bytes,
+                                              uint64_t max_batch_cells, uint32_t n_slots, scrust_status* status);
+/* Copies the q x d queries and returns a ticket (0 on error). */
+SCRUST_API uint64_t scrust_serve_submit(scrust_server* server, const float* queries, uint64_t q,
+                                        scrust_status* status);
+/* Blocks until the request is answered; writes q x k ids and distances,
+ * optionally the connectivities CSR (free with scrust_csr_free) and the
+ * submit-to-answer latency.  A ticket is waited for once. */
+SCRUST_API int32_t scrust_serve_wait(scrust_server* server, uint64_t ticket, uint32_t* out_indices,
+                                     float* out_distances, scrust_csr** out_connectivities, double* latency_ms,
+                                     scrust_status* status);
+/* batches, requests answered, most batches on the GPU at once, cells
+ * answered, max batch cells, budget bytes per cell, slots; returns the count
+ * written. */
+SCRUST_API int32_t scrust_serve_stats(scrust_server* server, uint64_t* out, int32_t max_words);
+/* Answers what is pending, then stops the scheduler and frees everything. */
+SCRUST_API void scrust_serve_destroy(scrust_server* server);
+
 /* Phase timing.  When enabled, each kNN / connectivities call records CUDA
  * events on the context stream around its phases; scrust_cuda_phase_times
  * writes the last call's milliseconds (after a synchronise) in the order

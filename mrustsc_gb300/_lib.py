@@ -122,6 +122,14 @@ _SIGNATURES = {
     "scrust_cuda_batch_plan_choice": (ctypes.c_int32, [_P, ctypes.POINTER(ctypes.c_uint32),
                                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float)]),
     "scrust_cuda_batch_plan_destroy": (None, [_P]),
+    "scrust_serve_create": (_P, [ctypes.c_int32, _P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                 ctypes.POINTER(KnnOptions), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                 ctypes.POINTER(Status)]),
+    "scrust_serve_submit": (ctypes.c_uint64, [_P, _P, ctypes.c_uint64, ctypes.POINTER(Status)]),
+    "scrust_serve_wait": (ctypes.c_int32, [_P, ctypes.c_uint64, _P, _P, ctypes.POINTER(_P),
+                                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(Status)]),
+    "scrust_serve_stats": (ctypes.c_int32, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.c_int32]),
+    "scrust_serve_destroy": (None, [_P]),
     "scrust_cuda_version": (ctypes.c_char_p, []),
 }
 

@@ -161,6 +161,47 @@ __global__ void directed_kernel(const uint32_t* __restrict__ idx, const float* _
     }
 }
 
+// Query rows against a reference: the directed weights of each row
+// (directed_kernel's arithmetic, with no self to drop), columns ascending.
+__global__ void query_rows_kernel(const uint32_t* __restrict__ idx, const float* __restrict__ dist, int64_t q, int k,
+                                  const float* __restrict__ sigmas, const float* __restrict__ rhos,
+                                  uint32_t* __restrict__ dcol, float* __restrict__ dw, uint32_t* __restrict__ dcnt) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= q) return;
+    uint32_t* col = dcol + i * k;
+    float* w = dw + i * k;
+    int m = 0;
+    const float sigma = sigmas[i], rho = rhos[i];
+    for (int j = 0; j < k; j++) {
+        const uint32_t nb = idx[i * k + j];
+        const float offset = __fsub_rn(dist[i * k + j], rho);
+        const float wt = (offset <= 0.f || sigma == 0.f) ? 1.0f : expf(__fdiv_rn(-offset, sigma));
+        if (wt == 0.f) continue;
+        int s = m;
+        while (s > 0 && col[s - 1] > nb) {
+            col[s] = col[s - 1];
+            w[s] = w[s - 1];
+            s--;
+        }
+        col[s] = nb;
+        w[s] = wt;
+        m++;
+    }
+    dcnt[i] = (uint32_t)m;
+}
+
+__global__ void query_csr_kernel(const uint32_t* __restrict__ dcol, const float* __restrict__ dw,
+                                 const uint32_t* __restrict__ dcnt, const uint32_t* __restrict__ indptr, int64_t q,
+                                 int k, uint32_t* __restrict__ indices, float* __restrict__ values) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= q) return;
+    const uint32_t o = indptr[i];
+    for (uint32_t t = 0; t < dcnt[i]; ++t) {
+        indices[o + t] = dcol[i * k + t];
+        values[o + t] = dw[i * k + t];
+    }
+}
+
 // ---- stable LSD radix sort (8-bit digits) ---------------------------------
 
 constexpr int RS_THREADS = 256;
@@ -389,6 +430,33 @@ cudaError_t launch_smooth_knn(scrust_context* ctx, const float* dist, int64_t n,
     smooth_knn_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(dist, n, k, target, mean,
                                                                            sigmas, rhos);
     return cudaGetLastError();
+}
+
+int32_t run_query_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t q, int k,
+                                 CsrBuffers* out, scrust_status* st) {
+    cudaError_t e = cudaSuccess;
+    cudaStream_t s = ctx->stream;
+    const int64_t E = q * (int64_t)k;
+    const size_t scan_elems = scan_scratch_elems(q + 1);
+    char* a = (char*)ws_get(ctx, SLOT_CONN_A, sizeof(float) * 2 * (size_t)q + sizeof(uint32_t) * (size_t)(q + 1) + 256, &e);
+    uint32_t* dcol = (uint32_t*)ws_get(ctx, SLOT_CONN_B, sizeof(uint32_t) * (size_t)E, &e);
+    float* dw = (float*)ws_get(ctx, SLOT_CONN_C, sizeof(float) * (size_t)E, &e);
+    uint32_t* scan_scratch = (uint32_t*)ws_get(ctx, SLOT_SCAN, sizeof(uint32_t) * scan_elems, &e);
+    if (!a || !dcol || !dw || !scan_scratch) return cuda_fail(st, e, "query connectivities: workspace");
+    float* sig = (float*)a;
+    float* rho = sig + q;
+    uint32_t* dcnt = (uint32_t*)(rho + q);  // q + 1
+    if ((e = launch_smooth_knn(ctx, dist, q, k, sig, rho)) != cudaSuccess) return cuda_fail(st, e, "smooth_knn");
+    query_rows_kernel<<<(unsigned)((q + 127) / 128), 128, 0, s>>>(idx, dist, q, k, sig, rho, dcol, dw, dcnt);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "query rows");
+    if ((e = cudaMemsetAsync(dcnt + q, 0, sizeof(uint32_t), s)) != cudaSuccess) return cuda_fail(st, e, "memset");
+    if ((e = device_exclusive_scan(ctx, dcnt, out->indptr, q + 1, scan_scratch, scan_elems)) != cudaSuccess)
+        return cuda_fail(st, e, "query row scan");
+    query_csr_kernel<<<(unsigned)((q + 127) / 128), 128, 0, s>>>(dcol, dw, dcnt, out->indptr, q, k, out->indices,
+                                                                out->values);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "query csr");
+    ctx->launches += 5;
+    return ok(st);
 }
 
 int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n, int k,

@@ -252,13 +252,15 @@ struct RowBounds {
 // the end of the candidate pass) as well, no selection is needed.  List rows
 // whose perm entry is 0xffffffff are padding and skipped.  row_lo/row_hi
 // (per input row) confine a batch's solves: ids are reported relative to
-// row_lo and the fallback scans [row_lo, row_hi).
+// row_lo and the fallback scans [row_lo, row_hi).  xr_list: the reference
+// rows by list entry when they are not xs (a query-versus-reference solve).
 cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float* qx,
                           const float* rx, const float* qnorm2, const float* rnorm2,
                           const double* qn64, const double* rn64, const float* qraw,
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
                           const uint32_t* perm, const float* xs, const float* theta, uint32_t* out_idx,
-                          float* out_dist, const uint32_t* row_lo = nullptr, const uint32_t* row_hi = nullptr);
+                          float* out_dist, const uint32_t* row_lo = nullptr, const uint32_t* row_hi = nullptr,
+                          const float* xr_list = nullptr);
 // order.cu: row blocks sorted by decreasing count (stable) into `order`;
 // `scratch` holds work_order_scratch(items) bytes.
 size_t work_order_scratch(int items);
@@ -272,6 +274,11 @@ cudaError_t launch_smooth_knn(scrust_context* ctx, const float* dist, int64_t n,
                               float* sigmas, float* rhos);
 int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n,
                            int k, bool validate, CsrBuffers* out, scrust_status* st);
+// Rows of the directed fuzzy set of query rows against a reference (no
+// symmetrisation, no self to drop): sigma/rho per row as smooth_knn, then
+// exp weights, zero weights dropped, columns ascending, as a CSR of q rows.
+int32_t run_query_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t q, int k,
+                                 CsrBuffers* out, scrust_status* st);
 
 // Device-wide primitives (conn.cu).
 cudaError_t device_exclusive_scan(scrust_context* ctx, const uint32_t* in, uint32_t* out, int64_t n,

@@ -40,6 +40,7 @@ struct RerankArgs {
     Lists lists;
     const uint32_t* perm;  // list row / list entry -> input row, or null
     const float* xs;       // working rows in list order (ordered solves), or null
+    const float* xr_list;  // reference rows indexed by list entry (xs for a self solve)
     const uint32_t* row_lo;  // per input row: first row of its solve (a batch of solves), or null
     const uint32_t* row_hi;  // per input row: end of its solve
     const float* theta;    // per list: its threshold when the candidate pass ended, or null
@@ -248,7 +249,7 @@ __global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs
             if (keep) {
                 const int pos = m + __popc(ballot & lanemask_lt());
                 if (pos < RS_KEYS) {
-                    const float r = dist2_f32(xq, a.xs + (int64_t)id * a.d, a.d);
+                    const float r = dist2_f32(xq, a.xr_list + (int64_t)id * a.d, a.d);
                     keys[pos] = ((unsigned long long)float_key(r) << 32) | (uint32_t)input_row(a, id);
                 }
             }
@@ -379,7 +380,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
                           const double* qn64, const double* rn64, const float* qraw,
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
                           const uint32_t* perm, const float* xs, const float* theta, uint32_t* out_idx,
-                          float* out_dist, const uint32_t* row_lo, const uint32_t* row_hi) {
+                          float* out_dist, const uint32_t* row_lo, const uint32_t* row_hi, const float* xr_list) {
     cudaError_t e;
     uint32_t* fb_rows = (uint32_t*)ws_get(ctx, SLOT_FALLBACK_ROWS, sizeof(uint32_t) * (size_t)plan.nq, &e);
     if (!fb_rows) return e;
@@ -399,6 +400,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.lists = lists;
     a.perm = perm;
     a.xs = xs;
+    a.xr_list = xr_list ? xr_list : xs;
     a.theta = theta;
     a.row_lo = row_lo;
     a.row_hi = row_hi;

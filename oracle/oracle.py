@@ -218,3 +218,21 @@ def exact_knn_numpy(x, k: int):
         order = sorted((j for j in range(n) if j != cell), key=lambda j: (d[cell, j], j))
         indices[cell] = order[:k]
     return indices, np.take_along_axis(d, indices, 1)
+
+
+def knn_fp64_cross(queries, reference, k: int):
+    """Exact k nearest reference rows of every query row in FP64 (difference
+    form, lowest reference index on ties, no self-exclusion): the semantics of
+    tests/test_neighbors_audit.py:52-61 for a query-versus-reference solve.
+    numpy; returns (indices, FP64 distances)."""
+    q64 = np.asarray(queries, dtype=np.float64)
+    r64 = np.asarray(reference, dtype=np.float64)
+    idx = np.zeros((len(q64), k), dtype=np.int64)
+    dist = np.zeros((len(q64), k), dtype=np.float64)
+    for b in range(0, len(q64), 256):
+        qb = q64[b:b + 256]
+        d2 = ((qb[:, None, :] - r64[None, :, :]) ** 2).sum(-1)
+        order = np.lexsort((np.broadcast_to(np.arange(len(r64)), d2.shape), d2), axis=1)[:, :k]
+        idx[b:b + 256] = order
+        dist[b:b + 256] = np.sqrt(np.take_along_axis(d2, order, 1))
+    return idx, dist
