@@ -304,7 +304,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
         // own, and the rerank needs no selection.
         scrust_knn_options lo = o;
         if (order_rows || o.segments == 0) lo.segments = 1;
-        const bool keep_theta = lo.segments == 1;
+
         RowOrder order;
         if (order_rows) {
             int32_t rc = build_row_order(ctx, xwork, n, d, means, max_bits, cosine, bf16, A16, B16, bA, beps, bdelta,
@@ -355,15 +355,20 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
                 return cuda_fail(st, e, "knn_candidates_tc");
             ctx->launches += 2;
         } else {
-            float* theta = nullptr;
-            if (keep_theta) {
-                theta = (float*)ws_get(ctx, SLOT_THETA, sizeof(float) * 2 * (size_t)n_pad, &e);
-                if (!theta) return cuda_fail(st, e, "workspace");
-                rerank_xs = xwork;
-                rerank_theta = theta;
+            // Every list keeps its threshold, so the rerank needs no selection.
+            float* theta = (float*)ws_get(ctx, SLOT_THETA, sizeof(float) * (size_t)lists.segments * n_pad, &e);
+            if (!theta) return cuda_fail(st, e, "workspace");
+            rerank_xs = xwork;
+            rerank_theta = theta;
+            TileLists shared;  // several column segments share each row's threshold
+            if (lists.segments > 2) {
+                shared.row_theta = (uint32_t*)ws_get(ctx, SLOT_ROWTHETA, sizeof(uint32_t) * (size_t)n_pad, &e);
+                if (!shared.row_theta) return cuda_fail(st, e, "workspace");
+                if ((e = cudaMemsetAsync(shared.row_theta, 0xff, sizeof(uint32_t) * (size_t)n_pad, s)) != cudaSuccess)
+                    return cuda_fail(st, e, "memset");
             }
             if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                              nullptr, false, theta, nullptr, ctx->d_stats)) != cudaSuccess)
+                                              &shared, false, theta, nullptr, ctx->d_stats)) != cudaSuccess)
                 return cuda_fail(st, e, "knn_candidates_tc");
             ctx->launches += 1;
         }
@@ -411,7 +416,6 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
     if ((e = launch_rerank(ctx, plan, xr, xr, norm2, norm2, norm64, norm64, x, x, bounds, lists, perm, rerank_xs,
                            rerank_theta, out_idx, out_dist)) != cudaSuccess)
         return cuda_fail(st, e, "knn_rerank");
-    ctx->launches += 2;
     mark(ctx, PH_RERANK);
     return ok(st);
 }

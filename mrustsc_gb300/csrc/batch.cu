@@ -205,7 +205,7 @@ int32_t batch_enqueue(scrust_context* ctx, const float* x, const void* table, ui
     if ((e = launch_rerank(ctx, plan, xwork, xwork, norm2, norm2, norm64, norm64, x, x, bounds, lists, row_map, xs, theta,
                            out_idx, out_dist, row_lo, row_hi)) != cudaSuccess)
         return cuda_fail(st, e, "batch: knn_rerank");
-    ctx->launches += 3;
+    ctx->launches += 1;  // the row gather (the rerank counts its own)
     mark(ctx, PH_RERANK);
     return ok(st);
 }

@@ -54,6 +54,8 @@ enum Slot : int {
     SLOT_BATCH,         // batch layout maps, work order, thresholds
     SLOT_BATCH_TABLE,   // batch sample table
     SLOT_THETA,         // list thresholds of an unordered tensor-form solve
+    SLOT_ROWTHETA,      // per-row shared thresholds across column segments
+    SLOT_RERANK_BIG,    // rows for the rerank's second sorted pass
     SLOT_COUNT
 };
 
@@ -224,6 +226,9 @@ struct TileLists {
     // sweeps (a batch of independent solves laid out block-diagonally), or null.
     const uint2* range = nullptr;
     const uint32_t* row_map = nullptr;  // query row -> input row, 0xffffffff for padding; null: identity
+    // Per query row, the smallest threshold of any of its lists (float_key,
+    // initialised to 0xffffffff), shared by the column segments; or null.
+    uint32_t* row_theta = nullptr;
 };
 // One pass of the tensor sweep.  `tiles` null: every column tile, outward
 // from the diagonal.  `resume`: lists and thresholds continue from an earlier

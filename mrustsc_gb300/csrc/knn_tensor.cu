@@ -81,6 +81,8 @@ struct TensorArgs {
     int tl_stride;
     const uint32_t* item_order; // items by decreasing work, dealt out in a snake, or null: round robin
     const uint2* item_range;    // per item its column tiles [x, y) (one column segment), or null
+    uint32_t* row_theta;        // per query row the smallest threshold any of its lists reached
+                                // (float_key; 0xffffffff = none), shared across column segments; or null
     const uint32_t* row_map;    // per query row its input row, 0xffffffff for padding; null: all rows real
     // k = 1 without lists: per (row, part) the smallest MMA value and its
     // column, packed as float_key << 32 | column; null otherwise.
@@ -563,9 +565,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
                 if (a.stats) c_wait += clock64() - w0;
                 tc_fence_after();
-                // The partner part's threshold bounds this row just as well.
+                // The partner part's threshold bounds this row just as well,
+                // and so does any other column segment's (through HBM).
                 const unsigned long long o = *other_th;
                 if ((o & 0xffffffff00000000ull) == tag) th = fminf(th, __uint_as_float((uint32_t)o));
+                if (a.row_theta && valid) th = fminf(th, key_float(a.row_theta[row]));
                 const int64_t col0 = (int64_t)ct * TBN + part * kPartCols;
                 const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(h * TBN + part * kPartCols);
                 const uint32_t before = cnt;
@@ -647,7 +651,10 @@ __global__ void __launch_bounds__(THREADS, 1)
                     }
                     if (a.stats) c_prune += clock64() - p0;
                 }
-                if (__any_sync(0xffffffffu, th != th_before)) *my_th = tag | __float_as_uint(th);
+                if (__any_sync(0xffffffffu, th != th_before)) {
+                    *my_th = tag | __float_as_uint(th);
+                    if (a.row_theta && valid && th < th_before) atomicMin(a.row_theta + row, float_key(th));
+                }
                 tc++;
             }
             // A last prune keeps every finished list short enough for the
@@ -888,6 +895,7 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.item_order = nullptr;
     a.item_range = tiles ? tiles->range : nullptr;
     a.row_map = tiles ? tiles->row_map : nullptr;
+    a.row_theta = tiles ? tiles->row_theta : nullptr;
     if (tiles && !tiles->tiles) a.item_order = tiles->order;
     if (a.item_range && lists.segments != PARTS) return cudaErrorInvalidValue;
     if (tiles && tiles->tiles) {

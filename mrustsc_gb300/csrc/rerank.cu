@@ -52,6 +52,9 @@ struct RerankArgs {
     uint32_t* fb_rows;
     uint32_t* fb_count;
     uint32_t* fb_next;
+    uint32_t* big_rows;   // rows with many survivors, for the second sorted pass
+    uint32_t* big_count;
+    uint32_t* big_next;
     float* fb_scratch;
     int* err;
 };
@@ -208,23 +211,21 @@ __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a
 // list row keeps the entries below the smaller of its lists' thresholds,
 // measures them on the working rows laid out in list order (for an ordered
 // solve neighbouring rows share candidates, which stay in cache), and
-// finishes as above with input ids.  More than RS_KEYS survivors go to the
-// fallback.
+// finishes as above with input ids.  A row with more than RS_KEYS survivors
+// (many cells inside the bound of the k-th, as for queries off the data's
+// manifold in high dimension) is finished by a second pass with room for
+// RS_BIG_KEYS; beyond that, by the fallback.
 constexpr int RS_WARPS = 8;
 constexpr int RS_KEYS = 256;
-__global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs a) {
-    extern __shared__ unsigned long long rs_smem[];
-    const int warp = threadIdx.x >> 5;
+constexpr int RS_BIG_WARPS = 4;
+constexpr int RS_BIG_KEYS = 2048;
+
+// 0: done; 1: more than `cap` survivors; 2: needs the fallback.
+template <int CAP>
+__device__ int sorted_row(const RerankArgs& a, int64_t slot, unsigned long long* keys, double* dbl) {
     const int lane = threadIdx.x & 31;
-    unsigned long long* keys = rs_smem + (size_t)warp * 2 * RS_KEYS;
-    double* dbl = reinterpret_cast<double*>(keys + RS_KEYS);
-    const int64_t slot = (int64_t)blockIdx.x * RS_WARPS + warp;
-    if (slot >= a.nq || (a.perm && a.perm[slot] == 0xffffffffu)) return;  // padding of a batch layout
     WarpTeam team;
-    if (a.lists.overflow[slot]) {
-        if (lane == 0) push_fallback(a, slot);
-        return;
-    }
+    if (a.lists.overflow[slot]) return 2;
     const int segs = a.lists.segments;
     float theta = __int_as_float(0x7f800000);
     for (int l = 0; l < segs; ++l) theta = fminf(theta, a.theta[slot * segs + l]);
@@ -248,7 +249,7 @@ __global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs
             const uint32_t ballot = __ballot_sync(0xffffffffu, keep);
             if (keep) {
                 const int pos = m + __popc(ballot & lanemask_lt());
-                if (pos < RS_KEYS) {
+                if (pos < CAP) {
                     const float r = dist2_f32(xq, a.xr_list + (int64_t)id * a.d, a.d);
                     keys[pos] = ((unsigned long long)float_key(r) << 32) | (uint32_t)input_row(a, id);
                 }
@@ -256,16 +257,53 @@ __global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs
             m += __popc(ballot);
         }
     }
-    if (m > RS_KEYS || m < a.k) {
-        if (lane == 0) push_fallback(a, slot);
-        return;
-    }
+    if (m < a.k) return 2;
+    if (m > CAP) return 1;
     __syncwarp();
     const int P = next_pow2(m);
     for (int p = m + lane; p < P; p += 32) keys[p] = ~0ull;
     __syncwarp();
     team_bitonic_sort(team, keys, P);
     finalize_row(team, a, input_row(a, slot), keys, m, dbl);
+    return 0;
+}
+
+__global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs a) {
+    extern __shared__ unsigned long long rs_smem[];
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    unsigned long long* keys = rs_smem + (size_t)warp * 2 * RS_KEYS;
+    double* dbl = reinterpret_cast<double*>(keys + RS_KEYS);
+    const int64_t slot = (int64_t)blockIdx.x * RS_WARPS + warp;
+    if (slot >= a.nq || (a.perm && a.perm[slot] == 0xffffffffu)) return;  // padding of a batch layout
+    const int r = sorted_row<RS_KEYS>(a, slot, keys, dbl);
+    if (r && lane == 0) {
+        if (r == 1) {
+            a.big_rows[atomicAdd(a.big_count, 1u)] = (uint32_t)slot;
+        } else {
+            push_fallback(a, slot);
+        }
+    }
+}
+
+// The rows with more survivors than the first pass holds: warps take them
+// from a queue.
+__global__ void __launch_bounds__(RS_BIG_WARPS * 32) rerank_sorted_big_kernel(RerankArgs a) {
+    extern __shared__ unsigned long long rb_smem[];
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    unsigned long long* keys = rb_smem + (size_t)warp * 2 * RS_BIG_KEYS;
+    double* dbl = reinterpret_cast<double*>(keys + RS_BIG_KEYS);
+    for (;;) {
+        uint32_t i = 0;
+        if (lane == 0) i = atomicAdd(a.big_next, 1u);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= *a.big_count) break;
+        const int64_t slot = a.big_rows[i];
+        const int r = sorted_row<RS_BIG_KEYS>(a, slot, keys, dbl);
+        if (r && lane == 0) push_fallback(a, slot);
+        __syncwarp();
+    }
 }
 
 // One block per row, over every reference row: used for rows whose
@@ -417,26 +455,40 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.fb_rows = fb_rows;
     a.fb_count = ctx->d_counter;
     a.fb_next = ctx->d_counter + 1;
+    a.big_count = ctx->d_counter + 2;
+    a.big_next = ctx->d_counter + 3;
+    a.big_rows = nullptr;
+    if (xs && theta) {
+        a.big_rows = (uint32_t*)ws_get(ctx, SLOT_RERANK_BIG, sizeof(uint32_t) * (size_t)plan.nq, &e);
+        if (!a.big_rows) return e;
+    }
     a.fb_scratch = fb_scratch;
     a.err = ctx->d_err;
-    e = cudaMemsetAsync(ctx->d_counter, 0, 2 * sizeof(uint32_t), ctx->stream);
+    e = cudaMemsetAsync(ctx->d_counter, 0, 4 * sizeof(uint32_t), ctx->stream);
     if (e != cudaSuccess) return e;
     if (xs && theta) {
         const size_t smem_s = (size_t)RS_WARPS * 2 * RS_KEYS * sizeof(unsigned long long);
         const unsigned blocks = (unsigned)((plan.nq + RS_WARPS - 1) / RS_WARPS);
         rerank_sorted_kernel<<<blocks, RS_WARPS * 32, smem_s, ctx->stream>>>(a);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        const size_t smem_b = (size_t)RS_BIG_WARPS * 2 * RS_BIG_KEYS * sizeof(unsigned long long);
+        if ((e = set_smem_limit(ctx, (const void*)rerank_sorted_big_kernel, (int)smem_b)) != cudaSuccess) return e;
+        rerank_sorted_big_kernel<<<2 * ctx->sm_count, RS_BIG_WARPS * 32, smem_b, ctx->stream>>>(a);
+        ctx->launches += 2;
     } else {
         const size_t smem_w = (size_t)RR_WARPS * 2 * RC * sizeof(unsigned long long);
         e = set_smem_limit(ctx, (const void*)rerank_warp_kernel, (int)smem_w);
         if (e != cudaSuccess) return e;
         const unsigned blocks = (unsigned)((plan.nq + RR_WARPS - 1) / RR_WARPS);
         rerank_warp_kernel<<<blocks, RR_WARPS * 32, smem_w, ctx->stream>>>(a);
+        ctx->launches += 1;
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const size_t smem_f = (size_t)FB_CAP * (sizeof(unsigned long long) + sizeof(double));
     e = set_smem_limit(ctx, (const void*)rerank_fallback_kernel, (int)smem_f);
     if (e != cudaSuccess) return e;
     rerank_fallback_kernel<<<FB_BLOCKS, FB_THREADS, smem_f, ctx->stream>>>(a);
+    ctx->launches += 1;
     return cudaGetLastError();
 }
 

@@ -153,8 +153,14 @@ int32_t cross_enqueue(scrust_server* sv, scrust_context* ctx, const float* dq, i
     plan.segments = lists.segments;
     float* theta = (float*)ws_get(ctx, SLOT_THETA, sizeof(float) * (size_t)q_pad * lists.segments, &e);
     if (!theta) return cuda_fail(st, e, "serve: workspace");
+    uint32_t* row_theta = (uint32_t*)ws_get(ctx, SLOT_ROWTHETA, sizeof(uint32_t) * (size_t)q_pad, &e);
+    if (!row_theta) return cuda_fail(st, e, "serve: workspace");
+    if ((e = cudaMemsetAsync(row_theta, 0xff, sizeof(uint32_t) * (size_t)q_pad, s)) != cudaSuccess)
+        return cuda_fail(st, e, "serve: memset");
+    TileLists shared;  // the column segments of a row share its threshold
+    shared.row_theta = row_theta;
     if ((e = launch_tensor_candidates(ctx, plan, A16, q_pad, sv->B16, sv->m_pad, bA, bdelta, beps2, lists, sv->bf16,
-                                      nullptr, false, theta, nullptr, nullptr)) != cudaSuccess)
+                                      &shared, false, theta, nullptr, nullptr)) != cudaSuccess)
         return cuda_fail(st, e, "serve: knn_candidates_tc");
     RowBounds bounds;
     bounds.A = bA;
@@ -163,7 +169,7 @@ int32_t cross_enqueue(scrust_server* sv, scrust_context* ctx, const float* dq, i
     if ((e = launch_rerank(ctx, plan, dq, sv->atlas, nullptr, nullptr, nullptr, nullptr, dq, sv->atlas, bounds, lists,
                            nullptr, dq, theta, d_idx, d_dist, nullptr, nullptr, sv->atlas)) != cudaSuccess)
         return cuda_fail(st, e, "serve: knn_rerank");
-    ctx->launches += 7;
+    ctx->launches += 3;  // operands, bounds, candidates (the rerank counts its own)
     return run_query_connectivities(ctx, d_idx, d_dist, q, k, csr, st);
 }
 
