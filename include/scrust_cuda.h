@@ -208,6 +208,15 @@ SCRUST_API int32_t scrust_cuda_smooth_knn_distances_noalloc(const float* distanc
                                                             float* sigmas, float* rhos, void* stream,
                                                             scrust_status* status);
 
+/* Row-range solve for a sharded graph build: the k nearest rows of x (n x d,
+ * device) for each row in [row_begin, row_end), self excluded, ids global.
+ * Outputs are (row_end - row_begin) x k.  Tensor form, exact Euclidean, d at
+ * most 61.  The rows' union over shards equals scrust_cuda_knn_device. */
+SCRUST_API int32_t scrust_cuda_knn_rows_device(scrust_context* context, const float* embedding, uint64_t n,
+                                               uint64_t d, uint32_t k, uint64_t row_begin, uint64_t row_end,
+                                               const scrust_knn_options* options, uint32_t* out_indices,
+                                               float* out_distances, scrust_status* status);
+
 /* ---- Batches of independent samples (no reference counterpart) ----
  *
  * `n_samples` independent self-kNN solves in one tensor-form sweep.  The

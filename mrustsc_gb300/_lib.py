@@ -130,6 +130,9 @@ _SIGNATURES = {
                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(Status)]),
     "scrust_serve_stats": (ctypes.c_int32, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.c_int32]),
     "scrust_serve_destroy": (None, [_P]),
+    "scrust_cuda_knn_rows_device": (ctypes.c_int32, [_P, _P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                                      ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(KnnOptions),
+                                                      _P, _P, ctypes.POINTER(Status)]),
     "scrust_cuda_version": (ctypes.c_char_p, []),
 }
 

@@ -56,6 +56,8 @@ enum Slot : int {
     SLOT_THETA,         // list thresholds of an unordered tensor-form solve
     SLOT_ROWTHETA,      // per-row shared thresholds across column segments
     SLOT_RERANK_BIG,    // rows for the rerank's second sorted pass
+    SLOT_QTERMS,        // per-query-row bound terms of a query-versus-reference solve
+    SLOT_QSCRATCH,      // scratch operands of a query-versus-reference solve
     SLOT_COUNT
 };
 
@@ -129,7 +131,8 @@ void* ws_get(scrust_context* ctx, Slot slot, size_t bytes, cudaError_t* err);
 struct KnnPlan {
     int64_t nq = 0, nr = 0;   // query rows, reference rows (equal for self-kNN)
     int d = 0, k = 0;
-    bool self = true;         // query i is reference i (exclude it)
+    bool self = true;         // query i is reference i + self_offset (exclude it)
+    int64_t self_offset = 0;
     int form = SCRUST_FORM_PLAIN;
     int metric = SCRUST_METRIC_EUCLIDEAN;
     int mode = SCRUST_MODE_EXACT;
@@ -293,6 +296,26 @@ int radix_blocks(int64_t n);
 cudaError_t radix_sort_pairs(scrust_context* ctx, uint32_t* kA, unsigned long long* vA, uint32_t* kB,
                              unsigned long long* vB, int64_t n, int bits, uint32_t* hist, uint32_t* scan_scratch,
                              size_t scan_elems, uint32_t** keys_out, unsigned long long** vals_out);
+
+// A reference set prepared for query-versus-reference solves (cross.cu):
+// its rows, centring means, tensor operands B and the words max centred
+// norm, max quantisation radius, max |b_hat| that fix the scale and bounds.
+struct Reference {
+    const float* rows = nullptr;
+    int64_t n = 0, n_pad = 0;
+    int d = 0;
+    const double* means = nullptr;
+    const uint32_t* words = nullptr;
+    const void* B16 = nullptr;
+    bool bf16 = false;
+};
+// Prepares x (n x d, device) as a reference in this context's workspace.
+int32_t reference_prepare(scrust_context* ctx, const float* x, int64_t n, int d, bool bf16, Reference* out,
+                          scrust_status* st);
+// k nearest reference rows of q query rows (device), exact; self_offset >= 0
+// marks query i as reference row i + self_offset (excluded).  Outputs q x k.
+int32_t cross_knn_enqueue(scrust_context* ctx, const Reference& ref, const float* dq, int64_t q, int k,
+                          int64_t self_offset, uint32_t* d_idx, float* d_dist, scrust_status* st);
 
 // Tensor-map encoding through the driver entry point.
 bool encode_2d(scrust_context* ctx, CUtensorMap* map, CUtensorMapDataType dtype, void* base,

@@ -67,6 +67,7 @@ struct TensorArgs {
     int64_t nq, nr;
     int k;
     int self;
+    int64_t self_offset;  // query row i is column i + self_offset
     int col_tiles;
     int tiles_per_seg;
     int items;
@@ -207,7 +208,7 @@ __device__ __forceinline__ void test_chunk(const uint32_t (&v)[32], int64_t colb
                                            const TensorArgs& a, uint32_t* ids, float* vals, uint32_t& cnt) {
     const float m = min32(v);
     if (__any_sync(0xffffffffu, m < th))
-        append_chunk(v, colbase, th, chunk_valid(colbase, a.nr, a.self != 0, row), ids, vals, cnt);
+        append_chunk(v, colbase, th, chunk_valid(colbase, a.nr, a.self != 0, row + a.self_offset), ids, vals, cnt);
 }
 
 // The K smallest values a lane has met (k <= K), ascending, in registers.
@@ -258,7 +259,7 @@ __device__ __forceinline__ float topk_chunk(const uint32_t (&v)[32], int64_t col
     if constexpr (K == 1) {
         // The chunk minimum is the only candidate; its column is kept too.
         if (__any_sync(0xffffffffu, m < top.v[0])) {
-            const uint32_t valid = chunk_valid(colbase, a.nr, a.self != 0, row);
+            const uint32_t valid = chunk_valid(colbase, a.nr, a.self != 0, row + a.self_offset);
             float mv = m;
             if (valid != 0xffffffffu) {
                 mv = __int_as_float(0x7f800000);
@@ -283,7 +284,7 @@ __device__ __forceinline__ float topk_chunk(const uint32_t (&v)[32], int64_t col
         uint32_t want = 0;
 #pragma unroll
         for (int j = 0; j < 32; j++) want |= (f_of(v[j]) < lim) ? (1u << j) : 0u;
-        want &= chunk_valid(colbase, a.nr, a.self != 0, row);
+        want &= chunk_valid(colbase, a.nr, a.self != 0, row + a.self_offset);
         if (want) {
             const float old = top.kth(a.k);
             while (want) {
@@ -611,7 +612,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             tmem_ld32(tbase + 32 * c, va);
                             tmem_ld_wait(va);
                             append_chunk(va, col0 + 32 * c, th,
-                                         chunk_valid(col0 + 32 * c, a.nr, a.self != 0, row), ids, vals, cnt);
+                                         chunk_valid(col0 + 32 * c, a.nr, a.self != 0, row + a.self_offset), ids, vals, cnt);
                         }
                     }
                 } else {
@@ -876,6 +877,7 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.nr = plan.nr;
     a.k = plan.k;
     a.self = plan.self ? 1 : 0;
+    a.self_offset = plan.self_offset;
     a.col_tiles = (int)(nr_pad / TBN);
     const int col_segs = lists.segments / PARTS;
     a.tiles_per_seg = (a.col_tiles + col_segs - 1) / col_segs;

@@ -46,6 +46,7 @@ struct RerankArgs {
     const float* theta;    // per list: its threshold when the candidate pass ended, or null
     int64_t nq, nr;
     int d, k, mode, metric, self;
+    int64_t self_offset;  // query row q is reference row q + self_offset
     float gamma;
     uint32_t* out_idx;
     float* out_dist;
@@ -334,7 +335,7 @@ __global__ void __launch_bounds__(FB_THREADS) rerank_fallback_kernel(RerankArgs 
         // The columns of the row's own solve: [lo, hi) of the input rows.
         const int64_t lo = a.row_lo ? (int64_t)a.row_lo[q] : 0, hi = a.row_lo ? (int64_t)a.row_hi[q] : a.nr;
         for (int64_t j = tid; j < a.nr; j += blockDim.x)
-            sc[j] = (a.self && j == q) || j < lo || j >= hi ? __int_as_float(0x7f800000) : compute_r(a, q, (uint32_t)j);
+            sc[j] = (a.self && j == q + a.self_offset) || j < lo || j >= hi ? __int_as_float(0x7f800000) : compute_r(a, q, (uint32_t)j);
         __syncthreads();
         // k-th smallest of the row: four 8-bit radix passes.
         if (tid == 0) {
@@ -449,6 +450,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.mode = plan.mode;
     a.metric = plan.metric;
     a.self = plan.self ? 1 : 0;
+    a.self_offset = plan.self_offset;
     a.gamma = dist2_f32_gamma(plan.d);
     a.out_idx = out_idx;
     a.out_dist = out_dist;

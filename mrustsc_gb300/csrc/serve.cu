@@ -114,63 +114,18 @@ size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 // Query rows of one batch against the atlas, on the slot's stream.
 int32_t cross_enqueue(scrust_server* sv, scrust_context* ctx, const float* dq, int64_t q, uint32_t* d_idx,
                       float* d_dist, CsrBuffers* csr, scrust_status* st) {
-    cudaStream_t s = ctx->stream;
-    cudaError_t e = cudaSuccess;
-    const int d = sv->d, k = sv->k;
-    const int64_t q_pad = (int64_t)round_up((size_t)q, 256);
-    void* A16 = ws_get(ctx, SLOT_A16, (size_t)q_pad * 128, &e);
-    void* B16 = ws_get(ctx, SLOT_B16, (size_t)q_pad * 128, &e);
-    float* rb = (float*)ws_get(ctx, SLOT_QERR, sizeof(float) * 4 * (size_t)q_pad + 64, &e);
-    if (!A16 || !B16 || !rb) return cuda_fail(st, e, "serve: workspace");
-    float *bA = rb, *eps = rb + q_pad, *bdelta = rb + 2 * q_pad, *beps2 = rb + 3 * q_pad;
-    uint32_t* scratch_words = (uint32_t*)(rb + 4 * q_pad);
-    if ((e = launch_tensor_operands(dq, q, q_pad, d, sv->means, sv->words, false, sv->bf16, nullptr, A16, B16, bA, eps,
-                                    scratch_words, scratch_words + 1, s)) != cudaSuccess ||
-        (e = launch_tensor_bounds(q, bA, eps, sv->words + 1, sv->words + 2, bdelta, beps2, s)) != cudaSuccess)
-        return cuda_fail(st, e, "serve: query operands");
-    // Column segments so that small batches still fill the GPU; every list
-    // keeps its threshold and the rerank takes the smallest.
-    const int items = (int)(q_pad / 256), col_tiles = (int)(sv->m_pad / 256);
-    int csegs = std::max(1, std::min((2 * ctx->sm_count + items - 1) / items, std::min(col_tiles, 16)));
-    const int per = (col_tiles + csegs - 1) / csegs;
-    csegs = (col_tiles + per - 1) / per;
-    KnnPlan plan;
-    plan.nq = q;
-    plan.nr = (int64_t)sv->m;
-    plan.d = d;
-    plan.k = k;
-    plan.self = false;
-    plan.form = SCRUST_FORM_TENSOR;
-    plan.precision = sv->opts.precision;
-    Lists lists;
-    lists.cap = std::max(64, (2 * k + 32 + 31) / 32 * 32);
-    lists.ctot = lists.cap + 128;
-    lists.segments = 2 * csegs;
-    int32_t rc = alloc_lists(ctx, q_pad, &lists, st);
+    Reference ref;
+    ref.rows = sv->atlas;
+    ref.n = (int64_t)sv->m;
+    ref.n_pad = sv->m_pad;
+    ref.d = sv->d;
+    ref.means = sv->means;
+    ref.words = sv->words;
+    ref.B16 = sv->B16;
+    ref.bf16 = sv->bf16;
+    int32_t rc = cross_knn_enqueue(ctx, ref, dq, q, sv->k, -1, d_idx, d_dist, st);
     if (rc) return rc;
-    plan.cap = lists.cap;
-    plan.ctot = lists.ctot;
-    plan.segments = lists.segments;
-    float* theta = (float*)ws_get(ctx, SLOT_THETA, sizeof(float) * (size_t)q_pad * lists.segments, &e);
-    if (!theta) return cuda_fail(st, e, "serve: workspace");
-    uint32_t* row_theta = (uint32_t*)ws_get(ctx, SLOT_ROWTHETA, sizeof(uint32_t) * (size_t)q_pad, &e);
-    if (!row_theta) return cuda_fail(st, e, "serve: workspace");
-    if ((e = cudaMemsetAsync(row_theta, 0xff, sizeof(uint32_t) * (size_t)q_pad, s)) != cudaSuccess)
-        return cuda_fail(st, e, "serve: memset");
-    TileLists shared;  // the column segments of a row share its threshold
-    shared.row_theta = row_theta;
-    if ((e = launch_tensor_candidates(ctx, plan, A16, q_pad, sv->B16, sv->m_pad, bA, bdelta, beps2, lists, sv->bf16,
-                                      &shared, false, theta, nullptr, nullptr)) != cudaSuccess)
-        return cuda_fail(st, e, "serve: knn_candidates_tc");
-    RowBounds bounds;
-    bounds.A = bA;
-    bounds.delta = bdelta;
-    bounds.eps2 = beps2;
-    if ((e = launch_rerank(ctx, plan, dq, sv->atlas, nullptr, nullptr, nullptr, nullptr, dq, sv->atlas, bounds, lists,
-                           nullptr, dq, theta, d_idx, d_dist, nullptr, nullptr, sv->atlas)) != cudaSuccess)
-        return cuda_fail(st, e, "serve: knn_rerank");
-    ctx->launches += 3;  // operands, bounds, candidates (the rerank counts its own)
-    return run_query_connectivities(ctx, d_idx, d_dist, q, k, csr, st);
+    return run_query_connectivities(ctx, d_idx, d_dist, q, sv->k, csr, st);
 }
 
 bool grow_csr(CsrBuffers* b, uint64_t rows, uint64_t nnz) {
