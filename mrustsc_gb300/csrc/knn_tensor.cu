@@ -238,7 +238,45 @@ struct TopK {
         for (int j = 1; j < K; j++) r = (j == k - 1) ? v[j] : r;
         return r;
     }
+    // Merges 32 ascending values in: the K smallest of both, ascending (the
+    // elementwise minimum against the reversed run is bitonic; a bitonic
+    // clean-up sorts it).
+    __device__ __forceinline__ void merge_sorted(const float (&x)[32]) {
+        static_assert(K <= 32, "merge_sorted holds at most 32 values");
+#pragma unroll
+        for (int i = 0; i < K; i++) v[i] = fminf(v[i], x[K - 1 - i]);
+#pragma unroll
+        for (int stride = K >> 1; stride > 0; stride >>= 1)
+#pragma unroll
+            for (int i = 0; i < K; i++) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const float lo = fminf(v[i], v[j]), hi = fmaxf(v[i], v[j]);
+                    v[i] = lo;
+                    v[j] = hi;
+                }
+            }
+    }
 };
+
+// Ascending bitonic sort of 32 values held in registers (fully unrolled,
+// static indices).
+__device__ __forceinline__ void sort32(float (&x)[32]) {
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1)
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1)
+#pragma unroll
+            for (int i = 0; i < 32; i++) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const bool up = (i & size) == 0;
+                    const float lo = fminf(x[i], x[j]), hi = fmaxf(x[i], x[j]);
+                    x[i] = up ? lo : hi;
+                    x[j] = up ? hi : lo;
+                }
+            }
+}
 
 __device__ __forceinline__ float pick32(const uint32_t (&v)[32], int j) {
     float x = f_of(v[0]);
@@ -281,21 +319,31 @@ __device__ __forceinline__ float topk_chunk(const uint32_t (&v)[32], int64_t col
     }
     if (__any_sync(0xffffffffu, m < top.v[K - 1])) {
         const float lim = top.v[K - 1];
+        const uint32_t valid = chunk_valid(colbase, a.nr, a.self != 0, row + a.self_offset);
         uint32_t want = 0;
 #pragma unroll
         for (int j = 0; j < 32; j++) want |= (f_of(v[j]) < lim) ? (1u << j) : 0u;
-        want &= chunk_valid(colbase, a.nr, a.self != 0, row + a.self_offset);
-        if (want) {
-            const float old = top.kth(a.k);
+        want &= valid;
+        const float old = top.kth(a.k);
+        // Many entrants in some lane (the first chunks of a row block): sort
+        // the chunk and merge it in, with the warp converged; few: insert
+        // them one by one.
+        if (__reduce_max_sync(0xffffffffu, (uint32_t)__popc(want)) >= 6u) {
+            float x[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++) x[j] = ((valid >> j) & 1u) ? f_of(v[j]) : __int_as_float(0x7f800000);
+            sort32(x);
+            top.merge_sorted(x);
+        } else if (want) {
             while (want) {
                 const int j = __ffs(want) - 1;
                 want &= want - 1;
                 const float x = pick32(v, j);
                 if (x < top.v[K - 1]) top.insert(x);
             }
-            const float kth = top.kth(a.k);
-            if (kth < old) th = fminf(th, bnd.theta_f32(kth));
         }
+        const float kth = top.kth(a.k);
+        if (kth < old) th = fminf(th, bnd.theta_f32(kth));
     }
     return m;
 }
