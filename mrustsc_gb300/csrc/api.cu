@@ -343,17 +343,34 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
             first.count = order.prio_cnt;
             first.stride = kPrioMax;
             first.order = order.prio_order;
+            // k <= 32: both passes only tighten the thresholds; two collect
+            // passes over the same tiles then append just the columns below
+            // the final thresholds.  Larger k: the passes keep lists.
+            const bool split = k <= 32;
+            const int mode = split ? kPassThresholds : kPassFull;
             if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                              &first, false, order.theta, nullptr, ctx->d_stats)) != cudaSuccess)
+                                              &first, false, order.theta, nullptr, ctx->d_stats, nullptr, mode)) !=
+                cudaSuccess)
                 return cuda_fail(st, e, "knn_candidates_tc");
             mark(ctx, PH_PASS1);
             TileLists second;
             if ((rc = build_second_pass(ctx, A16, bf16, n, d, order, bA, bdelta, &second, st))) return rc;
             mark(ctx, PH_LISTS);
             if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                              &second, true, order.theta, nullptr, ctx->d_stats)) != cudaSuccess)
+                                              &second, true, order.theta, nullptr, ctx->d_stats, nullptr, mode)) !=
+                cudaSuccess)
                 return cuda_fail(st, e, "knn_candidates_tc");
             ctx->launches += 2;
+            if (split) {
+                if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
+                                                  &first, false, order.theta, nullptr, ctx->d_stats, nullptr,
+                                                  kPassCollect)) != cudaSuccess ||
+                    (e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
+                                                  &second, true, order.theta, nullptr, ctx->d_stats, nullptr,
+                                                  kPassCollect)) != cudaSuccess)
+                    return cuda_fail(st, e, "knn_candidates_tc");
+                ctx->launches += 2;
+            }
         } else {
             // Every list keeps its threshold, so the rerank needs no selection.
             float* theta = (float*)ws_get(ctx, SLOT_THETA, sizeof(float) * (size_t)lists.segments * n_pad, &e);

@@ -243,7 +243,11 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
                                      const void* B16, int64_t nr_pad, const float* bA, const float* bdelta,
                                      const float* beps2, const Lists& lists, bool bf16, const TileLists* tiles,
                                      bool resume, float* theta_io, int* grid_out, unsigned long long* stats,
-                                     unsigned long long* argmin_out = nullptr);
+                                     unsigned long long* argmin_out = nullptr, int pass_mode = 0);
+// Pass modes of launch_tensor_candidates (k <= 32, one column segment):
+// thresholds only (register top-k, theta_io written, lists untouched), then
+// collection at the fixed thresholds (appends only).
+constexpr int kPassFull = 0, kPassThresholds = 1, kPassCollect = 2;
 
 // Per-row bound of the candidate lists, as the rerank re-applies it: the
 // plain form's additive margin, or the tensor form's (A, delta, eps2).

@@ -90,6 +90,10 @@ struct TensorArgs {
     unsigned long long* argmin_out;
     int final_cap;              // lists longer than this are pruned once more when an item ends
     int resume;                 // lists and thresholds continue from an earlier pass
+    // thr_only: the pass only tightens thresholds (register top-k, theta_io
+    // written), no list is touched.  collect: the thresholds are fixed at the
+    // smaller of each row's theta_io entries and the pass only appends.
+    int thr_only, collect;
     float* theta_io;            // per list: the threshold when the item ends (read when resuming)
 };
 
@@ -594,8 +598,12 @@ __global__ void __launch_bounds__(THREADS, 1)
             TensorBound bnd{0.f, 0.f, 0.f};
             if (valid) bnd = TensorBound{a.bA[row], a.bdelta[row], a.beps2[row]};
             const int64_t lslot = (row * col_segs + seg) * PARTS + part;
-            if (valid && a.resume) {
-                cnt = min(a.lists.cnt[lslot], (uint32_t)cap);  // below cap when an item ends
+            if (valid && a.collect) {
+                // One column segment: the row's lists are lslot and lslot ^ 1.
+                th = fminf(a.theta_io[lslot], a.theta_io[lslot ^ 1]);
+                if (a.resume) cnt = min(a.lists.cnt[lslot], (uint32_t)cap);
+            } else if (valid && a.resume) {
+                if (!a.thr_only) cnt = min(a.lists.cnt[lslot], (uint32_t)cap);  // below cap when an item ends
                 th = a.theta_io[lslot];
             }
             uint32_t* ids = a.lists.ids + lslot * (int64_t)a.lists.ctot;
@@ -629,7 +637,30 @@ __global__ void __launch_bounds__(THREADS, 1)
                     // the tightened threshold are read again and appended.
                     uint32_t va[32];
                     float cm[4];
-                    if constexpr (TOPK <= 16) {
+                    if (a.collect) {
+                        // At the final thresholds every column that passes is a
+                        // candidate: only its id is kept (the rerank measures it
+                        // again), and each lane loops over its own passes.
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            tmem_ld32(tbase + 32 * c, va);
+                            tmem_ld_wait(va);
+                            cm[c] = min32(va);
+                            if (__any_sync(0xffffffffu, cm[c] < th)) {
+                                uint32_t mask = 0;
+#pragma unroll
+                                for (int j = 0; j < 32; j++) mask |= (f_of(va[j]) < th) ? (1u << j) : 0u;
+                                mask &= chunk_valid(col0 + 32 * c, a.nr, a.self != 0, row + a.self_offset);
+                                while (mask) {
+                                    const int j = __ffs(mask) - 1;
+                                    mask &= mask - 1;
+                                    ids[cnt] = (uint32_t)(col0 + 32 * c + j);
+                                    vals[cnt] = __int_as_float(0xff800000);
+                                    cnt++;
+                                }
+                            }
+                        }
+                    } else if constexpr (TOPK <= 16) {
                         uint32_t vb[32];
                         tmem_ld32(tbase, va);
                         tmem_ld_wait(va);
@@ -656,7 +687,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if ((o2 & 0xffffffff00000000ull) == tag) th = fminf(th, __uint_as_float((uint32_t)o2));
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
-                        if (!a.argmin_out && __any_sync(0xffffffffu, cm[c] < th)) {
+                        if (!a.collect && !a.thr_only && !a.argmin_out && __any_sync(0xffffffffu, cm[c] < th)) {
                             tmem_ld32(tbase + 32 * c, va);
                             tmem_ld_wait(va);
                             append_chunk(va, col0 + 32 * c, th,
@@ -731,8 +762,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                 continue;
             }
             if (valid && ok) {
-                a.lists.cnt[lslot] = min(cnt, (uint32_t)a.lists.ctot);
-                if (a.theta_io) a.theta_io[lslot] = th;
+                if (!a.thr_only) a.lists.cnt[lslot] = min(cnt, (uint32_t)a.lists.ctot);
+                if (a.theta_io && !a.collect) a.theta_io[lslot] = th;
             }
         }
         if (a.stats) {
@@ -908,7 +939,7 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
                                      const void* B16, int64_t nr_pad, const float* bA, const float* bdelta,
                                      const float* beps2, const Lists& lists, bool bf16, const TileLists* tiles,
                                      bool resume, float* theta_io, int* grid_out, unsigned long long* stats,
-                                     unsigned long long* argmin_out) {
+                                     unsigned long long* argmin_out, int pass_mode) {
     if (nq_pad % ROWS || nr_pad % TBN) return cudaErrorInvalidValue;
     CUtensorMap ta, tb;
     const CUtensorMapDataType dt = bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
@@ -959,6 +990,10 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     }
     a.resume = resume ? 1 : 0;
     a.theta_io = theta_io;
+    a.thr_only = pass_mode == kPassThresholds ? 1 : 0;
+    a.collect = pass_mode == kPassCollect ? 1 : 0;
+    if ((a.thr_only || a.collect) && (!theta_io || plan.k > 32 || lists.segments != PARTS))
+        return cudaErrorInvalidValue;
     a.argmin_out = argmin_out;
     if (argmin_out && (plan.k != 1 || resume)) return cudaErrorInvalidValue;
     if (resume && !theta_io) return cudaErrorInvalidValue;
