@@ -123,12 +123,16 @@ __global__ void directed_kernel(const uint32_t* __restrict__ idx, const float* _
                                 int64_t n, int k, const float* __restrict__ sigmas,
                                 const float* __restrict__ rhos, uint32_t* __restrict__ dcol,
                                 float* __restrict__ dw, uint32_t* __restrict__ dcnt,
-                                uint32_t* __restrict__ ekey, unsigned long long* __restrict__ eval,
-                                uint32_t* __restrict__ indeg) {
+                                uint32_t* __restrict__ ekey, unsigned long long* __restrict__ eval) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint32_t* col = dcol + i * k;
-    float* w = dw + i * k;
+    // Rows of up to 32 neighbours are sorted in thread-local storage; wider
+    // rows in place in dcol/dw.
+    uint32_t lcol[32];
+    float lw[32];
+    const bool local = k <= 32;
+    uint32_t* col = local ? lcol : dcol + i * k;
+    float* w = local ? lw : dw + i * k;
     int m = 0;
     const float sigma = sigmas[i], rho = rhos[i];
     for (int j = 0; j < k; j++) {
@@ -151,14 +155,32 @@ __global__ void directed_kernel(const uint32_t* __restrict__ idx, const float* _
     for (int t = 0; t < k; t++) {
         const int64_t slot = i * k + t;
         if (t < m) {
+            if (local) {
+                dcol[slot] = col[t];
+                dw[slot] = w[t];
+            }
             ekey[slot] = col[t];
             eval[slot] = ((unsigned long long)(uint32_t)i << 32) | __float_as_uint(w[t]);
-            atomicAdd(indeg + col[t], 1u);
         } else {
             ekey[slot] = (uint32_t)n;
             eval[slot] = 0ull;
         }
     }
+}
+
+// Bucket starts of the edges sorted by target row: start[j] = the number of
+// keys below j, for j in [0, n] (keys are at most n; n marks unused slots).
+// Position p writes the starts of the rows in (key[p-1], key[p]]; the last
+// position also those above its key.
+__global__ void bucket_starts_kernel(const uint32_t* __restrict__ keys, int64_t E, int64_t n,
+                                     uint32_t* __restrict__ start) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= E) return;
+    const int64_t kp = keys[p];
+    const int64_t lo = p == 0 ? 0 : (int64_t)keys[p - 1] + 1;
+    for (int64_t j = lo; j <= kp && j <= n; ++j) start[j] = (uint32_t)p;
+    if (p == E - 1)
+        for (int64_t j = kp + 1; j <= n; ++j) start[j] = (uint32_t)E;
 }
 
 // Query rows against a reference: the directed weights of each row
@@ -499,10 +521,8 @@ int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float
     unsigned long long* valB = valA + E;
 
     if ((e = launch_smooth_knn(ctx, dist, n, k, sig, rho)) != cudaSuccess) return cuda_fail(st, e, "smooth_knn");
-    if ((e = cudaMemsetAsync(indeg, 0, sizeof(uint32_t) * (size_t)(n + 1), s)) != cudaSuccess)
-        return cuda_fail(st, e, "memset");
     directed_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(idx, dist, n, k, sig, rho, dcol, dw, dcnt, keyA,
-                                                                 valA, indeg);
+                                                                 valA);
     scan_launches += 3 /* smooth_knn */ + 1 /* directed */ + 2 /* merges */;
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "directed weights");
     // Stable radix sort of the edge slots by target row.
@@ -520,9 +540,10 @@ int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
-    // Transpose bucket starts.
-    if ((e = device_exclusive_scan(ctx, indeg, indeg, n + 1, scan_scratch, scan_elems)) != cudaSuccess)
-        return cuda_fail(st, e, "indegree scan");
+    // Transpose bucket starts, from the sorted keys.
+    bucket_starts_kernel<<<(unsigned)((E + 255) / 256), 256, 0, s>>>(kin, E, n, indeg);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "bucket starts");
+    scan_launches += 1;
     merge_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(dcol, dw, dcnt, vin, indeg, n, k, nullptr, rowcnt,
                                                              nullptr, nullptr);
     if ((e = cudaMemsetAsync(rowcnt + n, 0, sizeof(uint32_t), s)) != cudaSuccess) return cuda_fail(st, e, "memset");

@@ -44,63 +44,88 @@ __global__ void anchors_kernel(const float* __restrict__ x, int d, int64_t n, in
     for (int t = threadIdx.x; t < d; t += blockDim.x) out[c * d + t] = x[r * d + t];
 }
 
-// One block per anchor: its kAnchorNeighbours nearest other anchors by FP32
-// squared distance (ties to the smaller id), 0xffffffff past the last.
-constexpr int AK_THREADS = 256;
-__global__ void __launch_bounds__(AK_THREADS) anchor_knn_kernel(const float* __restrict__ anc, int64_t m, int d,
-                                                                uint32_t* __restrict__ nb) {
-    extern __shared__ float ak_dist[];
-    __shared__ float wv[AK_THREADS / 32];
-    __shared__ uint32_t wi[AK_THREADS / 32];
-    const int64_t c = blockIdx.x;
-    const float* a = anc + c * d;
-    for (int64_t j = threadIdx.x; j < m; j += AK_THREADS) {
-        const float* b = anc + j * d;
-        float s = 0.f;
-        for (int t = 0; t < d; ++t) {
-            const float df = a[t] - b[t];
-            s = fmaf(df, df, s);
+// Squared FP32 distances between all anchors (a sequential fma chain over
+// the dimensions per pair), 64 x 64 per block and 4 x 4 per thread; the
+// diagonal is +inf.
+__global__ void __launch_bounds__(256) anchor_dist_kernel(const float* __restrict__ anc, int m, int d,
+                                                          float* __restrict__ dist) {
+    __shared__ __align__(16) float As[64][64];
+    __shared__ __align__(16) float Bs[64][64];
+    const int i0 = blockIdx.y * 64, j0 = blockIdx.x * 64;
+    const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+    float acc[4][4] = {};
+    for (int t0 = 0; t0 < d; t0 += 64) {  // 64 dimensions at a time
+        const int dc = min(64, d - t0);
+        __syncthreads();
+        for (int p = threadIdx.x; p < 64 * 64; p += blockDim.x) {
+            const int r = p / 64, t = p % 64;
+            As[t][r] = (i0 + r < m && t < dc) ? anc[(int64_t)(i0 + r) * d + t0 + t] : 0.f;
+            Bs[t][r] = (j0 + r < m && t < dc) ? anc[(int64_t)(j0 + r) * d + t0 + t] : 0.f;
         }
-        ak_dist[j] = j == c ? __int_as_float(0x7f800000) : s;
+        __syncthreads();
+        for (int t = 0; t < dc; ++t) {
+            const float4 a4 = *reinterpret_cast<const float4*>(&As[t][ty * 4]);
+            const float4 b4 = *reinterpret_cast<const float4*>(&Bs[t][tx * 4]);
+            const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float df = av[p] - bv[q];
+                    acc[p][q] = fmaf(df, df, acc[p][q]);
+                }
+        }
     }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int r = 0; r < kAnchorNeighbours; ++r) {
-        float bv = __int_as_float(0x7f800000);
-        uint32_t bi = 0xffffffffu;
-        for (int64_t j = threadIdx.x; j < m; j += AK_THREADS) {
-            const float v = ak_dist[j];
-            if (v < bv) {  // ascending j per thread: the first minimum wins
-                bv = v;
-                bi = (uint32_t)j;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+        const int i = i0 + ty * 4 + p;
+        if (i >= m) continue;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int j = j0 + tx * 4 + q;
+            if (j < m) dist[(int64_t)i * m + j] = i == j ? __int_as_float(0x7f800000) : acc[p][q];
+        }
+    }
+}
+
+// One warp per anchor: its kAnchorNeighbours nearest other anchors, nearest
+// first, ties to the smaller id; 0xffffffff past the last.  Each lane keeps a
+// sorted top-k of its columns, then the lanes' heads are merged.
+__global__ void __launch_bounds__(128) anchor_top_kernel(const float* __restrict__ dist, int m,
+                                                         uint32_t* __restrict__ nb) {
+    const int lane = threadIdx.x & 31;
+    const int64_t c = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (c >= m) return;
+    constexpr int K = kAnchorNeighbours;
+    unsigned long long top[K];
+#pragma unroll
+    for (int r = 0; r < K; ++r) top[r] = ~0ull;
+    for (int j = lane; j < m; j += 32) {
+        unsigned long long key = ((unsigned long long)float_key(dist[c * m + j]) << 32) | (uint32_t)j;
+        if (key < top[K - 1]) {
+#pragma unroll
+            for (int r = 0; r < K; ++r) {
+                const unsigned long long lo = key < top[r] ? key : top[r];
+                key = key < top[r] ? top[r] : key;
+                top[r] = lo;
             }
         }
+    }
+    for (int r = 0; r < K; ++r) {
+        unsigned long long best = top[0];
         for (int o = 16; o > 0; o >>= 1) {
-            const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-            const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ov < bv || (ov == bv && oi < bi)) {
-                bv = ov;
-                bi = oi;
-            }
+            const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, o);
+            best = other < best ? other : best;
+        }
+        if (top[0] == best) {  // the owning lane pops its head (keys are distinct)
+#pragma unroll
+            for (int q = 0; q < K - 1; ++q) top[q] = top[q + 1];
+            top[K - 1] = ~0ull;
         }
         if (lane == 0) {
-            wv[w] = bv;
-            wi[w] = bi;
+            const bool found = (uint32_t)(best >> 32) < float_key(__int_as_float(0x7f800000));
+            nb[c * K + r] = found ? (uint32_t)best : 0xffffffffu;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            float v = wv[0];
-            uint32_t id = wi[0];
-            for (int t = 1; t < AK_THREADS / 32; ++t)
-                if (wv[t] < v || (wv[t] == v && wi[t] < id)) {
-                    v = wv[t];
-                    id = wi[t];
-                }
-            const bool found = id < (uint32_t)m && v < __int_as_float(0x7f800000);
-            nb[c * kAnchorNeighbours + r] = found ? id : 0xffffffffu;
-            if (found) ak_dist[id] = __int_as_float(0x7f800000);
-        }
-        __syncthreads();
     }
 }
 
@@ -640,6 +665,7 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
                  o_perm = take(4 * (size_t)n), o_cell = take(4 * (size_t)n), o_ccnt = take(4 * (size_t)(m + 1)),
                  o_cst = take(4 * (size_t)(m + 1)), o_nb = take(4 * (size_t)m * kAnchorNeighbours),
                  o_nb2 = take(4 * (size_t)m * kAnchorNeighbours), o_rank = take(4 * (size_t)m),
+                 o_adist = take(4 * (size_t)m * (size_t)m),
                  o_prio = take(4 * (size_t)items * kPrioMax), o_pc = take(4 * (size_t)items),
                  o_theta = take(8 * (size_t)n_pad), o_po = take(4 * (size_t)items),
                  o_best = take(16 * (size_t)n_pad), o_A0 = take(128 * (size_t)n_pad),
@@ -679,8 +705,14 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     ctx->launches += 4;
 
     // Anchor neighbourhoods and the walk that orders the cells.
-    anchor_knn_kernel<<<(unsigned)m, AK_THREADS, sizeof(float) * (size_t)m, s>>>(anc, m, d, anchor_nb);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor neighbours");
+    {
+        float* adist = (float*)(base + o_adist);
+        const dim3 grid((unsigned)((m + 63) / 64), (unsigned)((m + 63) / 64));
+        anchor_dist_kernel<<<grid, 256, 0, s>>>(anc, (int)m, d, adist);
+        anchor_top_kernel<<<(unsigned)((m + 3) / 4), 128, 0, s>>>(adist, (int)m, anchor_nb);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor neighbours");
+        ctx->launches += 2;
+    }
     const size_t chain_smem = 4 * (size_t)((m + 31) / 32) + 2 * (size_t)m * kChainNb;
     if ((e = set_smem_limit(ctx, (const void*)anchor_chain_kernel, (int)chain_smem)) != cudaSuccess)
         return cuda_fail(st, e, "ordering: anchor walk");
