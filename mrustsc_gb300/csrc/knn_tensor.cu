@@ -111,6 +111,10 @@ enum TensorStat : int {
     TS_PRUNE_CYCLES = 9,   // epilogue cycles spent in prunes
     TS_LD_CYCLES = 10,     // epilogue cycles from issuing TMEM loads to their completion
     TS_APPEND_CALLS = 11,  // 32-column chunks that had survivors in some lane (per warp)
+    TS_TOPK_ENTER = 12,    // register top-k: 32-column chunks with an entrant in some lane (per warp)
+    TS_TOPK_BULK = 13,     // register top-k: chunks sorted and merged in bulk (per warp)
+    TS_TOPK_INSERTS = 14,  // register top-k: one-by-one insertion rounds (per warp)
+    TS_TOPK_ENTRANTS = 15, // register top-k: entrants (per lane)
     TS_COUNT = 16
 };
 
@@ -222,9 +226,11 @@ __device__ __forceinline__ void test_chunk(const uint32_t (&v)[32], int64_t colb
 template <int K>
 struct TopK {
     float v[K];
-    __device__ __forceinline__ void reset() {
+    // The first K - k slots hold -inf, so v[K-1] is always the k-th
+    // smallest value met (+inf until k values have been met).
+    __device__ __forceinline__ void reset(int k) {
 #pragma unroll
-        for (int j = 0; j < K; j++) v[j] = __int_as_float(0x7f800000);
+        for (int j = 0; j < K; j++) v[j] = j < K - k ? __int_as_float(0xff800000) : __int_as_float(0x7f800000);
     }
     // x below v[K-1]: shifts the larger entries up by one (independent
     // selects, no dependent chain).
@@ -236,12 +242,7 @@ struct TopK {
         for (int j = K - 1; j > 0; j--) v[j] = gt[j - 1] ? v[j - 1] : (gt[j] ? x : v[j]);
         v[0] = gt[0] ? x : v[0];
     }
-    __device__ __forceinline__ float kth(int k) const {
-        float r = v[0];
-#pragma unroll
-        for (int j = 1; j < K; j++) r = (j == k - 1) ? v[j] : r;
-        return r;
-    }
+    __device__ __forceinline__ float kth() const { return v[K - 1]; }
     // Merges 32 ascending values in: the K smallest of both, ascending (the
     // elementwise minimum against the reversed run is bitonic; a bitonic
     // clean-up sorts it).
@@ -282,11 +283,19 @@ __device__ __forceinline__ void sort32(float (&x)[32]) {
             }
 }
 
+// v[j] for a lane-varying j, by a five-level select tree (short dependency
+// chains; the register array keeps static indices).
 __device__ __forceinline__ float pick32(const uint32_t (&v)[32], int j) {
-    float x = f_of(v[0]);
+    uint32_t t[16];
 #pragma unroll
-    for (int q = 1; q < 32; q++) x = (j == q) ? f_of(v[q]) : x;
-    return x;
+    for (int q = 0; q < 16; q++) t[q] = (j & 1) ? v[2 * q + 1] : v[2 * q];
+#pragma unroll
+    for (int q = 0; q < 8; q++) t[q] = (j & 2) ? t[2 * q + 1] : t[2 * q];
+#pragma unroll
+    for (int q = 0; q < 4; q++) t[q] = (j & 4) ? t[2 * q + 1] : t[2 * q];
+#pragma unroll
+    for (int q = 0; q < 2; q++) t[q] = (j & 8) ? t[2 * q + 1] : t[2 * q];
+    return f_of((j & 16) ? t[1] : t[0]);
 }
 
 // A chunk's columns below the lane's K-th smallest so far enter its top-K,
@@ -321,21 +330,33 @@ __device__ __forceinline__ float topk_chunk(const uint32_t (&v)[32], int64_t col
         }
         return m;
     }
-    if (__any_sync(0xffffffffu, m < top.v[K - 1])) {
-        const float lim = top.v[K - 1];
+    // A column at or above the row's current threshold can neither be one of
+    // its k nearest nor lower the threshold, so it is not an entrant either.
+    if (__any_sync(0xffffffffu, m < fminf(top.kth(), th))) {
+        const float lim = fminf(top.kth(), th);
         const uint32_t valid = chunk_valid(colbase, a.nr, a.self != 0, row + a.self_offset);
         uint32_t want = 0;
 #pragma unroll
         for (int j = 0; j < 32; j++) want |= (f_of(v[j]) < lim) ? (1u << j) : 0u;
         want &= valid;
-        const float old = top.kth(a.k);
+        const float old = top.kth();
+        const uint32_t most = __reduce_max_sync(0xffffffffu, (uint32_t)__popc(want));
+        if (a.stats) {
+            const uint32_t all = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(want));
+            if ((threadIdx.x & 31) == 0) {
+                atomicAdd(a.stats + TS_TOPK_ENTER, 1ull);
+                atomicAdd(a.stats + (most >= 6u ? TS_TOPK_BULK : TS_TOPK_INSERTS),
+                          (unsigned long long)(most >= 6u ? 1u : most));
+                atomicAdd(a.stats + TS_TOPK_ENTRANTS, (unsigned long long)all);
+            }
+        }
         // Many entrants in some lane (the first chunks of a row block): sort
         // the chunk and merge it in, with the warp converged; few: insert
         // them one by one.
-        if (__reduce_max_sync(0xffffffffu, (uint32_t)__popc(want)) >= 6u) {
+        if (most >= 6u) {
             float x[32];
 #pragma unroll
-            for (int j = 0; j < 32; j++) x[j] = ((valid >> j) & 1u) ? f_of(v[j]) : __int_as_float(0x7f800000);
+            for (int j = 0; j < 32; j++) x[j] = ((want >> j) & 1u) ? f_of(v[j]) : __int_as_float(0x7f800000);
             sort32(x);
             top.merge_sorted(x);
         } else if (want) {
@@ -343,10 +364,10 @@ __device__ __forceinline__ float topk_chunk(const uint32_t (&v)[32], int64_t col
                 const int j = __ffs(want) - 1;
                 want &= want - 1;
                 const float x = pick32(v, j);
-                if (x < top.v[K - 1]) top.insert(x);
+                if (x < top.kth()) top.insert(x);
             }
         }
-        const float kth = top.kth(a.k);
+        const float kth = top.kth();
         if (kth < old) th = fminf(th, bnd.theta_f32(kth));
     }
     return m;
@@ -611,7 +632,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const uint64_t tag = (uint64_t)(uint32_t)w << 32;
             *my_th = tag | __float_as_uint(th);
             TopK<(TOPK > 0 ? TOPK : 1)> top;
-            if constexpr (TOPK > 0) top.reset();
+            if constexpr (TOPK > 0) top.reset(TOPK == 1 ? 1 : a.k);
             uint32_t best = 0xffffffffu;
             for (int it = 0; it < order.count; ++it) {
                 const int ct = order.next(it);
