@@ -281,6 +281,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
     const uint32_t* perm = nullptr;  // rows of the lists -> input rows (tensor form with ordering)
     const float* rerank_xs = nullptr;
     const float* rerank_theta = nullptr;
+    int rerank_stride = 0;  // floats per row of rerank_xs
     if (tensor) {
         const bool bf16 = o.precision == SCRUST_PRECISION_BF16;
         void* A16 = ws_get(ctx, SLOT_A16, (size_t)n_pad * 64 * 2, &e);
@@ -377,6 +378,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
             if (!theta) return cuda_fail(st, e, "workspace");
             rerank_xs = xwork;
             rerank_theta = theta;
+            rerank_stride = d;
             TileLists shared;  // several column segments share each row's threshold
             if (lists.segments > 2) {
                 shared.row_theta = (uint32_t*)ws_get(ctx, SLOT_ROWTHETA, sizeof(uint32_t) * (size_t)n_pad, &e);
@@ -392,13 +394,14 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
         mark(ctx, PH_CAND);
         perm = order.perm;
         if (order_rows) {
-            float* xs = (float*)ws_get(ctx, SLOT_XSORTED, sizeof(float) * (size_t)n * d, &e);
+            float* xs = (float*)ws_get(ctx, SLOT_XSORTED, sizeof(float) * (size_t)n * padded_row_floats(d), &e);
             if (!xs) return cuda_fail(st, e, "workspace");
-            if ((e = launch_gather_rows(xwork, order.perm, n, d, xs, s)) != cudaSuccess)
+            if ((e = launch_gather_rows(xwork, order.perm, n, d, padded_row_floats(d), xs, s)) != cudaSuccess)
                 return cuda_fail(st, e, "gather rows");
             ctx->launches += 1;
             rerank_xs = xs;
             rerank_theta = order.theta;
+            rerank_stride = padded_row_floats(d);
         }
         bounds.A = bA;
         bounds.delta = bdelta;
@@ -431,7 +434,8 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
 
     const float* xr = ref ? xcentred : xwork;
     if ((e = launch_rerank(ctx, plan, xr, xr, norm2, norm2, norm64, norm64, x, x, bounds, lists, perm, rerank_xs,
-                           rerank_theta, out_idx, out_dist)) != cudaSuccess)
+                           rerank_theta, out_idx, out_dist, nullptr, nullptr, nullptr, rerank_stride)) !=
+        cudaSuccess)
         return cuda_fail(st, e, "knn_rerank");
     mark(ctx, PH_RERANK);
     return ok(st);

@@ -194,16 +194,16 @@ int32_t batch_enqueue(scrust_context* ctx, const float* x, const void* table, ui
 
     // Exact rerank over the rows in the padded layout; ids relative to each
     // sample's first row.
-    float* xs = (float*)ws_get(ctx, SLOT_XSORTED, sizeof(float) * (size_t)n_pad * d, &e);
+    float* xs = (float*)ws_get(ctx, SLOT_XSORTED, sizeof(float) * (size_t)n_pad * padded_row_floats(d), &e);
     if (!xs) return cuda_fail(st, e, "workspace");
-    if ((e = launch_gather_rows(xwork, row_map, n_pad, d, xs, s)) != cudaSuccess)
+    if ((e = launch_gather_rows(xwork, row_map, n_pad, d, padded_row_floats(d), xs, s)) != cudaSuccess)
         return cuda_fail(st, e, "batch: gather rows");
     RowBounds bounds;
     bounds.A = bA;
     bounds.delta = bdelta;
     bounds.eps2 = beps2;
     if ((e = launch_rerank(ctx, plan, xwork, xwork, norm2, norm2, norm64, norm64, x, x, bounds, lists, row_map, xs, theta,
-                           out_idx, out_dist, row_lo, row_hi)) != cudaSuccess)
+                           out_idx, out_dist, row_lo, row_hi, nullptr, padded_row_floats(d))) != cudaSuccess)
         return cuda_fail(st, e, "batch: knn_rerank");
     ctx->launches += 1;  // the row gather (the rerank counts its own)
     mark(ctx, PH_RERANK);

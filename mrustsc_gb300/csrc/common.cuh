@@ -86,6 +86,24 @@ __device__ __forceinline__ float dist2_f32(const float* __restrict__ a, const fl
     return __fadd_rn(__fadd_rn(s0, s1), __fadd_rn(s2, s3));
 }
 
+// dist2_f32 on rows padded with zeros to d4 float4 words: the same
+// accumulators in the same order (the padding adds exact zeros), so the same
+// value, with a quarter of the loads.
+__device__ __forceinline__ float dist2_f32_v4(const float4* __restrict__ a, const float4* __restrict__ b, int d4) {
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll 4
+    for (int t = 0; t < d4; ++t) {
+        const float4 x = __ldg(a + t), y = __ldg(b + t);
+        const float d0 = __fsub_rn(x.x, y.x), d1 = __fsub_rn(x.y, y.y), d2 = __fsub_rn(x.z, y.z),
+                    d3 = __fsub_rn(x.w, y.w);
+        s0 = __fmaf_rn(d0, d0, s0);
+        s1 = __fmaf_rn(d1, d1, s1);
+        s2 = __fmaf_rn(d2, d2, s2);
+        s3 = __fmaf_rn(d3, d3, s3);
+    }
+    return __fadd_rn(__fadd_rn(s0, s1), __fadd_rn(s2, s3));
+}
+
 // Relative error bound of dist2_f32 with a 1.5x safety factor.
 __host__ __device__ __forceinline__ float dist2_f32_gamma(int d) {
     return (float)(1.5 * ((double)((d + 3) / 4) + 5.0) * kUnit32);

@@ -272,14 +272,16 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
                           const uint32_t* perm, const float* xs, const float* theta, uint32_t* out_idx,
                           float* out_dist, const uint32_t* row_lo = nullptr, const uint32_t* row_hi = nullptr,
-                          const float* xr_list = nullptr);
+                          const float* xr_list = nullptr, int xs_stride = 0);
 // order.cu: row blocks sorted by decreasing count (stable) into `order`;
 // `scratch` holds work_order_scratch(items) bytes.
 size_t work_order_scratch(int items);
 cudaError_t sort_by_work(scrust_context* ctx, const uint32_t* counts, int items, char* scratch, uint32_t* order);
 // order.cu: rows of x in list order, xs[s] = x[perm[s]] (zeros where perm
-// holds 0xffffffff).
-cudaError_t launch_gather_rows(const float* x, const uint32_t* perm, int64_t n, int d, float* xs, cudaStream_t s);
+// holds 0xffffffff), `stride` floats apart with zeros after the d-th.
+cudaError_t launch_gather_rows(const float* x, const uint32_t* perm, int64_t n, int d, int stride, float* xs,
+                               cudaStream_t s);
+inline int padded_row_floats(int d) { return (d + 3) / 4 * 4; }
 
 // conn.cu
 cudaError_t launch_smooth_knn(scrust_context* ctx, const float* dist, int64_t n, int k,

@@ -589,12 +589,12 @@ __global__ void narrow_kernel(const unsigned long long* __restrict__ vals, int i
 }
 
 __global__ void gather_rows_kernel(const float* __restrict__ x, const uint32_t* __restrict__ perm, int64_t n, int d,
-                                   float* __restrict__ xs) {
+                                   int stride, float* __restrict__ xs) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n * d) return;
-    const int64_t s = i / d, t = i % d;
+    if (i >= n * stride) return;
+    const int64_t s = i / stride, t = i % stride;
     const uint32_t r = perm[s];
-    xs[i] = r == 0xffffffffu ? 0.f : x[(int64_t)r * d + t];
+    xs[i] = (r == 0xffffffffu || t >= d) ? 0.f : x[(int64_t)r * d + t];
 }
 
 }  // namespace
@@ -634,8 +634,9 @@ cudaError_t sort_by_work(scrust_context* ctx, const uint32_t* counts, int items,
     return cudaGetLastError();
 }
 
-cudaError_t launch_gather_rows(const float* x, const uint32_t* perm, int64_t n, int d, float* xs, cudaStream_t s) {
-    gather_rows_kernel<<<(unsigned)((n * d + 255) / 256), 256, 0, s>>>(x, perm, n, d, xs);
+cudaError_t launch_gather_rows(const float* x, const uint32_t* perm, int64_t n, int d, int stride, float* xs,
+                               cudaStream_t s) {
+    gather_rows_kernel<<<(unsigned)((n * stride + 255) / 256), 256, 0, s>>>(x, perm, n, d, stride, xs);
     return cudaGetLastError();
 }
 

@@ -41,6 +41,8 @@ struct RerankArgs {
     const uint32_t* perm;  // list row / list entry -> input row, or null
     const float* xs;       // working rows in list order (ordered solves), or null
     const float* xr_list;  // reference rows indexed by list entry (xs for a self solve)
+    int xs_stride;         // floats per row of xs and xr_list
+    int xs_v4;             // rows padded with zeros to a multiple of 4 floats, 16-byte aligned
     const uint32_t* row_lo;  // per input row: first row of its solve (a batch of solves), or null
     const uint32_t* row_hi;  // per input row: end of its solve
     const float* theta;    // per list: its threshold when the candidate pass ended, or null
@@ -230,7 +232,7 @@ __device__ int sorted_row(const RerankArgs& a, int64_t slot, unsigned long long*
     const int segs = a.lists.segments;
     float theta = __int_as_float(0x7f800000);
     for (int l = 0; l < segs; ++l) theta = fminf(theta, a.theta[slot * segs + l]);
-    const float* xq = a.xs + slot * a.d;
+    const float* xq = a.xs + slot * a.xs_stride;
     int m = 0;
     for (int l = 0; l < segs; ++l) {
         const int c = (int)min(a.lists.cnt[slot * segs + l], (uint32_t)a.lists.ctot);
@@ -251,7 +253,10 @@ __device__ int sorted_row(const RerankArgs& a, int64_t slot, unsigned long long*
             if (keep) {
                 const int pos = m + __popc(ballot & lanemask_lt());
                 if (pos < CAP) {
-                    const float r = dist2_f32(xq, a.xr_list + (int64_t)id * a.d, a.d);
+                    const float* xr = a.xr_list + (int64_t)id * a.xs_stride;
+                    const float r = a.xs_v4 ? dist2_f32_v4(reinterpret_cast<const float4*>(xq),
+                                                           reinterpret_cast<const float4*>(xr), a.xs_stride / 4)
+                                            : dist2_f32(xq, xr, a.d);
                     keys[pos] = ((unsigned long long)float_key(r) << 32) | (uint32_t)input_row(a, id);
                 }
             }
@@ -269,6 +274,155 @@ __device__ int sorted_row(const RerankArgs& a, int64_t slot, unsigned long long*
     return 0;
 }
 
+__device__ __forceinline__ unsigned long long min_u64(unsigned long long x, unsigned long long y) {
+    return x < y ? x : y;
+}
+__device__ __forceinline__ unsigned long long max_u64(unsigned long long x, unsigned long long y) {
+    return x < y ? y : x;
+}
+
+// Rows whose lists hold at most 64 entries in all (nearly every row): the
+// entries are read two per lane, the survivors measured, and the (distance,
+// id) keys sorted in registers across the warp (bitonic over 64 positions,
+// position lane + 32 r in key[r]); tie groups are then found from a ballot of
+// the positions that start one.  The result is finalize_row's.  Returns 0
+// when done, 2 for the fallback, 3 when the lists hold more than 64 entries.
+__device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long long* keys_s, double* dbl) {
+    const int lane = threadIdx.x & 31;
+    if (a.lists.overflow[slot]) return 2;
+    const int segs = a.lists.segments;
+    if (segs > 32) return 3;
+    const int cl = lane < segs ? (int)min(a.lists.cnt[slot * segs + lane], (uint32_t)a.lists.ctot) : 0;
+    const float tl = lane < segs ? a.theta[slot * segs + lane] : __int_as_float(0x7f800000);
+    float theta = tl;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) theta = fminf(theta, __shfl_xor_sync(0xffffffffu, theta, o));
+    // Entry e of the row's lists (in list order) -> list and position.
+    int list[2] = {-1, -1}, pos[2] = {0, 0};
+    int m0 = 0;
+    for (int l = 0; l < segs; ++l) {
+        const int c = __shfl_sync(0xffffffffu, cl, l);
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int e = lane + 32 * r;
+            if (list[r] < 0 && e < m0 + c) {
+                list[r] = l;
+                pos[r] = e - m0;
+            }
+        }
+        m0 += c;
+    }
+    if (m0 > 64) return 3;
+    const float* xq = a.xs + slot * a.xs_stride;
+    unsigned long long key[2] = {~0ull, ~0ull};
+    int m = 0;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        bool keep = false;
+        uint32_t id = 0;
+        if (list[r] >= 0) {
+            const int64_t at = (slot * segs + list[r]) * (int64_t)a.lists.ctot + pos[r];
+            id = a.lists.ids[at];
+            if ((int64_t)id >= a.nr) {  // never written by a candidate kernel: refuse to read it
+                atomicExch(a.err + DERR_CANDIDATES, 1);
+            } else {
+                keep = a.lists.vals[at] < theta;
+            }
+        }
+        if (keep) {
+            const float* xr = a.xr_list + (int64_t)id * a.xs_stride;
+            const float d2 = a.xs_v4 ? dist2_f32_v4(reinterpret_cast<const float4*>(xq),
+                                                    reinterpret_cast<const float4*>(xr), a.xs_stride / 4)
+                                     : dist2_f32(xq, xr, a.d);
+            key[r] = ((unsigned long long)float_key(d2) << 32) | (uint32_t)input_row(a, id);
+        }
+        m += __popc(__ballot_sync(0xffffffffu, keep));
+    }
+    if (m < a.k) return 2;
+    // Bitonic sort of the 64 positions (32 when the second half is empty).
+    const int P = m0 > 32 ? 64 : 32;
+    for (int size = 2; size <= P; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride == 32) {
+                const unsigned long long lo = min_u64(key[0], key[1]), hi = max_u64(key[0], key[1]);
+                key[0] = lo;
+                key[1] = hi;
+            } else {
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    if (r == 1 && P == 32) break;
+                    const int i = lane + 32 * r;
+                    const unsigned long long o = __shfl_xor_sync(0xffffffffu, key[r], stride);
+                    const bool take_min = ((i & stride) == 0) == ((i & size) == 0);
+                    key[r] = take_min ? min_u64(key[r], o) : max_u64(key[r], o);
+                }
+            }
+        }
+    }
+    // Positions that start a tie group (runs of consecutive tied values).
+    const unsigned long long up0 = __shfl_up_sync(0xffffffffu, key[0], 1);
+    const unsigned long long up1 = __shfl_up_sync(0xffffffffu, key[1], 1);
+    const unsigned long long last0 = __shfl_sync(0xffffffffu, key[0], 31);
+    bool start[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int p = lane + 32 * r;
+        const unsigned long long prev = r == 0 ? up0 : (lane == 0 ? last0 : up1);
+        start[r] = p == 0 || p >= m || !tied(a, key_r(prev), key_r(key[r]));
+    }
+    const unsigned long long S =
+        (unsigned long long)__ballot_sync(0xffffffffu, start[0]) |
+        ((unsigned long long)__ballot_sync(0xffffffffu, start[1]) << 32);
+    const int k = a.k;
+    const int64_t q = input_row(a, slot);
+    int gs[2], ge[2];
+    bool need[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int p = lane + 32 * r;
+        const unsigned long long upto = p == 63 ? ~0ull : (2ull << p) - 1;  // positions 0..p
+        gs[r] = 63 - __clzll(S & upto);
+        const unsigned long long after = S & ~upto;
+        ge[r] = min(after ? __ffsll(after) - 2 : 63, m - 1);
+        need[r] = p < m && gs[r] < k && (ge[r] > gs[r] || a.metric == SCRUST_METRIC_COSINE);
+    }
+    const bool any_group = __any_sync(0xffffffffu, need[0] || need[1]);
+    if (any_group) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int p = lane + 32 * r;
+            if (p < m) keys_s[p] = key[r];
+            if (need[r]) dbl[p] = adjudicate(a, q, key_id(key[r]));
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int p = lane + 32 * r;
+        if (p >= m || gs[r] >= k) continue;
+        const uint32_t id = key_id(key[r]);
+        int at = p;
+        if (ge[r] > gs[r]) {
+            const double dv = dbl[p];
+            int rank = 0;
+            for (int o = gs[r]; o <= ge[r]; ++o) {
+                const double dq = dbl[o];
+                const uint32_t io = key_id(keys_s[o]);
+                rank += (dq < dv) || (dq == dv && io < id);
+            }
+            at = gs[r] + rank;
+        }
+        if (at < k) {
+            const float dist = (a.metric == SCRUST_METRIC_COSINE || ge[r] > gs[r]) ? __double2float_rn(dbl[p])
+                                                                                    : sqrtf(key_r(key[r]));
+            a.out_idx[q * k + at] = a.row_lo ? id - a.row_lo[q] : id;
+            a.out_dist[q * k + at] = dist;
+        }
+    }
+    __syncwarp();
+    return 0;
+}
+
 __global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs a) {
     extern __shared__ unsigned long long rs_smem[];
     const int warp = threadIdx.x >> 5;
@@ -277,7 +431,8 @@ __global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs
     double* dbl = reinterpret_cast<double*>(keys + RS_KEYS);
     const int64_t slot = (int64_t)blockIdx.x * RS_WARPS + warp;
     if (slot >= a.nq || (a.perm && a.perm[slot] == 0xffffffffu)) return;  // padding of a batch layout
-    const int r = sorted_row<RS_KEYS>(a, slot, keys, dbl);
+    int r = sorted_row_regs(a, slot, keys, dbl);
+    if (r == 3) r = sorted_row<RS_KEYS>(a, slot, keys, dbl);
     if (r && lane == 0) {
         if (r == 1) {
             a.big_rows[atomicAdd(a.big_count, 1u)] = (uint32_t)slot;
@@ -419,7 +574,8 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
                           const double* qn64, const double* rn64, const float* qraw,
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
                           const uint32_t* perm, const float* xs, const float* theta, uint32_t* out_idx,
-                          float* out_dist, const uint32_t* row_lo, const uint32_t* row_hi, const float* xr_list) {
+                          float* out_dist, const uint32_t* row_lo, const uint32_t* row_hi, const float* xr_list,
+                          int xs_stride) {
     cudaError_t e;
     uint32_t* fb_rows = (uint32_t*)ws_get(ctx, SLOT_FALLBACK_ROWS, sizeof(uint32_t) * (size_t)plan.nq, &e);
     if (!fb_rows) return e;
@@ -440,6 +596,8 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.perm = perm;
     a.xs = xs;
     a.xr_list = xr_list ? xr_list : xs;
+    a.xs_stride = xs_stride > 0 ? xs_stride : plan.d;
+    a.xs_v4 = !xr_list && xs && a.xs_stride % 4 == 0 && ((uintptr_t)xs & 15) == 0;
     a.theta = theta;
     a.row_lo = row_lo;
     a.row_hi = row_hi;
