@@ -86,19 +86,49 @@ __device__ __forceinline__ double adjudicate(const RerankArgs& a, int64_t q, uin
 __device__ __forceinline__ float key_r(unsigned long long key) { return key_float((uint32_t)(key >> 32)); }
 __device__ __forceinline__ uint32_t key_id(unsigned long long key) { return (uint32_t)key; }
 
+// Rows of the reference with the same bits in every coordinate.
+__device__ __forceinline__ bool rows_equal(const float* __restrict__ u, const float* __restrict__ v, int d) {
+    const uint32_t* x = reinterpret_cast<const uint32_t*>(u);
+    const uint32_t* y = reinterpret_cast<const uint32_t*>(v);
+    for (int t0 = 0; t0 < d; t0 += 8) {
+        bool eq = true;
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+            if (t0 + t < d) eq &= __ldg(x + t0 + t) == __ldg(y + t0 + t);
+        if (!eq) return false;
+    }
+    return true;
+}
+
+// Tie groups are runs of consecutive sorted candidates whose FP32 values the
+// difference form cannot order.  A group that reaches the first k positions
+// is ordered by FP64 (distance, id), and its members take FP64 distances --
+// unless every member's row has the same bits as the first member's row
+// (duplicated cells): the FP32 values are then equal, the order by id that
+// the sort left is already the FP64 order, and the FP32 value is the
+// distance.  Cosine rows always take FP64 values.
+enum : uint8_t { TIE_NONE = 0, TIE_SAME = 1, TIE_DIFF = 2 };
+
 // Writes the first k of the sorted candidates keys[0..m), resolving tie
-// groups that reach position k-1 by FP64 (distance, id).
+// groups as above; dbl and flags hold m entries of scratch.
 template <class Team>
 __device__ void finalize_row(const Team& team, const RerankArgs& a, int64_t q,
-                             const unsigned long long* keys, int m, double* dbl) {
+                             const unsigned long long* keys, int m, double* dbl, uint8_t* flags) {
     const int k = a.k;
+    const bool cosine = a.metric == SCRUST_METRIC_COSINE;
     for (int p = team.rank; p < m; p += team.size()) {
         int gs = p;
         while (gs > 0 && tied(a, key_r(keys[gs - 1]), key_r(keys[gs]))) gs--;
         if (gs >= k) continue;
         int ge = p;
         while (ge + 1 < m && tied(a, key_r(keys[ge]), key_r(keys[ge + 1]))) ge++;
-        if (ge > gs || a.metric == SCRUST_METRIC_COSINE) dbl[p] = adjudicate(a, q, key_id(keys[p]));
+        uint8_t f = TIE_NONE;
+        if (ge > gs && !cosine)
+            f = (p == gs || rows_equal(a.rraw + (int64_t)key_id(keys[gs]) * a.d,
+                                       a.rraw + (int64_t)key_id(keys[p]) * a.d, a.d))
+                    ? TIE_SAME
+                    : TIE_DIFF;
+        flags[p] = f;
     }
     team.sync();
     for (int p = team.rank; p < m; p += team.size()) {
@@ -107,9 +137,24 @@ __device__ void finalize_row(const Team& team, const RerankArgs& a, int64_t q,
         if (gs >= k) continue;
         int ge = p;
         while (ge + 1 < m && tied(a, key_r(keys[ge]), key_r(keys[ge + 1]))) ge++;
+        bool fp64 = cosine;
+        if (ge > gs && !cosine)
+            for (int o = gs; o <= ge; ++o) fp64 |= flags[o] == TIE_DIFF;
+        if (fp64) dbl[p] = adjudicate(a, q, key_id(keys[p]));
+    }
+    team.sync();
+    for (int p = team.rank; p < m; p += team.size()) {
+        int gs = p;
+        while (gs > 0 && tied(a, key_r(keys[gs - 1]), key_r(keys[gs]))) gs--;
+        if (gs >= k) continue;
+        int ge = p;
+        while (ge + 1 < m && tied(a, key_r(keys[ge]), key_r(keys[ge + 1]))) ge++;
+        bool fp64 = cosine;
+        if (ge > gs && !cosine)
+            for (int o = gs; o <= ge; ++o) fp64 |= flags[o] == TIE_DIFF;
         const uint32_t id = key_id(keys[p]);
         int pos = p;
-        if (ge > gs) {
+        if (fp64 && ge > gs) {
             const double dv = dbl[p];
             int rank = 0;
             for (int o = gs; o <= ge; ++o) {
@@ -120,11 +165,7 @@ __device__ void finalize_row(const Team& team, const RerankArgs& a, int64_t q,
             pos = gs + rank;
         }
         if (pos < k) {
-            float dist;
-            if (a.metric == SCRUST_METRIC_COSINE || ge > gs)
-                dist = __double2float_rn(dbl[p]);
-            else
-                dist = sqrtf(key_r(keys[p]));
+            const float dist = fp64 ? __double2float_rn(dbl[p]) : sqrtf(key_r(keys[p]));
             a.out_idx[q * k + pos] = a.row_lo ? id - a.row_lo[q] : id;
             a.out_dist[q * k + pos] = dist;
         }
@@ -147,6 +188,7 @@ __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a
     const int lane = threadIdx.x & 31;
     unsigned long long* A = rr_smem + (size_t)warp * 2 * RC;
     unsigned long long* B = A + RC;
+    uint8_t* flags = reinterpret_cast<uint8_t*>(rr_smem + (size_t)RR_WARPS * 2 * RC) + (size_t)warp * RC;
     const int64_t slot = (int64_t)blockIdx.x * RR_WARPS + warp;  // list row
     if (slot >= a.nq || (a.perm && a.perm[slot] == 0xffffffffu)) return;
     WarpTeam team;
@@ -206,7 +248,7 @@ __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a
     for (int p = m + lane; p < P; p += 32) B[p] = ~0ull;
     __syncwarp();
     team_bitonic_sort(team, B, P);
-    finalize_row(team, a, q, B, m, reinterpret_cast<double*>(A));
+    finalize_row(team, a, q, B, m, reinterpret_cast<double*>(A), flags);
 }
 
 // Tensor-form solves: the candidate pass left every list with a threshold no
@@ -225,7 +267,7 @@ constexpr int RS_BIG_KEYS = 2048;
 
 // 0: done; 1: more than `cap` survivors; 2: needs the fallback.
 template <int CAP>
-__device__ int sorted_row(const RerankArgs& a, int64_t slot, unsigned long long* keys, double* dbl) {
+__device__ int sorted_row(const RerankArgs& a, int64_t slot, unsigned long long* keys, double* dbl, uint8_t* flags) {
     const int lane = threadIdx.x & 31;
     WarpTeam team;
     if (a.lists.overflow[slot]) return 2;
@@ -270,7 +312,7 @@ __device__ int sorted_row(const RerankArgs& a, int64_t slot, unsigned long long*
     for (int p = m + lane; p < P; p += 32) keys[p] = ~0ull;
     __syncwarp();
     team_bitonic_sort(team, keys, P);
-    finalize_row(team, a, input_row(a, slot), keys, m, dbl);
+    finalize_row(team, a, input_row(a, slot), keys, m, dbl, flags);
     return 0;
 }
 
@@ -374,9 +416,10 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
         (unsigned long long)__ballot_sync(0xffffffffu, start[0]) |
         ((unsigned long long)__ballot_sync(0xffffffffu, start[1]) << 32);
     const int k = a.k;
+    const bool cosine = a.metric == SCRUST_METRIC_COSINE;
     const int64_t q = input_row(a, slot);
     int gs[2], ge[2];
-    bool need[2];
+    bool grouped[2];
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
         const int p = lane + 32 * r;
@@ -384,7 +427,31 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
         gs[r] = 63 - __clzll(S & upto);
         const unsigned long long after = S & ~upto;
         ge[r] = min(after ? __ffsll(after) - 2 : 63, m - 1);
-        need[r] = p < m && gs[r] < k && (ge[r] > gs[r] || a.metric == SCRUST_METRIC_COSINE);
+        grouped[r] = p < m && gs[r] < k && ge[r] > gs[r];
+    }
+    // Members whose row differs from their group's first member's row.
+    unsigned long long D = 0;
+    if (!cosine && __any_sync(0xffffffffu, grouped[0] || grouped[1])) {
+        bool differs[2];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int p = lane + 32 * r;
+            const uint32_t f0 = __shfl_sync(0xffffffffu, key_id(key[0]), gs[r] & 31);
+            const uint32_t f1 = __shfl_sync(0xffffffffu, key_id(key[1]), gs[r] & 31);
+            const uint32_t first = gs[r] < 32 ? f0 : f1;
+            differs[r] = grouped[r] && p != gs[r] &&
+                         !rows_equal(a.rraw + (int64_t)first * a.d, a.rraw + (int64_t)key_id(key[r]) * a.d, a.d);
+        }
+        D = (unsigned long long)__ballot_sync(0xffffffffu, differs[0]) |
+            ((unsigned long long)__ballot_sync(0xffffffffu, differs[1]) << 32);
+    }
+    bool need[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int p = lane + 32 * r;
+        const unsigned long long span =
+            (ge[r] == 63 ? ~0ull : (2ull << ge[r]) - 1) & ~((1ull << gs[r]) - 1);  // positions gs..ge
+        need[r] = p < m && gs[r] < k && (cosine || (grouped[r] && (D & span) != 0));
     }
     const bool any_group = __any_sync(0xffffffffu, need[0] || need[1]);
     if (any_group) {
@@ -402,7 +469,7 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
         if (p >= m || gs[r] >= k) continue;
         const uint32_t id = key_id(key[r]);
         int at = p;
-        if (ge[r] > gs[r]) {
+        if (need[r] && ge[r] > gs[r]) {
             const double dv = dbl[p];
             int rank = 0;
             for (int o = gs[r]; o <= ge[r]; ++o) {
@@ -413,8 +480,7 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
             at = gs[r] + rank;
         }
         if (at < k) {
-            const float dist = (a.metric == SCRUST_METRIC_COSINE || ge[r] > gs[r]) ? __double2float_rn(dbl[p])
-                                                                                    : sqrtf(key_r(key[r]));
+            const float dist = need[r] ? __double2float_rn(dbl[p]) : sqrtf(key_r(key[r]));
             a.out_idx[q * k + at] = a.row_lo ? id - a.row_lo[q] : id;
             a.out_dist[q * k + at] = dist;
         }
@@ -429,10 +495,11 @@ __global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs
     const int lane = threadIdx.x & 31;
     unsigned long long* keys = rs_smem + (size_t)warp * 2 * RS_KEYS;
     double* dbl = reinterpret_cast<double*>(keys + RS_KEYS);
+    uint8_t* flags = reinterpret_cast<uint8_t*>(rs_smem + (size_t)RS_WARPS * 2 * RS_KEYS) + (size_t)warp * RS_KEYS;
     const int64_t slot = (int64_t)blockIdx.x * RS_WARPS + warp;
     if (slot >= a.nq || (a.perm && a.perm[slot] == 0xffffffffu)) return;  // padding of a batch layout
     int r = sorted_row_regs(a, slot, keys, dbl);
-    if (r == 3) r = sorted_row<RS_KEYS>(a, slot, keys, dbl);
+    if (r == 3) r = sorted_row<RS_KEYS>(a, slot, keys, dbl, flags);
     if (r && lane == 0) {
         if (r == 1) {
             a.big_rows[atomicAdd(a.big_count, 1u)] = (uint32_t)slot;
@@ -450,13 +517,15 @@ __global__ void __launch_bounds__(RS_BIG_WARPS * 32) rerank_sorted_big_kernel(Re
     const int lane = threadIdx.x & 31;
     unsigned long long* keys = rb_smem + (size_t)warp * 2 * RS_BIG_KEYS;
     double* dbl = reinterpret_cast<double*>(keys + RS_BIG_KEYS);
+    uint8_t* flags =
+        reinterpret_cast<uint8_t*>(rb_smem + (size_t)RS_BIG_WARPS * 2 * RS_BIG_KEYS) + (size_t)warp * RS_BIG_KEYS;
     for (;;) {
         uint32_t i = 0;
         if (lane == 0) i = atomicAdd(a.big_next, 1u);
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= *a.big_count) break;
         const int64_t slot = a.big_rows[i];
-        const int r = sorted_row<RS_BIG_KEYS>(a, slot, keys, dbl);
+        const int r = sorted_row<RS_BIG_KEYS>(a, slot, keys, dbl, flags);
         if (r && lane == 0) push_fallback(a, slot);
         __syncwarp();
     }
@@ -468,6 +537,7 @@ __global__ void __launch_bounds__(FB_THREADS) rerank_fallback_kernel(RerankArgs 
     extern __shared__ unsigned long long fb_smem[];
     unsigned long long* keys = fb_smem;
     double* dbl = reinterpret_cast<double*>(fb_smem + FB_CAP);
+    uint8_t* flags = reinterpret_cast<uint8_t*>(fb_smem + 2 * FB_CAP);
     __shared__ int scratch;
     __shared__ uint32_t row_s;
     __shared__ uint32_t hist[256];
@@ -562,7 +632,7 @@ __global__ void __launch_bounds__(FB_THREADS) rerank_fallback_kernel(RerankArgs 
             __syncthreads();
             continue;
         }
-        finalize_row(team, a, q, keys, m, dbl);
+        finalize_row(team, a, q, keys, m, dbl, flags);
         __syncthreads();
     }
 }
@@ -627,16 +697,16 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     e = cudaMemsetAsync(ctx->d_counter, 0, 4 * sizeof(uint32_t), ctx->stream);
     if (e != cudaSuccess) return e;
     if (xs && theta) {
-        const size_t smem_s = (size_t)RS_WARPS * 2 * RS_KEYS * sizeof(unsigned long long);
+        const size_t smem_s = (size_t)RS_WARPS * (2 * RS_KEYS * sizeof(unsigned long long) + RS_KEYS);
         const unsigned blocks = (unsigned)((plan.nq + RS_WARPS - 1) / RS_WARPS);
         rerank_sorted_kernel<<<blocks, RS_WARPS * 32, smem_s, ctx->stream>>>(a);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        const size_t smem_b = (size_t)RS_BIG_WARPS * 2 * RS_BIG_KEYS * sizeof(unsigned long long);
+        const size_t smem_b = (size_t)RS_BIG_WARPS * (2 * RS_BIG_KEYS * sizeof(unsigned long long) + RS_BIG_KEYS);
         if ((e = set_smem_limit(ctx, (const void*)rerank_sorted_big_kernel, (int)smem_b)) != cudaSuccess) return e;
         rerank_sorted_big_kernel<<<2 * ctx->sm_count, RS_BIG_WARPS * 32, smem_b, ctx->stream>>>(a);
         ctx->launches += 2;
     } else {
-        const size_t smem_w = (size_t)RR_WARPS * 2 * RC * sizeof(unsigned long long);
+        const size_t smem_w = (size_t)RR_WARPS * (2 * RC * sizeof(unsigned long long) + RC);
         e = set_smem_limit(ctx, (const void*)rerank_warp_kernel, (int)smem_w);
         if (e != cudaSuccess) return e;
         const unsigned blocks = (unsigned)((plan.nq + RR_WARPS - 1) / RR_WARPS);
@@ -644,7 +714,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
         ctx->launches += 1;
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    const size_t smem_f = (size_t)FB_CAP * (sizeof(unsigned long long) + sizeof(double));
+    const size_t smem_f = (size_t)FB_CAP * (sizeof(unsigned long long) + sizeof(double) + 1);
     e = set_smem_limit(ctx, (const void*)rerank_fallback_kernel, (int)smem_f);
     if (e != cudaSuccess) return e;
     rerank_fallback_kernel<<<FB_BLOCKS, FB_THREADS, smem_f, ctx->stream>>>(a);
