@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(256) tile_balls_kernel(const T* __restrict__ o
     __shared__ float scentre[kSegMax][64];
     __shared__ int sstart[kSegMax + 1];
     __shared__ int wheads[8];
-    __shared__ unsigned long long rmax_all, rmax_seg[kSegMax];
+    __shared__ uint32_t rmax_all, rmax_seg[kSegMax];
     __shared__ uint32_t umax_all, umax_seg[kSegMax];
     const int tile = blockIdx.x;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -341,11 +341,11 @@ __global__ void __launch_bounds__(256) tile_balls_kernel(const T* __restrict__ o
     const uint32_t hb = __ballot_sync(0xffffffffu, head);
     if (lane == 0) wheads[w] = __popc(hb);
     if (threadIdx.x == 0) {
-        rmax_all = 0ull;
+        rmax_all = 0u;
         umax_all = 0u;
     }
     if (threadIdx.x < kSegMax) {
-        rmax_seg[threadIdx.x] = 0ull;
+        rmax_seg[threadIdx.x] = 0u;
         umax_seg[threadIdx.x] = 0u;
     }
     __syncthreads();
@@ -380,32 +380,39 @@ __global__ void __launch_bounds__(256) tile_balls_kernel(const T* __restrict__ o
     }
     __syncthreads();
     if (valid) {
-        double r2 = 0.0, s2 = 0.0;
+        // Squared distances to both centres in f32: a sum of d non-negative
+        // rounded squares of rounded differences is at most (d + 2) units of
+        // the last place below the exact value, so scaling by
+        // 1 + (d + 4) 2^-23 (rounded up) bounds it from above.
+        float r2 = 0.f, s2 = 0.f;
         for (int t = 0; t < d; ++t) {
-            const double v = (double)op_float(row[t]);
-            const double df = v - (double)centre[t], ds = v - (double)scentre[seg][t];
-            r2 += df * df;
-            s2 += ds * ds;
+            const float v = op_float(row[t]);
+            const float df = v - centre[t], ds = v - scentre[seg][t];
+            r2 = fmaf(df, df, r2);
+            s2 = fmaf(ds, ds, s2);
         }
+        const float grow = 1.0f + (float)(d + 4) * 1.1920929e-07f;
+        r2 = __fmul_ru(r2, grow);
+        s2 = __fmul_ru(s2, grow);
         const float th = fminf(theta[2 * j], theta[2 * j + 1]);
-        const double v = (double)th + (double)bA[j] + (double)bdelta[j];
-        const float u = isinf(th) && th > 0.f ? th : (v > 0.0 ? __double2float_ru(sqrt(v)) : 0.f);
-        // Non-negative doubles and floats order like their bit patterns.
-        atomicMax(&rmax_all, (unsigned long long)__double_as_longlong(r2));
-        atomicMax(&rmax_seg[seg], (unsigned long long)__double_as_longlong(s2));
+        // The reach sqrt(theta + A + delta), every step rounded up.
+        const float v = __fadd_ru(__fadd_ru(th, bA[j]), bdelta[j]);
+        const float u = isinf(th) && th > 0.f ? th : (v > 0.f ? __fsqrt_ru(v) : 0.f);
+        // Non-negative floats order like their bit patterns.
+        atomicMax(&rmax_all, __float_as_uint(r2));
+        atomicMax(&rmax_seg[seg], __float_as_uint(s2));
         atomicMax(&umax_all, __float_as_uint(u));
         atomicMax(&umax_seg[seg], __float_as_uint(u));
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        b.radius[tile] = __double2float_ru(sqrt(__longlong_as_double((long long)rmax_all)) * (1.0 + 1e-9));
+        b.radius[tile] = __fmul_ru(__fsqrt_ru(__uint_as_float(rmax_all)), 1.0f + 1e-6f);
         b.reach[tile] = __uint_as_float(umax_all);
         b.nseg[tile] = (uint32_t)nseg;
     }
     if (threadIdx.x < nseg) {
         const int sg = threadIdx.x;
-        b.seg_radius[(int64_t)sg * tiles + tile] =
-            __double2float_ru(sqrt(__longlong_as_double((long long)rmax_seg[sg])) * (1.0 + 1e-9));
+        b.seg_radius[(int64_t)sg * tiles + tile] = __fmul_ru(__fsqrt_ru(__uint_as_float(rmax_seg[sg])), 1.0f + 1e-6f);
         b.seg_reach[(int64_t)sg * tiles + tile] = __uint_as_float(umax_seg[sg]);
     }
 }
@@ -413,10 +420,13 @@ __global__ void __launch_bounds__(256) tile_balls_kernel(const T* __restrict__ o
 // Whether a ball of reach u around centre I may hold a point within u of a
 // point of ball T (conservatively true).  The f32 centre distance is within
 // 1e-5 relative plus 3e-5 absolute (centre coordinates are at most 64 in
-// magnitude); the slack covers both, and the comparison itself is in f64.
+// magnitude); the slack covers both.  The test is made on squares in f32,
+// each side moved past its own rounding (a few units of 2^-24 relative), so
+// it never drops a tile the exact test keeps; a NaN keeps the tile.
 __device__ __forceinline__ bool tile_needed(float dc2, float rI, float rT, float uI) {
-    const double dc = sqrt((double)dc2) * (1.0 - 1e-5);
-    return !(dc >= (double)rI + (double)rT + (double)uI * (1.0 + 1e-5) + 1e-4);
+    const float reach = (rI + rT + uI * (1.0f + 1e-5f) + 1e-4f) * (1.0f + 1e-6f);
+    const float lhs = dc2 * ((1.0f - 1e-5f) * (1.0f - 1e-5f) * (1.0f - 1e-6f));
+    return !(lhs >= reach * reach * (1.0f + 1e-6f));
 }
 
 // The cell-segment balls of all tiles, one row each (centres padded to 64
