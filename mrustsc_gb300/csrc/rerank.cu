@@ -331,44 +331,89 @@ __device__ __forceinline__ unsigned long long max_u64(unsigned long long x, unsi
 // when done, 2 for the fallback, 3 when the lists hold more than 64 entries.
 __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long long* keys_s, double* dbl) {
     const int lane = threadIdx.x & 31;
-    if (a.lists.overflow[slot]) return 2;
     const int segs = a.lists.segments;
     if (segs > 32) return 3;
+    // The row's header, its own coordinates and -- with two lists, the
+    // common case -- the first 64 slots of both lists are read at once (the
+    // lists hold at least 64 slots each); only then is anything tested.
+    const uint32_t ovf = a.lists.overflow[slot];
     const int cl = lane < segs ? (int)min(a.lists.cnt[slot * segs + lane], (uint32_t)a.lists.ctot) : 0;
     const float tl = lane < segs ? a.theta[slot * segs + lane] : __int_as_float(0x7f800000);
+    const int64_t base0 = slot * segs * (int64_t)a.lists.ctot;
+    uint32_t sid[2][2];
+    float sval[2][2];
+    if (segs == 2) {
+#pragma unroll
+        for (int l = 0; l < 2; ++l)
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                sid[l][r] = a.lists.ids[base0 + l * (int64_t)a.lists.ctot + lane + 32 * r];
+                sval[l][r] = a.lists.vals[base0 + l * (int64_t)a.lists.ctot + lane + 32 * r];
+            }
+    }
+    if (ovf) return 2;
     float theta = tl;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) theta = fminf(theta, __shfl_xor_sync(0xffffffffu, theta, o));
-    // Entry e of the row's lists (in list order) -> list and position.
-    int list[2] = {-1, -1}, pos[2] = {0, 0};
     int m0 = 0;
-    for (int l = 0; l < segs; ++l) {
-        const int c = __shfl_sync(0xffffffffu, cl, l);
+    uint32_t eid[2] = {0u, 0u};
+    float eval[2] = {0.f, 0.f};
+    bool have[2] = {false, false};
+    if (segs == 2) {
+        const int c0 = __shfl_sync(0xffffffffu, cl, 0), c1 = __shfl_sync(0xffffffffu, cl, 1);
+        m0 = c0 + c1;
+        if (m0 > 64) return 3;
+        // Position e = lane + 32 r: list 0 slot e below c0, else list 1 slot e - c0.
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
             const int e = lane + 32 * r;
-            if (list[r] < 0 && e < m0 + c) {
-                list[r] = l;
-                pos[r] = e - m0;
+            const int p1 = max(e - c0, 0);
+            const uint32_t i10 = __shfl_sync(0xffffffffu, sid[1][0], p1 & 31);
+            const uint32_t i11 = __shfl_sync(0xffffffffu, sid[1][1], p1 & 31);
+            const float v10 = __shfl_sync(0xffffffffu, sval[1][0], p1 & 31);
+            const float v11 = __shfl_sync(0xffffffffu, sval[1][1], p1 & 31);
+            have[r] = e < m0;
+            eid[r] = e < c0 ? sid[0][r] : (p1 < 32 ? i10 : i11);
+            eval[r] = e < c0 ? sval[0][r] : (p1 < 32 ? v10 : v11);
+        }
+    } else {
+        // Entry e of the row's lists (in list order) -> list and position.
+        int list[2] = {-1, -1}, pos[2] = {0, 0};
+        for (int l = 0; l < segs; ++l) {
+            const int c = __shfl_sync(0xffffffffu, cl, l);
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const int e = lane + 32 * r;
+                if (list[r] < 0 && e < m0 + c) {
+                    list[r] = l;
+                    pos[r] = e - m0;
+                }
+            }
+            m0 += c;
+        }
+        if (m0 > 64) return 3;
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            if (list[r] >= 0) {
+                const int64_t at = base0 + list[r] * (int64_t)a.lists.ctot + pos[r];
+                have[r] = true;
+                eid[r] = a.lists.ids[at];
+                eval[r] = a.lists.vals[at];
             }
         }
-        m0 += c;
     }
-    if (m0 > 64) return 3;
     const float* xq = a.xs + slot * a.xs_stride;
     unsigned long long key[2] = {~0ull, ~0ull};
     int m = 0;
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
         bool keep = false;
-        uint32_t id = 0;
-        if (list[r] >= 0) {
-            const int64_t at = (slot * segs + list[r]) * (int64_t)a.lists.ctot + pos[r];
-            id = a.lists.ids[at];
+        const uint32_t id = eid[r];
+        if (have[r]) {
             if ((int64_t)id >= a.nr) {  // never written by a candidate kernel: refuse to read it
                 atomicExch(a.err + DERR_CANDIDATES, 1);
             } else {
-                keep = a.lists.vals[at] < theta;
+                keep = eval[r] < theta;
             }
         }
         if (keep) {
