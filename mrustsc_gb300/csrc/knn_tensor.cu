@@ -823,21 +823,33 @@ template <>
 __device__ __forceinline__ __nv_bfloat16 to16<__nv_bfloat16>(float v) {
     return __float2bfloat16_rn(v);
 }
-__device__ __forceinline__ double f64_of(__half v) { return (double)__half2float(v); }
-__device__ __forceinline__ double f64_of(__nv_bfloat16 v) { return (double)__bfloat162float(v); }
+__device__ __forceinline__ float f32_of(__half v) { return __half2float(v); }
+__device__ __forceinline__ float f32_of(__nv_bfloat16 v) { return __bfloat162float(v); }
+__device__ __forceinline__ uint32_t bits16(__half v) { return (uint32_t)__half_as_ushort(v); }
+__device__ __forceinline__ uint32_t bits16(__nv_bfloat16 v) { return (uint32_t)__bfloat16_as_ushort(v); }
 
 // One thread per padded row: writes A_i and B_i of input row perm[i] (a
 // padding row where perm[i] is 0xffffffff or i >= n) (64 16-bit values each), the
 // quantised squared norm A = |a_hat|^2, the per-row error radius
 // eps = |a_hat - scale*c| + scale*u*|c| (+ scale*u for normalised rows), and
 // the running maxima of eps and |b_hat|.
+//
+// All in f32.  Rows are centred on the f32-rounded column means (the same
+// centre for every row and query, so no distance depends on it).  A square
+// of a 16-bit value is exact in f32, and |a_hat|^2 is summed as an
+// unevaluated pair (two-sum), so its three-part split is as close as an f64
+// sum's.  Sums of rounded non-negative terms are scaled up past their
+// rounding and every step of a bound is rounded upwards.
 template <class T>
-__global__ void tensor_operands_kernel(const float* __restrict__ x, int64_t n, int64_t n_pad, int d,
+__global__ void __launch_bounds__(128) tensor_operands_kernel(const float* __restrict__ x, int64_t n, int64_t n_pad, int d,
                                        const double* __restrict__ means, const uint32_t* __restrict__ max_norm_bits,
                                        int cosine, const uint32_t* __restrict__ perm, T* __restrict__ A16,
                                        T* __restrict__ B16,
                                        float* __restrict__ bA, float* __restrict__ eps,
                                        uint32_t* __restrict__ max_eps_bits, uint32_t* __restrict__ max_bhat_bits) {
+    __shared__ float mean32[TK];
+    for (int t = threadIdx.x; t < d; t += blockDim.x) mean32[t] = __double2float_rn(means[t]);
+    __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_pad) return;
     const float M = __uint_as_float(*max_norm_bits);
@@ -845,67 +857,96 @@ __global__ void tensor_operands_kernel(const float* __restrict__ x, int64_t n, i
     int sexp = M > 0.f ? (int)floorf(log2f(64.0f / M)) : 0;
     sexp = max(-100, min(100, sexp));
     const float scale = ldexpf(1.0f, sexp);
-    __align__(16) T arow[TK];
-    __align__(16) T brow[TK];
-    const T zero = to16<T>(0.f);
-#pragma unroll
-    for (int t = 0; t < TK; t++) {
-        arow[t] = zero;
-        brow[t] = zero;
-    }
+    // Rows are built as packed 16-bit pairs in registers (static indices
+    // only): aw[w] holds columns 2w and 2w + 1.
+    uint32_t aw[TK / 2], bw[TK / 2];
     const bool real = i < n && (!perm || perm[i] != 0xffffffffu);
+    const uint32_t one = bits16(to16<T>(1.0f));
     if (real) {
         const int64_t src = perm ? (int64_t)perm[i] : i;
-        double hh = 0.0, e2 = 0.0, c2 = 0.0;
-        for (int t = 0; t < d; t++) {
-            const float c = __double2float_rn(__dsub_rn((double)__ldg(x + src * d + t), means[t]));
-            const float y = c * scale;
-            const T q = to16<T>(y);
-            const double qd = f64_of(q);
-            arow[t] = q;
-            brow[t] = to16<T>(-2.0f * (float)qd);
-            hh += qd * qd;
-            const double err = qd - (double)y;
-            e2 += err * err;
-            c2 += (double)c * (double)c;
+        const float* xr = x + src * d;
+        float hs = 0.f, hl = 0.f, e2 = 0.f, c2 = 0.f;
+#pragma unroll
+        for (int w = 0; w < TK / 2; w++) {
+            uint32_t pa = 0u, pb = 0u;
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const int t = 2 * w + hh;
+                if (t < d) {
+                    const float c = __fsub_rn(__ldg(xr + t), mean32[t]);
+                    const float y = c * scale;
+                    const T q = to16<T>(y);
+                    const float qf = f32_of(q);
+                    pa |= bits16(q) << (16 * hh);
+                    pb |= bits16(to16<T>(-2.0f * qf)) << (16 * hh);
+                    const float sq = __fmul_rn(qf, qf);  // exact: at most 22 significant bits
+                    const float sum = __fadd_rn(hs, sq), bv = __fsub_rn(sum, hs);
+                    hl = __fadd_rn(hl, __fadd_rn(__fsub_rn(hs, __fsub_rn(sum, bv)), __fsub_rn(sq, bv)));
+                    hs = sum;
+                    const float err = __fsub_rn(qf, y);  // exact: q is y rounded
+                    e2 = __fmaf_rn(err, err, e2);
+                    c2 = __fmaf_rn(c, c, c2);
+                }
+            }
+            aw[w] = pa;
+            bw[w] = pb;
         }
-        const T one = to16<T>(1.0f);
-        arow[d] = one;
-        arow[d + 1] = one;
-        arow[d + 2] = one;
-        const T n1 = to16<T>((float)hh);
-        const double r1 = hh - f64_of(n1);
-        const T n2 = to16<T>((float)r1);
-        const double r2 = r1 - f64_of(n2);
-        const T n3 = to16<T>((float)r2);
-        brow[d] = n1;
-        brow[d + 1] = n2;
-        brow[d + 2] = n3;
-        bA[i] = (float)hh;
-        double ep = sqrt(e2) + 1.01 * (double)scale * kUnit32 * sqrt(c2);
-        if (cosine) ep += 1.01 * (double)scale * kUnit32;
-        ep += 1e-30;
-        const float epf = __double2float_ru(ep);
-        eps[i] = epf;
-        atomicMax(max_eps_bits, __float_as_uint(epf));
-        atomicMax(max_bhat_bits, __float_as_uint(__double2float_ru(sqrt(hh))));
+        // |a_hat|^2 = h + hlo, then n1 + n2 + n3 (each difference below is
+        // exact: a value less its own 16-bit rounding).
+        const float h = __fadd_rn(hs, hl), hlo = __fsub_rn(hl, __fsub_rn(h, hs));
+        const T n1 = to16<T>(h);
+        const float r1 = __fadd_rn(__fsub_rn(h, f32_of(n1)), hlo);
+        const T n2 = to16<T>(r1);
+        const float r2 = __fsub_rn(r1, f32_of(n2));
+        const T n3 = to16<T>(r2);
+        // Columns d .. d + 2: ones in A, the split norm in B.
+#pragma unroll
+        for (int w = 0; w < TK / 2; w++)
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const int t = 2 * w + hh;
+                const int k3 = t - d;
+                if (k3 >= 0 && k3 < 3) {
+                    const uint32_t nb = bits16(k3 == 0 ? n1 : (k3 == 1 ? n2 : n3));
+                    aw[w] |= one << (16 * hh);
+                    bw[w] |= nb << (16 * hh);
+                }
+            }
+        bA[i] = h;
+        const float grow = 1.0f + (float)(d + 4) * 1.1920929e-07f;
+        const float ku = __fmul_ru(__fmul_ru(1.01f, scale), 5.9604645e-08f);
+        float ep = __fadd_ru(__fsqrt_ru(__fmul_ru(e2, grow)), __fmul_ru(ku, __fsqrt_ru(__fmul_ru(c2, grow))));
+        if (cosine) ep = __fadd_ru(ep, ku);
+        ep = __fadd_ru(ep, 1e-30f);
+        eps[i] = ep;
+        atomicMax(max_eps_bits, __float_as_uint(ep));
+        atomicMax(max_bhat_bits, __float_as_uint(__fmul_ru(__fsqrt_ru(__fadd_ru(hs, hl)), 1.0f + 1e-6f)));
     } else {
         // Padding: a reference row whose value against any query is +inf,
         // so it can never become a candidate (and a query row with the same
         // ones as a real row, so that no product is 0 * inf).
-        brow[d] = to16<T>(__int_as_float(0x7f800000));
-        arow[d] = arow[d + 1] = arow[d + 2] = to16<T>(1.0f);
+        const uint32_t inf = bits16(to16<T>(__int_as_float(0x7f800000)));
+#pragma unroll
+        for (int w = 0; w < TK / 2; w++) {
+            uint32_t pa = 0u, pb = 0u;
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const int k3 = 2 * w + hh - d;
+                if (k3 >= 0 && k3 < 3) pa |= one << (16 * hh);
+                if (k3 == 0) pb |= inf << (16 * hh);
+            }
+            aw[w] = pa;
+            bw[w] = pb;
+        }
         bA[i] = 0.f;
         eps[i] = 0.f;
     }
     uint4* ad = reinterpret_cast<uint4*>(A16 + i * TK);
     uint4* bd = reinterpret_cast<uint4*>(B16 + i * TK);
-    const uint4* as = reinterpret_cast<const uint4*>(arow);
-    const uint4* bs = reinterpret_cast<const uint4*>(brow);
 #pragma unroll
-    for (int t = 0; t < TK * 2 / 16; t++) {
-        ad[t] = as[t];
-        bd[t] = bs[t];
+    for (int q = 0; q < TK / 8; q++) {
+        ad[q] = make_uint4(aw[4 * q], aw[4 * q + 1], aw[4 * q + 2], aw[4 * q + 3]);
+        bd[q] = make_uint4(bw[4 * q], bw[4 * q + 1], bw[4 * q + 2], bw[4 * q + 3]);
     }
 }
 
@@ -913,20 +954,24 @@ __global__ void tensor_operands_kernel(const float* __restrict__ x, int64_t n, i
 // 8 * 64 * 2^-24 * (2 |a_hat| Mb + Mb^2 + 3), plus the rounding of A to f32
 // and the residual of the three-part 16-bit split of |b_hat|^2 (at most
 // 2^-24 |b_hat|^2 for bf16 parts, far less for fp16); eps2 = 2 (eps_i + E).
+// Every step rounded upwards.
 __global__ void tensor_bounds_kernel(int64_t n, const float* __restrict__ bA, const float* __restrict__ eps,
                                      const uint32_t* __restrict__ max_eps_bits,
                                      const uint32_t* __restrict__ max_bhat_bits, float* __restrict__ bdelta,
                                      float* __restrict__ beps2) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double Mb = (double)__uint_as_float(*max_bhat_bits);
-    const double E = (double)__uint_as_float(*max_eps_bits);
-    const double A = (double)bA[i];
-    const double a = sqrt(A);
-    const double delta = 8.0 * 64.0 * kUnit32 * (2.0 * a * Mb + Mb * Mb + 3.0) + 2.0 * kUnit32 * A +
-                         4.0 * kUnit32 * Mb * Mb + 1e-7;
-    bdelta[i] = __double2float_ru(delta);
-    beps2[i] = __double2float_ru(2.0 * ((double)eps[i] + E));
+    const float Mb = __uint_as_float(*max_bhat_bits);
+    const float E = __uint_as_float(*max_eps_bits);
+    const float A = bA[i];
+    const float a = __fsqrt_ru(A);
+    const float mb2 = __fmul_ru(Mb, Mb);
+    const float chain = __fadd_ru(__fadd_ru(__fmul_ru(__fmul_ru(2.0f, a), Mb), mb2), 3.0f);
+    float delta = __fmul_ru(3.0517578125e-05f, chain);           // 8 * 64 * 2^-24
+    delta = __fadd_ru(delta, __fmul_ru(1.1920928955078125e-07f, A));  // 2 * 2^-24
+    delta = __fadd_ru(delta, __fmul_ru(2.384185791015625e-07f, mb2)); // 4 * 2^-24
+    bdelta[i] = __fadd_ru(delta, 1e-7f);
+    beps2[i] = __fmul_ru(2.0f, __fadd_ru(eps[i], E));
 }
 
 }  // namespace
