@@ -272,7 +272,8 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
     if (!means || !norm2 || !cnorm || !margin) return cuda_fail(st, e, "workspace");
     uint32_t* max_bits = (uint32_t*)(margin + n_pad);  // spare words: max norm, max eps, max |b_hat|
     if ((e = cudaMemsetAsync(max_bits, 0, 4 * sizeof(uint32_t), s)) != cudaSuccess) return cuda_fail(st, e, "memset");
-    if ((e = launch_column_means(xwork, n, d, ref, means, means + d, s)) != cudaSuccess)
+    if ((e = tensor ? launch_column_means_centre(xwork, n, d, means, means + d, s)
+                    : launch_column_means(xwork, n, d, ref, means, means + d, s)) != cudaSuccess)
         return cuda_fail(st, e, "column means");
     ctx->launches += ref ? 1 : 2;
 
@@ -289,8 +290,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
         float* rb = (float*)ws_get(ctx, SLOT_QERR, sizeof(float) * 4 * (size_t)n_pad, &e);
         if (!A16 || !B16 || !rb) return cuda_fail(st, e, "workspace");
         float *bA = rb, *beps = rb + n_pad, *bdelta = rb + 2 * n_pad, *beps2 = rb + 3 * n_pad;
-        if ((e = launch_centre_transpose(xwork, n, n_pad, d, dp, means, nullptr, norm2, cnorm, nullptr, max_bits, s)) !=
-            cudaSuccess)
+        if ((e = launch_max_centred_norm(xwork, n, d, means, max_bits, ctx->sm_count, s)) != cudaSuccess)
             return cuda_fail(st, e, "centre");
         ctx->launches += 1;
         const int items = (int)(n_pad / 256);

@@ -149,11 +149,9 @@ int32_t batch_enqueue(scrust_context* ctx, const float* x, const void* table, ui
     if (!means || !norm2 || !cnorm || !margin || !A16 || !B16 || !rb) return cuda_fail(st, e, "workspace");
     uint32_t* max_bits = (uint32_t*)(margin + n_pad);
     float *bA = rb, *beps = rb + n_pad, *bdelta = rb + 2 * n_pad, *beps2 = rb + 3 * n_pad;
-    const int dp = d <= 64 ? (d + 3) / 4 * 4 : (d + 63) / 64 * 64;
     if ((e = cudaMemsetAsync(max_bits, 0, 4 * sizeof(uint32_t), s)) != cudaSuccess ||
-        (e = launch_column_means(xwork, n_total, d, false, means, means + d, s)) != cudaSuccess ||
-        (e = launch_centre_transpose(xwork, n_total, (n_total + 255) / 256 * 256, d, dp, means, nullptr, norm2, cnorm,
-                                     nullptr, max_bits, s)) != cudaSuccess ||
+        (e = launch_column_means_centre(xwork, n_total, d, means, means + d, s)) != cudaSuccess ||
+        (e = launch_max_centred_norm(xwork, n_total, d, means, max_bits, ctx->sm_count, s)) != cudaSuccess ||
         (e = launch_tensor_operands(xwork, n_pad, n_pad, d, means, max_bits, cosine, bf16, row_map, A16, B16, bA, beps,
                                     max_bits + 1, max_bits + 2, s)) != cudaSuccess ||
         (e = launch_tensor_bounds(n_pad, bA, beps, max_bits + 1, max_bits + 2, bdelta, beps2, s)) != cudaSuccess)

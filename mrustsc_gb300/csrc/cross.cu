@@ -28,7 +28,6 @@ int32_t reference_prepare(scrust_context* ctx, const float* x, int64_t n, int d,
     cudaError_t e = cudaSuccess;
     const int64_t n_pad = (int64_t)round_up((size_t)n, 256);
     const int mean_blocks = (int)((n + 2047) / 2048);
-    const int dp = (d + 3) / 4 * 4;
     double* means = (double*)ws_get(ctx, SLOT_MEANS, sizeof(double) * ((size_t)d * (mean_blocks + 1)), &e);
     float* terms = (float*)ws_get(ctx, SLOT_QERR, sizeof(float) * 4 * (size_t)n_pad + 64, &e);
     void* A16 = ws_get(ctx, SLOT_A16, (size_t)n_pad * 128, &e);
@@ -36,9 +35,8 @@ int32_t reference_prepare(scrust_context* ctx, const float* x, int64_t n, int d,
     if (!means || !terms || !A16 || !B16) return cuda_fail(st, e, "reference: workspace");
     uint32_t* words = (uint32_t*)(terms + 4 * n_pad);
     if ((e = cudaMemsetAsync(words, 0, 16, s)) != cudaSuccess ||
-        (e = launch_column_means(x, n, d, false, means, means + d, s)) != cudaSuccess ||
-        (e = launch_centre_transpose(x, n, n_pad, d, dp, means, nullptr, terms, terms + n_pad, nullptr, words, s)) !=
-            cudaSuccess ||
+        (e = launch_column_means_centre(x, n, d, means, means + d, s)) != cudaSuccess ||
+        (e = launch_max_centred_norm(x, n, d, means, words, ctx->sm_count, s)) != cudaSuccess ||
         (e = launch_tensor_operands(x, n, n_pad, d, means, words, false, bf16, nullptr, A16, B16, terms + 2 * n_pad,
                                     terms + 3 * n_pad, words + 1, words + 2, s)) != cudaSuccess)
         return cuda_fail(st, e, "reference: operands");

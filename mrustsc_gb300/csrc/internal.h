@@ -195,6 +195,13 @@ cudaError_t launch_column_means(const float* x, int64_t n, int d, bool sequentia
                                 double* partial, cudaStream_t s);
 cudaError_t launch_normalise_rows(const float* x, int64_t n, int d, float* xn, double* norm64,
                                   int* d_err, cudaStream_t s);
+// prep.cu: column means that only fix a centre (tensor form, d <= 64): f32
+// block sums; `partial` as for launch_column_means.
+cudaError_t launch_column_means_centre(const float* x, int64_t n, int d, double* means, double* partial,
+                                       cudaStream_t s);
+// prep.cu: the largest centred row norm only (tensor form, d <= 64).
+cudaError_t launch_max_centred_norm(const float* x, int64_t n, int d, const double* means, uint32_t* max_norm_bits,
+                                    int sm_count, cudaStream_t s);
 cudaError_t launch_centre_transpose(const float* x, int64_t n, int64_t n_pad, int d, int dp,
                                     const double* means, float* coords_t, float* norm2,
                                     float* cnorm, float* xcentred, uint32_t* max_norm_bits,

@@ -11,6 +11,8 @@
 //   margins          per-row candidate margin from the derived error bound
 //
 // All kernels here are HBM-bound single passes over n x D floats.
+#include <algorithm>
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -165,9 +167,99 @@ cudaError_t launch_column_means(const float* x, int64_t n, int d, bool sequentia
     return cudaGetLastError();
 }
 
+namespace {
+
+// Column means for the tensor form, where they only fix a centre (any
+// centre serves, as long as every row and query is centred on the same
+// one): f32 partial sums over 1024-row blocks, one warp per row at a time,
+// then an f64 sum of the partials.  d <= 64.
+constexpr int kMeanRowsF32 = 1024;
+__global__ void __launch_bounds__(256) means_partial_f32_kernel(const float* __restrict__ x, int64_t n, int d,
+                                                                float* __restrict__ partial) {
+    __shared__ float acc_s[8][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t r0 = (int64_t)blockIdx.x * kMeanRowsF32;
+    const int64_t r1 = min(n, r0 + kMeanRowsF32);
+    float a0 = 0.f, a1 = 0.f;
+    for (int64_t r = r0 + w; r < r1; r += 8) {
+        if (lane < d) a0 += __ldg(x + r * d + lane);
+        if (lane + 32 < d) a1 += __ldg(x + r * d + lane + 32);
+    }
+    acc_s[w][lane] = a0;
+    acc_s[w][lane + 32] = a1;
+    __syncthreads();
+    if (threadIdx.x < d) {
+        float t = 0.f;
+        for (int q = 0; q < 8; ++q) t += acc_s[q][threadIdx.x];
+        partial[(int64_t)blockIdx.x * d + threadIdx.x] = t;
+    }
+}
+
+__global__ void means_final_f32_kernel(const float* __restrict__ partial, int blocks, int64_t n, int d,
+                                       double* __restrict__ means) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d) return;
+    double t = 0.0;
+    for (int b = 0; b < blocks; b++) t += (double)partial[(int64_t)b * d + c];
+    means[c] = t / (double)n;
+}
+
+}  // namespace
+
+// `partial` is the d * (ceil(n / 2048) + 1) doubles that launch_column_means
+// takes; the f32 partials of 1024-row blocks fit in it.
+cudaError_t launch_column_means_centre(const float* x, int64_t n, int d, double* means, double* partial,
+                                       cudaStream_t s) {
+    const int blocks = (int)((n + kMeanRowsF32 - 1) / kMeanRowsF32);
+    means_partial_f32_kernel<<<blocks, 256, 0, s>>>(x, n, d, reinterpret_cast<float*>(partial));
+    means_final_f32_kernel<<<1, 64, 0, s>>>(reinterpret_cast<const float*>(partial), blocks, n, d, means);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_normalise_rows(const float* x, int64_t n, int d, float* xn, double* norm64,
                                   int* d_err, cudaStream_t s) {
     normalise_rows_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, n, d, xn, norm64, d_err);
+    return cudaGetLastError();
+}
+
+// The largest norm of a row centred on the f32-rounded column means (as
+// the tensor operands centre them), bounded from above; one warp per row,
+// lanes over the coordinates (d <= 64).
+__global__ void __launch_bounds__(256) max_centred_norm_kernel(const float* __restrict__ x, int64_t n, int d,
+                                                               const double* __restrict__ means,
+                                                               uint32_t* __restrict__ max_norm_bits) {
+    __shared__ float m32[64];
+    if (threadIdx.x < 64) m32[threadIdx.x] = threadIdx.x < d ? __double2float_rn(means[threadIdx.x]) : 0.f;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    float best = 0.f;
+    for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n; r += warps) {
+        float acc = 0.f;
+        if (lane < d) {
+            const float c = __fsub_rn(__ldg(x + r * d + lane), m32[lane]);
+            acc = c * c;
+        }
+        if (lane + 32 < d) {
+            const float c = __fsub_rn(__ldg(x + r * d + lane + 32), m32[lane + 32]);
+            acc = __fmaf_rn(c, c, acc);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        best = fmaxf(best, acc);
+    }
+    if (lane == 0 && best > 0.f) {
+        // A sum of d rounded non-negative terms, scaled past its rounding.
+        const float grow = 1.0f + (float)(d + 4) * 1.1920929e-07f;
+        atomicMax(max_norm_bits, __float_as_uint(__fmul_ru(__fsqrt_ru(__fmul_ru(best, grow)), 1.0f + 9.5367431640625e-07f)));
+    }
+}
+
+cudaError_t launch_max_centred_norm(const float* x, int64_t n, int d, const double* means, uint32_t* max_norm_bits,
+                                    int sm_count, cudaStream_t s) {
+    const int64_t want = (n + 7) / 8;
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count * 16));
+    max_centred_norm_kernel<<<blocks, 256, 0, s>>>(x, n, d, means, max_norm_bits);
     return cudaGetLastError();
 }
 
