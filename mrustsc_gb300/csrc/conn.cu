@@ -245,15 +245,26 @@ __global__ void rs_hist_kernel(const uint32_t* __restrict__ keys, int64_t total,
     block_hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
 }
 
-__global__ void rs_scatter_kernel(const uint32_t* __restrict__ kin, const unsigned long long* __restrict__ vin,
-                                  uint32_t* __restrict__ kout, unsigned long long* __restrict__ vout,
-                                  int64_t total, int shift, const uint32_t* __restrict__ offsets,
-                                  int nblocks) {
+// One tile of RS_TILE pairs per block: each pair's rank among the tile's
+// pairs of its digit (warp by warp, in input order: the sort is stable), the
+// tile reordered by digit in shared memory, then written out digit run by
+// digit run so that neighbouring threads write neighbouring addresses.
+constexpr size_t RS_STAGE_BYTES = (size_t)RS_TILE * (sizeof(unsigned long long) + sizeof(uint32_t));
+__global__ void __launch_bounds__(RS_THREADS) rs_scatter_kernel(const uint32_t* __restrict__ kin,
+                                                                const unsigned long long* __restrict__ vin,
+                                                                uint32_t* __restrict__ kout,
+                                                                unsigned long long* __restrict__ vout, int64_t total,
+                                                                int shift, const uint32_t* __restrict__ offsets,
+                                                                int nblocks) {
+    extern __shared__ unsigned long long rs_stage[];  // RS_TILE payloads, then RS_TILE keys
+    uint32_t* kst = reinterpret_cast<uint32_t*>(rs_stage + RS_TILE);
     __shared__ uint32_t wcnt[RS_WARPS][256];
+    __shared__ uint32_t dstart[256], dout[256], wsum[RS_WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int d = lane; d < 256; d += 32) wcnt[warp][d] = 0;
     __syncwarp();
-    const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)warp * (RS_TILE / RS_WARPS);
+    const int64_t t0 = (int64_t)blockIdx.x * RS_TILE;
+    const int64_t base = t0 + (int64_t)warp * (RS_TILE / RS_WARPS);
     uint32_t key[RS_ROUNDS];
     unsigned long long val[RS_ROUNDS];
     uint32_t rank[RS_ROUNDS];
@@ -273,6 +284,8 @@ __global__ void rs_scatter_kernel(const uint32_t* __restrict__ kin, const unsign
     }
     __syncthreads();
     {
+        // Per digit: each warp's offset within the tile's run of that digit,
+        // then the run starts (an exclusive scan over the 256 digits).
         const int d = threadIdx.x;  // 256 threads, one digit each
         uint32_t run = 0;
         for (int w = 0; w < RS_WARPS; w++) {
@@ -280,6 +293,18 @@ __global__ void rs_scatter_kernel(const uint32_t* __restrict__ kin, const unsign
             wcnt[w][d] = run;
             run += c;
         }
+        uint32_t incl = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) wsum[warp] = incl;
+        dout[d] = offsets[(int64_t)d * nblocks + blockIdx.x];
+        __syncthreads();
+        uint32_t before = 0;
+        for (int w = 0; w < warp; w++) before += wsum[w];
+        dstart[d] = before + incl - run;
     }
     __syncthreads();
 #pragma unroll
@@ -287,10 +312,19 @@ __global__ void rs_scatter_kernel(const uint32_t* __restrict__ kin, const unsign
         const int64_t p = base + r * 32 + lane;
         if (p < total) {
             const uint32_t d = (key[r] >> shift) & 255u;
-            const int64_t dst = (int64_t)offsets[(int64_t)d * nblocks + blockIdx.x] + wcnt[warp][d] + rank[r];
-            kout[dst] = key[r];
-            vout[dst] = val[r];
+            const uint32_t lp = dstart[d] + wcnt[warp][d] + rank[r];
+            kst[lp] = key[r];
+            rs_stage[lp] = val[r];
         }
+    }
+    __syncthreads();
+    const int count = (int)min((int64_t)RS_TILE, total - t0);
+    for (int lp = threadIdx.x; lp < count; lp += RS_THREADS) {
+        const uint32_t k = kst[lp];
+        const uint32_t d = (k >> shift) & 255u;
+        const int64_t dst = (int64_t)dout[d] + (lp - (int)dstart[d]);
+        kout[dst] = k;
+        vout[dst] = rs_stage[lp];
     }
 }
 
@@ -425,7 +459,9 @@ cudaError_t radix_sort_pairs(scrust_context* ctx, uint32_t* kA, unsigned long lo
         rs_hist_kernel<<<nblocks, RS_THREADS, 0, ctx->stream>>>(kin, n, shift, hist, nblocks);
         if ((e = device_exclusive_scan(ctx, hist, hist, (int64_t)256 * nblocks, scan_scratch, scan_elems)) != cudaSuccess)
             return e;
-        rs_scatter_kernel<<<nblocks, RS_THREADS, 0, ctx->stream>>>(kin, vin, kout, vout, n, shift, hist, nblocks);
+        if ((e = set_smem_limit(ctx, (const void*)rs_scatter_kernel, (int)RS_STAGE_BYTES)) != cudaSuccess) return e;
+        rs_scatter_kernel<<<nblocks, RS_THREADS, RS_STAGE_BYTES, ctx->stream>>>(kin, vin, kout, vout, n, shift, hist,
+                                                                                nblocks);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         ctx->launches += 2;
         std::swap(kin, kout);
@@ -534,7 +570,9 @@ int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float
         rs_hist_kernel<<<nblocks, RS_THREADS, 0, s>>>(kin, E, shift, hist, nblocks);
         if ((e = device_exclusive_scan(ctx, hist, hist, (int64_t)256 * nblocks, scan_scratch, scan_elems)) != cudaSuccess)
             return cuda_fail(st, e, "radix scan");
-        rs_scatter_kernel<<<nblocks, RS_THREADS, 0, s>>>(kin, vin, kout, vout, E, shift, hist, nblocks);
+        if ((e = set_smem_limit(ctx, (const void*)rs_scatter_kernel, (int)RS_STAGE_BYTES)) != cudaSuccess)
+            return cuda_fail(st, e, "radix scatter");
+        rs_scatter_kernel<<<nblocks, RS_THREADS, RS_STAGE_BYTES, s>>>(kin, vin, kout, vout, E, shift, hist, nblocks);
         scan_launches += 2;
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "radix scatter");
         std::swap(kin, kout);
