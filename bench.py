@@ -350,16 +350,24 @@ def run_ours(args):
             line["recall_vs_plain"] = float((idx_t == idx).all(1).float().mean().item())
 
     if rank == 0 and not args.no_e2e:
+        # Pinned host buffers for the input and both neighbour arrays (the
+        # graph's host arrays come from the library's own pinned pool).
         xh = torch.from_numpy(x).pin_memory()
-        ih = np.empty((n, k), np.uint32)
-        dh = np.empty((n, k), np.float32)
+        ih = torch.empty((n, k), dtype=torch.int32).pin_memory()
+        dh = torch.empty((n, k), dtype=torch.float32).pin_memory()
         e2e_steps = max(1, min(args.steps, 3))
         nnz = 0
+        # One untimed call first: it sizes the device workspaces and the
+        # pinned pool, as the warm-up steps do for the device-resident timing.
+        out = ctypes.c_void_p()
+        _lib.check(L.scrust_cuda_neighbors_graph(ctx, xh.data_ptr(), n, d, k, ctypes.byref(opts), ih.data_ptr(),
+                                                 dh.data_ptr(), ctypes.byref(out), ctypes.byref(st)), st)
+        L.scrust_csr_free(out)
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             out = ctypes.c_void_p()
-            rc = L.scrust_cuda_neighbors_graph(ctx, xh.data_ptr(), n, d, k, ctypes.byref(opts), ih.ctypes.data,
-                                               dh.ctypes.data, ctypes.byref(out), ctypes.byref(st))
+            rc = L.scrust_cuda_neighbors_graph(ctx, xh.data_ptr(), n, d, k, ctypes.byref(opts), ih.data_ptr(),
+                                               dh.data_ptr(), ctypes.byref(out), ctypes.byref(st))
             _lib.check(rc, st)
             nnz = int(L.scrust_csr_nnz(out))
             L.scrust_csr_free(out)

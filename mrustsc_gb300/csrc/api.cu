@@ -7,7 +7,10 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <new>
+#include <utility>
+#include <vector>
 
 #include "common.cuh"
 #include "internal.h"
@@ -501,6 +504,53 @@ int32_t conn_device_impl(scrust_context* ctx, const uint32_t* idx, const float* 
 }
 
 // Copies a device CSR into a new host CSR (synchronising the stream).
+// Pinned host slabs for downloaded graphs, reused across calls and
+// contexts: a device-to-host copy into pinned memory runs at the link's
+// speed, while pageable memory goes through the driver's staging buffers.
+// Freed slabs are kept (up to kPinnedKeep of them) for the next download;
+// the pool is never torn down (the process exit reclaims it).
+std::mutex g_pinned_mu;
+std::vector<std::pair<void*, size_t>> g_pinned_free;
+constexpr size_t kPinnedKeep = 4;
+
+void* pinned_take(size_t bytes, size_t* got) {
+    {
+        std::lock_guard<std::mutex> lock(g_pinned_mu);
+        size_t best = g_pinned_free.size();
+        for (size_t i = 0; i < g_pinned_free.size(); ++i)
+            if (g_pinned_free[i].second >= bytes &&
+                (best == g_pinned_free.size() || g_pinned_free[i].second < g_pinned_free[best].second))
+                best = i;
+        if (best < g_pinned_free.size()) {
+            const auto slab = g_pinned_free[best];
+            g_pinned_free.erase(g_pinned_free.begin() + (long)best);
+            *got = slab.second;
+            return slab.first;
+        }
+    }
+    const size_t want = (bytes + bytes / 4 + 4095) & ~(size_t)4095;
+    void* p = nullptr;
+    if (cudaMallocHost(&p, want) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    *got = want;
+    return p;
+}
+
+void pinned_give(void* p, size_t bytes) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lock(g_pinned_mu);
+    g_pinned_free.emplace_back(p, bytes);
+    if (g_pinned_free.size() > kPinnedKeep) {  // drop the smallest
+        size_t small = 0;
+        for (size_t i = 1; i < g_pinned_free.size(); ++i)
+            if (g_pinned_free[i].second < g_pinned_free[small].second) small = i;
+        cudaFreeHost(g_pinned_free[small].first);
+        g_pinned_free.erase(g_pinned_free.begin() + (long)small);
+    }
+}
+
 int32_t csr_to_host(scrust_context* ctx, scrust_csr* dev, scrust_csr** out, scrust_status* st) {
     uint32_t nnz = 0;
     cudaError_t e = cudaMemcpyAsync(&nnz, dev->buf.indptr + dev->n_rows, sizeof(uint32_t),
@@ -509,28 +559,31 @@ int32_t csr_to_host(scrust_context* ctx, scrust_csr* dev, scrust_csr** out, scru
     if (e != cudaSuccess) return cuda_fail(st, e, "csr readback");
     scrust_csr* h = new (std::nothrow) scrust_csr;
     if (!h) return fail(st, SCRUST_OOM, "host allocation failed");
-    try {
-        h->h_indptr.resize(dev->n_rows + 1);
-        h->h_indices.resize(nnz);
-        h->h_values.resize(nnz);
-    } catch (...) {
+    const size_t ip_bytes = sizeof(uint32_t) * (dev->n_rows + 1);
+    const size_t off_idx = (ip_bytes + 255) & ~(size_t)255;
+    const size_t off_val = off_idx + ((sizeof(uint32_t) * (size_t)nnz + 255) & ~(size_t)255);
+    const size_t bytes = off_val + sizeof(float) * (size_t)nnz;
+    h->pinned = pinned_take(bytes, &h->pinned_bytes);
+    if (!h->pinned) {
         delete h;
-        return fail(st, SCRUST_OOM, "host allocation failed");
+        return fail(st, SCRUST_OOM, "pinned host allocation of %zu bytes failed", bytes);
     }
+    h->p_indptr = reinterpret_cast<uint32_t*>(h->pinned);
+    h->p_indices = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(h->pinned) + off_idx);
+    h->p_values = reinterpret_cast<float*>(reinterpret_cast<char*>(h->pinned) + off_val);
     h->n_rows = dev->n_rows;
     h->n_cols = dev->n_cols;
     h->nnz = nnz;
     h->on_device = 0;
-    e = cudaMemcpyAsync(h->h_indptr.data(), dev->buf.indptr, sizeof(uint32_t) * (dev->n_rows + 1),
-                        cudaMemcpyDeviceToHost, ctx->stream);
+    e = cudaMemcpyAsync(h->p_indptr, dev->buf.indptr, ip_bytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess && nnz)
-        e = cudaMemcpyAsync(h->h_indices.data(), dev->buf.indices, sizeof(uint32_t) * nnz, cudaMemcpyDeviceToHost,
+        e = cudaMemcpyAsync(h->p_indices, dev->buf.indices, sizeof(uint32_t) * nnz, cudaMemcpyDeviceToHost,
                             ctx->stream);
     if (e == cudaSuccess && nnz)
-        e = cudaMemcpyAsync(h->h_values.data(), dev->buf.values, sizeof(float) * nnz, cudaMemcpyDeviceToHost,
-                            ctx->stream);
+        e = cudaMemcpyAsync(h->p_values, dev->buf.values, sizeof(float) * nnz, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
+        pinned_give(h->pinned, h->pinned_bytes);
         delete h;
         return cuda_fail(st, e, "csr readback");
     }
@@ -600,6 +653,8 @@ scrust_context* scrust_cuda_context_create(int32_t device, scrust_status* st) {
     ctx->sm_count = p.multiProcessorCount;
     ctx->smem_optin = p.sharedMemPerBlockOptin;
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->copy_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int) * DERR_COUNT);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, sizeof(uint32_t) * 16);
     if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(int) * DERR_COUNT);
@@ -633,8 +688,13 @@ void scrust_cuda_context_destroy(scrust_context* ctx) {
         cudaFree(b.indices);
         cudaFree(b.values);
     }
-    for (int i = 0; i < 5; i++)
+    for (int i = 0; i < 7; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+    }
+    if (ctx->copy_ev) cudaEventDestroy(ctx->copy_ev);
     if (ctx->d_stats) cudaFree(ctx->d_stats);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
@@ -786,19 +846,32 @@ int32_t scrust_cuda_neighbors_graph(scrust_context* ctx, const float* x, uint64_
     if ((e = cudaMemcpyAsync(dx, x, sizeof(float) * n * d, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
         return cuda_fail(st, e, "upload");
     if ((rc = knn_device_impl(ctx, dx, n, d, k, opt, di, dd, st))) return rc;
-    scrust_csr* dev = nullptr;
-    if ((rc = conn_device_impl(ctx, di, dd, n, k, false, &dev, st))) return rc;
-    if ((e = cudaMemcpyAsync(out_idx, di, sizeof(uint32_t) * n * k, cudaMemcpyDeviceToHost, ctx->stream)) !=
+    // The neighbour lists download on the copy stream while the
+    // connectivities run on the main one.
+    if ((e = cudaEventRecord(ctx->copy_ev, ctx->stream)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev, 0)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(out_idx, di, sizeof(uint32_t) * n * k, cudaMemcpyDeviceToHost, ctx->copy_stream)) !=
             cudaSuccess ||
-        (e = cudaMemcpyAsync(out_dist, dd, sizeof(float) * n * k, cudaMemcpyDeviceToHost, ctx->stream)) !=
+        (e = cudaMemcpyAsync(out_dist, dd, sizeof(float) * n * k, cudaMemcpyDeviceToHost, ctx->copy_stream)) !=
             cudaSuccess) {
-        ctx->csr_pool.push_back(dev->buf);
-        delete dev;
+        cudaStreamSynchronize(ctx->copy_stream);
         return cuda_fail(st, e, "download");
+    }
+    scrust_csr* dev = nullptr;
+    if ((rc = conn_device_impl(ctx, di, dd, n, k, false, &dev, st))) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        return rc;
     }
     rc = csr_to_host(ctx, dev, conn, st);
     ctx->csr_pool.push_back(dev->buf);
     delete dev;
+    if ((e = cudaStreamSynchronize(ctx->copy_stream)) != cudaSuccess) {
+        if (!rc) {
+            scrust_csr_free(*conn);
+            *conn = nullptr;
+        }
+        return cuda_fail(st, e, "download");
+    }
     if (rc) return rc;
     return collect_device_errors(ctx, st);
 }
@@ -833,18 +906,19 @@ uint64_t scrust_csr_nnz(const scrust_csr* c) {
 
 int32_t scrust_csr_on_device(const scrust_csr* c) { return c ? c->on_device : 0; }
 const uint32_t* scrust_csr_indptr(const scrust_csr* c) {
-    return c ? (c->on_device ? c->buf.indptr : c->h_indptr.data()) : nullptr;
+    return c ? (c->on_device ? c->buf.indptr : c->pinned ? c->p_indptr : c->h_indptr.data()) : nullptr;
 }
 const uint32_t* scrust_csr_indices(const scrust_csr* c) {
-    return c ? (c->on_device ? c->buf.indices : c->h_indices.data()) : nullptr;
+    return c ? (c->on_device ? c->buf.indices : c->pinned ? c->p_indices : c->h_indices.data()) : nullptr;
 }
 const float* scrust_csr_values(const scrust_csr* c) {
-    return c ? (c->on_device ? c->buf.values : c->h_values.data()) : nullptr;
+    return c ? (c->on_device ? c->buf.values : c->pinned ? c->p_values : c->h_values.data()) : nullptr;
 }
 
 void scrust_csr_free(scrust_csr* c) {
     if (!c) return;
     if (c->on_device && c->owner) return_csr_buffers(c->owner, c->buf);
+    if (c->pinned) pinned_give(c->pinned, c->pinned_bytes);
     delete c;
 }
 

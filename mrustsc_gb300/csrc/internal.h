@@ -81,6 +81,8 @@ struct scrust_context {
     int sm_count = 0;
     size_t smem_optin = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // downloads that overlap later kernels on `stream`
+    cudaEvent_t copy_ev = nullptr;
     std::mutex mu;
     scrust::Workspace ws;
     int* d_err = nullptr;          // scrust::DERR_COUNT ints
@@ -102,8 +104,15 @@ struct scrust_csr {
     int32_t on_device = 0;
     scrust_context* owner = nullptr;  // device CSRs return their buffers to this pool
     scrust::CsrBuffers buf;
+    // Host arrays: either the vectors, or (downloads of a device graph) one
+    // pinned slab from a process-wide pool holding indptr, indices, values.
     std::vector<uint32_t> h_indptr, h_indices;
     std::vector<float> h_values;
+    void* pinned = nullptr;
+    size_t pinned_bytes = 0;
+    uint32_t* p_indptr = nullptr;
+    uint32_t* p_indices = nullptr;
+    float* p_values = nullptr;
 };
 
 namespace scrust {
