@@ -149,6 +149,7 @@ struct KnnPlan {
     int cap = 0;              // list capacity that triggers a prune
     int ctot = 0;             // list storage per (row, segment)
     int segments = 1;
+    int max_ctas = 0;         // tensor sweep: CTAs at most (0: one per SM)
 };
 
 // Keys the rerank's warp path holds per row (the union of the row's lists);

@@ -1069,7 +1069,7 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
                             : tensor_candidates_kernel<0>;
     cudaError_t e = set_smem_limit(ctx, (const void*)kern, (int)SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    const int grid = std::min(a.items, ctx->sm_count);
+    const int grid = std::min(a.items, plan.max_ctas > 0 ? std::min(plan.max_ctas, ctx->sm_count) : ctx->sm_count);
     if (grid_out) *grid_out = grid;
     kern<<<grid, THREADS, SMEM_BYTES, ctx->stream>>>(ta, tb, a);
     return cudaGetLastError();

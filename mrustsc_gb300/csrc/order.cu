@@ -724,15 +724,20 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor neighbours");
         ctx->launches += 2;
     }
+    // The walk (one warp on one SM) runs on the copy stream beside the rows x
+    // anchors pass below, which leaves it that SM; the main stream waits for
+    // it before the cells are formed.
     const size_t chain_smem = 4 * (size_t)((m + 31) / 32) + 2 * (size_t)m * kChainNb;
-    if ((e = set_smem_limit(ctx, (const void*)anchor_chain_kernel, (int)chain_smem)) != cudaSuccess)
+    if ((e = set_smem_limit(ctx, (const void*)anchor_chain_kernel, (int)chain_smem)) != cudaSuccess ||
+        (e = cudaEventRecord(ctx->copy_ev, s)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev, 0)) != cudaSuccess)
         return cuda_fail(st, e, "ordering: anchor walk");
-    anchor_chain_kernel<<<1, 32, chain_smem, s>>>(anchor_nb, (int)m, rank);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor walk");
-    relabel_neighbours_kernel<<<(unsigned)((m * kAnchorNeighbours + 255) / 256), 256, 0, s>>>(anchor_nb, rank, (int)m,
-                                                                                               cell_nb);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor walk");
-    ctx->launches += 3;
+    anchor_chain_kernel<<<1, 32, chain_smem, ctx->copy_stream>>>(anchor_nb, (int)m, rank);
+    relabel_neighbours_kernel<<<(unsigned)((m * kAnchorNeighbours + 255) / 256), 256, 0, ctx->copy_stream>>>(
+        anchor_nb, rank, (int)m, cell_nb);
+    if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaEventRecord(ctx->copy_ev, ctx->copy_stream)) != cudaSuccess)
+        return cuda_fail(st, e, "ordering: anchor walk");
+    ctx->launches += 2;
 
     // Rows x anchors with k = 1 on the tensor cores, keeping only each row's
     // nearest anchor.
@@ -750,9 +755,11 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     px.cap = lx.cap;
     px.ctot = lx.ctot;
     px.segments = lx.segments;
+    px.max_ctas = ctx->sm_count - 1;
     unsigned long long* best = (unsigned long long*)(base + o_best);
     if ((e = launch_tensor_candidates(ctx, px, A0, n_pad, base + o_aB, m_pad, bA0, bdelta, beps2, lx, bf16, nullptr,
-                                      false, nullptr, nullptr, nullptr, best)) != cudaSuccess)
+                                      false, nullptr, nullptr, nullptr, best)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(s, ctx->copy_ev, 0)) != cudaSuccess)
         return cuda_fail(st, e, "ordering: anchor candidates");
     nearest_anchor_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(best, n, m, rank, keysA, valsA);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: nearest anchor");
