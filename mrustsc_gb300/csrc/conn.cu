@@ -69,12 +69,14 @@ __global__ void sum_partial_kernel(const float* __restrict__ x, int64_t total, d
     }
 }
 
+// One warp: strided f64 sums of the block partials, then a fixed tree.
 __global__ void mean_final_kernel(const double* __restrict__ partial, int blocks, int64_t total,
                                   float* __restrict__ mean) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double t = 0.0;
-    for (int b = 0; b < blocks; b++) t += partial[b];
-    *mean = __fdiv_rn(__double2float_rn(t), (float)total);
+    for (int b = threadIdx.x; b < blocks; b += 32) t += partial[b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) *mean = __fdiv_rn(__double2float_rn(t), (float)total);
 }
 
 __global__ void smooth_knn_kernel(const float* __restrict__ dist, int64_t n, int k, double target,

@@ -451,7 +451,8 @@ __global__ void flatten_segments_kernel(TileBalls b, int d, int tiles, const uin
 // All pairs of segment balls, 64 x 64 per block step, 4 x 4 per thread:
 // when segment i (of row block owner[i]) may reach segment j (of tile
 // owner[j]), bit (owner[i], owner[j]) of the reach bitmap is set.  The
-// segment count S is read on the device; blocks stride over the block pairs.
+// segment count S is read on the device; blocks stride over the block pairs
+// of the upper triangle, and each centre distance serves both directions.
 constexpr int SP = 64;
 __global__ void __launch_bounds__(256) segment_pairs_kernel(const float* __restrict__ fc, const float* __restrict__ fr,
                                                             const float* __restrict__ fu,
@@ -464,7 +465,9 @@ __global__ void __launch_bounds__(256) segment_pairs_kernel(const float* __restr
     const int nb = (S + SP - 1) / SP;
     const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
     for (int64_t bp = blockIdx.x; bp < (int64_t)nb * nb; bp += gridDim.x) {
-        const int i0 = (int)(bp / nb) * SP, j0 = (int)(bp % nb) * SP;
+        const int bi = (int)(bp / nb), bj = (int)(bp % nb);
+        if (bi > bj) continue;
+        const int i0 = bi * SP, j0 = bj * SP;
         __syncthreads();
         for (int p = threadIdx.x; p < SP * 64; p += blockDim.x) {
             const int r = p / 64, t = p % 64;
@@ -495,10 +498,13 @@ __global__ void __launch_bounds__(256) segment_pairs_kernel(const float* __restr
             for (int q = 0; q < 4; ++q) {
                 const int j = j0 + tx * 4 + q;
                 if (j >= S) continue;
-                if (tile_needed(acc[p][q], ri, fr[j], ui)) {
-                    const uint32_t oj = fo[j];
+                const float rj = fr[j];
+                const uint32_t oj = fo[j];
+                if (tile_needed(acc[p][q], ri, rj, ui))
                     atomicOr(bitmap + (int64_t)oi * words + (oj >> 5), 1u << (oj & 31));
-                }
+                // Off the diagonal block, the same distance for j reaching i.
+                if (bi != bj && tile_needed(acc[p][q], rj, ri, fu[j]))
+                    atomicOr(bitmap + (int64_t)oj * words + (oi >> 5), 1u << (oi & 31));
             }
         }
     }

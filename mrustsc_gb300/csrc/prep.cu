@@ -195,13 +195,23 @@ __global__ void __launch_bounds__(256) means_partial_f32_kernel(const float* __r
     }
 }
 
-__global__ void means_final_f32_kernel(const float* __restrict__ partial, int blocks, int64_t n, int d,
-                                       double* __restrict__ means) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= d) return;
-    double t = 0.0;
-    for (int b = 0; b < blocks; b++) t += (double)partial[(int64_t)b * d + c];
-    means[c] = t / (double)n;
+// One block of 256 threads per column: strided f32 sums of the partials,
+// then a tree.
+__global__ void __launch_bounds__(256) means_final_f32_kernel(const float* __restrict__ partial, int blocks,
+                                                              int64_t n, int d, double* __restrict__ means) {
+    __shared__ float ws[8];
+    const int c = blockIdx.x;
+    float t = 0.f;
+    for (int b = threadIdx.x; b < blocks; b += blockDim.x) t += partial[(int64_t)b * d + c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float s = 0.f;
+        for (int w = 0; w < 8; ++w) s += ws[w];
+        means[c] = (double)s / (double)n;
+    }
 }
 
 }  // namespace
@@ -212,7 +222,7 @@ cudaError_t launch_column_means_centre(const float* x, int64_t n, int d, double*
                                        cudaStream_t s) {
     const int blocks = (int)((n + kMeanRowsF32 - 1) / kMeanRowsF32);
     means_partial_f32_kernel<<<blocks, 256, 0, s>>>(x, n, d, reinterpret_cast<float*>(partial));
-    means_final_f32_kernel<<<1, 64, 0, s>>>(reinterpret_cast<const float*>(partial), blocks, n, d, means);
+    means_final_f32_kernel<<<d, 256, 0, s>>>(reinterpret_cast<const float*>(partial), blocks, n, d, means);
     return cudaGetLastError();
 }
 
