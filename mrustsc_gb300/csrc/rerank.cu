@@ -323,6 +323,32 @@ __device__ __forceinline__ unsigned long long max_u64(unsigned long long x, unsi
     return x < y ? y : x;
 }
 
+// Ascending bitonic sort across the warp of P = 32 or 64 keys, position
+// lane + 32 r in key[r] (key[1] unused when P = 32); fully unrolled.
+template <int P>
+__device__ __forceinline__ void warp_sort_keys(unsigned long long (&key)[2]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int size = 2; size <= P; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride == 32) {
+                const unsigned long long lo = min_u64(key[0], key[1]), hi = max_u64(key[0], key[1]);
+                key[0] = lo;
+                key[1] = hi;
+            } else {
+#pragma unroll
+                for (int r = 0; r < P / 32; ++r) {
+                    const int i = lane + 32 * r;
+                    const unsigned long long o = __shfl_xor_sync(0xffffffffu, key[r], stride);
+                    const bool take_min = ((i & stride) == 0) == ((i & size) == 0);
+                    key[r] = ((key[r] < o) == take_min) ? key[r] : o;
+                }
+            }
+        }
+    }
+}
+
 // Rows whose lists hold at most 64 entries in all (nearly every row): the
 // entries are read two per lane, the survivors measured, and the (distance,
 // id) keys sorted in registers across the warp (bitonic over 64 positions,
@@ -427,25 +453,10 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
     }
     if (m < a.k) return 2;
     // Bitonic sort of the 64 positions (32 when the second half is empty).
-    const int P = m0 > 32 ? 64 : 32;
-    for (int size = 2; size <= P; size <<= 1) {
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            if (stride == 32) {
-                const unsigned long long lo = min_u64(key[0], key[1]), hi = max_u64(key[0], key[1]);
-                key[0] = lo;
-                key[1] = hi;
-            } else {
-#pragma unroll
-                for (int r = 0; r < 2; ++r) {
-                    if (r == 1 && P == 32) break;
-                    const int i = lane + 32 * r;
-                    const unsigned long long o = __shfl_xor_sync(0xffffffffu, key[r], stride);
-                    const bool take_min = ((i & stride) == 0) == ((i & size) == 0);
-                    key[r] = take_min ? min_u64(key[r], o) : max_u64(key[r], o);
-                }
-            }
-        }
-    }
+    if (m0 > 32)
+        warp_sort_keys<64>(key);
+    else
+        warp_sort_keys<32>(key);
     // Positions that start a tie group (runs of consecutive tied values).
     const unsigned long long up0 = __shfl_up_sync(0xffffffffu, key[0], 1);
     const unsigned long long up1 = __shfl_up_sync(0xffffffffu, key[1], 1);
