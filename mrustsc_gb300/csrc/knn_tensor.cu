@@ -438,10 +438,15 @@ __device__ __forceinline__ void prune_lanes(uint32_t need, const TensorArgs& a, 
 
 // TOPK = K (k <= K, K = 1, 16 or 32): thresholds from a register top-K per
 // lane (TopK); TOPK = 0: from warp-cooperative selections over the lists.
-template <int TOPK>
+template <int TOPK, int PASS>
 __global__ void __launch_bounds__(THREADS, 1)
     tensor_candidates_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
                              TensorArgs a) {
+    // PASS fixes the pass kind at compile time (1: thresholds only, 2:
+    // collect, 0: taken from the arguments), so a specialised pass carries
+    // none of the others' code or registers.
+    const bool thr_only = PASS == 1 || (PASS == 0 && a.thr_only);
+    const bool collect = PASS == 2 || (PASS == 0 && a.collect);
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char* sA = base;
@@ -619,12 +624,12 @@ __global__ void __launch_bounds__(THREADS, 1)
             TensorBound bnd{0.f, 0.f, 0.f};
             if (valid) bnd = TensorBound{a.bA[row], a.bdelta[row], a.beps2[row]};
             const int64_t lslot = (row * col_segs + seg) * PARTS + part;
-            if (valid && a.collect) {
+            if (valid && collect) {
                 // One column segment: the row's lists are lslot and lslot ^ 1.
                 th = fminf(a.theta_io[lslot], a.theta_io[lslot ^ 1]);
                 if (a.resume) cnt = min(a.lists.cnt[lslot], (uint32_t)cap);
             } else if (valid && a.resume) {
-                if (!a.thr_only) cnt = min(a.lists.cnt[lslot], (uint32_t)cap);  // below cap when an item ends
+                if (!thr_only) cnt = min(a.lists.cnt[lslot], (uint32_t)cap);  // below cap when an item ends
                 th = a.theta_io[lslot];
             }
             uint32_t* ids = a.lists.ids + lslot * (int64_t)a.lists.ctot;
@@ -658,7 +663,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     // the tightened threshold are read again and appended.
                     uint32_t va[32];
                     float cm[4];
-                    if (a.collect) {
+                    if (collect) {
                         // At the final thresholds every column that passes is a
                         // candidate: only its id is kept (the rerank measures it
                         // again), and each lane loops over its own passes.
@@ -708,7 +713,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if ((o2 & 0xffffffff00000000ull) == tag) th = fminf(th, __uint_as_float((uint32_t)o2));
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
-                        if (!a.collect && !a.thr_only && !a.argmin_out && __any_sync(0xffffffffu, cm[c] < th)) {
+                        if (!collect && !thr_only && !a.argmin_out && __any_sync(0xffffffffu, cm[c] < th)) {
                             tmem_ld32(tbase + 32 * c, va);
                             tmem_ld_wait(va);
                             append_chunk(va, col0 + 32 * c, th,
@@ -783,8 +788,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                 continue;
             }
             if (valid && ok) {
-                if (!a.thr_only) a.lists.cnt[lslot] = min(cnt, (uint32_t)a.lists.ctot);
-                if (a.theta_io && !a.collect) a.theta_io[lslot] = th;
+                if (!thr_only) a.lists.cnt[lslot] = min(cnt, (uint32_t)a.lists.ctot);
+                if (a.theta_io && !collect) a.theta_io[lslot] = th;
             }
         }
         if (a.stats) {
@@ -1063,10 +1068,12 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.argmin_out = argmin_out;
     if (argmin_out && (plan.k != 1 || resume)) return cudaErrorInvalidValue;
     if (resume && !theta_io) return cudaErrorInvalidValue;
-    auto kern = a.k == 1    ? tensor_candidates_kernel<1>
-                : a.k <= 16 ? tensor_candidates_kernel<16>
-                : a.k <= 32 ? tensor_candidates_kernel<32>
-                            : tensor_candidates_kernel<0>;
+    auto kern = a.k == 1    ? tensor_candidates_kernel<1, 0>
+                : a.k <= 16 ? (a.thr_only ? tensor_candidates_kernel<16, 1>
+                               : a.collect ? tensor_candidates_kernel<16, 2>
+                                           : tensor_candidates_kernel<16, 0>)
+                : a.k <= 32 ? tensor_candidates_kernel<32, 0>
+                            : tensor_candidates_kernel<0, 0>;
     cudaError_t e = set_smem_limit(ctx, (const void*)kern, (int)SMEM_BYTES);
     if (e != cudaSuccess) return e;
     const int grid = std::min(a.items, plan.max_ctas > 0 ? std::min(plan.max_ctas, ctx->sm_count) : ctx->sm_count);
