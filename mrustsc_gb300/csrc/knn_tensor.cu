@@ -167,6 +167,15 @@ __device__ __forceinline__ int item_at(const TensorArgs& a, int j) {
     return a.item_order ? (int)a.item_order[pos] : (int)pos;
 }
 
+__device__ __forceinline__ unsigned long long ld_shared_volatile_u64(uint32_t addr) {
+    unsigned long long v;
+    asm volatile("ld.volatile.shared.u64 %0, [%1];" : "=l"(v) : "r"(addr) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_shared_volatile_u64(uint32_t addr, unsigned long long v) {
+    asm volatile("st.volatile.shared.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+}
+
 __device__ __forceinline__ float min32(const uint32_t (&v)[32]) {
     float m[11];
 #pragma unroll
@@ -243,13 +252,13 @@ struct TopK {
         v[0] = gt[0] ? x : v[0];
     }
     __device__ __forceinline__ float kth() const { return v[K - 1]; }
-    // Merges 32 ascending values in: the K smallest of both, ascending (the
-    // elementwise minimum against the reversed run is bitonic; a bitonic
-    // clean-up sorts it).
-    __device__ __forceinline__ void merge_sorted(const float (&x)[32]) {
+    // Merges 32 ascending values in (f32 bit patterns): the K smallest of
+    // both, ascending (the elementwise minimum against the reversed run is
+    // bitonic; a bitonic clean-up sorts it).
+    __device__ __forceinline__ void merge_sorted(const uint32_t (&x)[32]) {
         static_assert(K <= 32, "merge_sorted holds at most 32 values");
 #pragma unroll
-        for (int i = 0; i < K; i++) v[i] = fminf(v[i], x[K - 1 - i]);
+        for (int i = 0; i < K; i++) v[i] = fminf(v[i], __uint_as_float(x[K - 1 - i]));
 #pragma unroll
         for (int stride = K >> 1; stride > 0; stride >>= 1)
 #pragma unroll
@@ -264,9 +273,9 @@ struct TopK {
     }
 };
 
-// Ascending bitonic sort of 32 values held in registers (fully unrolled,
-// static indices).
-__device__ __forceinline__ void sort32(float (&x)[32]) {
+// Ascending bitonic sort of 32 f32 values held as bit patterns in
+// registers, in place (fully unrolled, static indices).
+__device__ __forceinline__ void sort32(uint32_t (&x)[32]) {
 #pragma unroll
     for (int size = 2; size <= 32; size <<= 1)
 #pragma unroll
@@ -276,9 +285,10 @@ __device__ __forceinline__ void sort32(float (&x)[32]) {
                 const int j = i ^ stride;
                 if (j > i) {
                     const bool up = (i & size) == 0;
-                    const float lo = fminf(x[i], x[j]), hi = fmaxf(x[i], x[j]);
-                    x[i] = up ? lo : hi;
-                    x[j] = up ? hi : lo;
+                    const float a = __uint_as_float(x[i]), b = __uint_as_float(x[j]);
+                    const float lo = fminf(a, b), hi = fmaxf(a, b);
+                    x[i] = __float_as_uint(up ? lo : hi);
+                    x[j] = __float_as_uint(up ? hi : lo);
                 }
             }
 }
@@ -303,7 +313,7 @@ __device__ __forceinline__ float pick32(const uint32_t (&v)[32], int j) {
 // Appending is left to a second look at the tile, once the whole tile has
 // tightened the threshold.
 template <int K>
-__device__ __forceinline__ float topk_chunk(const uint32_t (&v)[32], int64_t colbase, float& th, int64_t row,
+__device__ __forceinline__ float topk_chunk(uint32_t (&v)[32], int64_t colbase, float& th, int64_t row,
                                             const TensorArgs& a, TopK<K>& top, const TensorBound& bnd,
                                             uint32_t& best) {
     const float m = min32(v);
@@ -354,11 +364,11 @@ __device__ __forceinline__ float topk_chunk(const uint32_t (&v)[32], int64_t col
         // the chunk and merge it in, with the warp converged; few: insert
         // them one by one.
         if (most >= 6u) {
-            float x[32];
+            // The chunk is not needed after this: sort it in place.
 #pragma unroll
-            for (int j = 0; j < 32; j++) x[j] = ((want >> j) & 1u) ? f_of(v[j]) : __int_as_float(0x7f800000);
-            sort32(x);
-            top.merge_sorted(x);
+            for (int j = 0; j < 32; j++) v[j] = ((want >> j) & 1u) ? v[j] : 0x7f800000u;
+            sort32(v);
+            top.merge_sorted(v);
         } else if (want) {
             while (want) {
                 const int j = __ffs(want) - 1;
@@ -605,8 +615,9 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int r_local = quarter * 32 + lane;
         const int cap = a.lists.cap;
         const int col_segs = csegs;
-        volatile unsigned long long* my_th = &theta_s[h][part][r_local];
-        volatile unsigned long long* other_th = &theta_s[h][part ^ 1][r_local];
+        // Shared-window addresses (32-bit) of this lane's and its partner's slot.
+        const uint32_t my_th = smem_addr(&theta_s[h][part][r_local]);
+        const uint32_t other_th = smem_addr(&theta_s[h][part ^ 1][r_local]);
         uint32_t tc = 0;
         uint32_t n_app = 0, n_prune = 0, n_ovf = 0;
         long long c_prune = 0, c_wait = 0;
@@ -635,22 +646,24 @@ __global__ void __launch_bounds__(THREADS, 1)
             uint32_t* ids = a.lists.ids + lslot * (int64_t)a.lists.ctot;
             float* vals = a.lists.vals + lslot * (int64_t)a.lists.ctot;
             const uint64_t tag = (uint64_t)(uint32_t)w << 32;
-            *my_th = tag | __float_as_uint(th);
+            st_shared_volatile_u64(my_th, tag | __float_as_uint(th));
             TopK<(TOPK > 0 ? TOPK : 1)> top;
             if constexpr (TOPK > 0) top.reset(TOPK == 1 ? 1 : a.k);
             uint32_t best = 0xffffffffu;
             for (int it = 0; it < order.count; ++it) {
                 const int ct = order.next(it);
-                const long long w0 = a.stats ? clock64() : 0;
+                // (Wait cycles are counted in the unspecialised passes only:
+                // their registers are scarce in the threshold pass.)
+                const long long w0 = (PASS == 0 && a.stats) ? clock64() : 0;
                 if (!mbar_wait_bounded(&tfull[h], tc & 1, a.err)) {
                     ok = false;
                     break;
                 }
-                if (a.stats) c_wait += clock64() - w0;
+                if (PASS == 0 && a.stats) c_wait += clock64() - w0;
                 tc_fence_after();
                 // The partner part's threshold bounds this row just as well,
                 // and so does any other column segment's (through HBM).
-                const unsigned long long o = *other_th;
+                const unsigned long long o = ld_shared_volatile_u64(other_th);
                 if ((o & 0xffffffff00000000ull) == tag) th = fminf(th, __uint_as_float((uint32_t)o));
                 if (a.row_theta && valid) th = fminf(th, key_float(a.row_theta[row]));
                 const int64_t col0 = (int64_t)ct * TBN + part * kPartCols;
@@ -709,7 +722,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             cm[c] = topk_chunk(va, col0 + 32 * c, th, row, a, top, bnd, best);
                         }
                     }
-                    const unsigned long long o2 = *other_th;
+                    const unsigned long long o2 = ld_shared_volatile_u64(other_th);
                     if ((o2 & 0xffffffff00000000ull) == tag) th = fminf(th, __uint_as_float((uint32_t)o2));
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
@@ -758,7 +771,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if (a.stats) c_prune += clock64() - p0;
                 }
                 if (__any_sync(0xffffffffu, th != th_before)) {
-                    *my_th = tag | __float_as_uint(th);
+                    st_shared_volatile_u64(my_th, tag | __float_as_uint(th));
                     if (a.row_theta && valid && th < th_before) atomicMin(a.row_theta + row, float_key(th));
                 }
                 tc++;
