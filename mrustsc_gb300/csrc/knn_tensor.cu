@@ -315,7 +315,7 @@ __device__ __forceinline__ float pick32(const uint32_t (&v)[32], int j) {
 template <int K>
 __device__ __forceinline__ float topk_chunk(uint32_t (&v)[32], int64_t colbase, float& th, int64_t row,
                                             const TensorArgs& a, TopK<K>& top, const TensorBound& bnd,
-                                            uint32_t& best) {
+                                            uint32_t& best, bool keep_threshold = true) {
     const float m = min32(v);
     if constexpr (K == 1) {
         // The chunk minimum is the only candidate; its column is kept too.
@@ -335,7 +335,7 @@ __device__ __forceinline__ float topk_chunk(uint32_t (&v)[32], int64_t colbase, 
                     if (((valid >> j) & 1u) && f_of(v[j]) == mv) jj = j;
                 top.v[0] = mv;
                 best = (uint32_t)(colbase + jj);
-                th = fminf(th, bnd.theta_f32(mv));
+                if (keep_threshold) th = fminf(th, bnd.theta_f32(mv));
             }
         }
         return m;
@@ -453,10 +453,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     tensor_candidates_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
                              TensorArgs a) {
     // PASS fixes the pass kind at compile time (1: thresholds only, 2:
-    // collect, 0: taken from the arguments), so a specialised pass carries
-    // none of the others' code or registers.
+    // collect, 3: nearest column only, 0: taken from the arguments), so a
+    // specialised pass carries none of the others' code or registers.
     const bool thr_only = PASS == 1 || (PASS == 0 && a.thr_only);
     const bool collect = PASS == 2 || (PASS == 0 && a.collect);
+    const bool argmin = PASS == 3 || (PASS == 0 && a.argmin_out != nullptr);
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char* sA = base;
@@ -704,29 +705,29 @@ __global__ void __launch_bounds__(THREADS, 1)
                         tmem_ld32(tbase, va);
                         tmem_ld_wait(va);
                         tmem_ld32(tbase + 32, vb);
-                        cm[0] = topk_chunk(va, col0, th, row, a, top, bnd, best);
+                        cm[0] = topk_chunk(va, col0, th, row, a, top, bnd, best, !argmin);
                         tmem_ld_wait(vb);
                         tmem_ld32(tbase + 64, va);
-                        cm[1] = topk_chunk(vb, col0 + 32, th, row, a, top, bnd, best);
+                        cm[1] = topk_chunk(vb, col0 + 32, th, row, a, top, bnd, best, !argmin);
                         tmem_ld_wait(va);
                         tmem_ld32(tbase + 96, vb);
-                        cm[2] = topk_chunk(va, col0 + 64, th, row, a, top, bnd, best);
+                        cm[2] = topk_chunk(va, col0 + 64, th, row, a, top, bnd, best, !argmin);
                         tmem_ld_wait(vb);
-                        cm[3] = topk_chunk(vb, col0 + 96, th, row, a, top, bnd, best);
+                        cm[3] = topk_chunk(vb, col0 + 96, th, row, a, top, bnd, best, !argmin);
                     } else {
                         // A top-32 leaves no registers for a second chunk in flight.
 #pragma unroll
                         for (int c = 0; c < 4; ++c) {
                             tmem_ld32(tbase + 32 * c, va);
                             tmem_ld_wait(va);
-                            cm[c] = topk_chunk(va, col0 + 32 * c, th, row, a, top, bnd, best);
+                            cm[c] = topk_chunk(va, col0 + 32 * c, th, row, a, top, bnd, best, !argmin);
                         }
                     }
                     const unsigned long long o2 = ld_shared_volatile_u64(other_th);
                     if ((o2 & 0xffffffff00000000ull) == tag) th = fminf(th, __uint_as_float((uint32_t)o2));
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
-                        if (!collect && !thr_only && !a.argmin_out && __any_sync(0xffffffffu, cm[c] < th)) {
+                        if (!collect && !thr_only && !argmin && __any_sync(0xffffffffu, cm[c] < th)) {
                             tmem_ld32(tbase + 32 * c, va);
                             tmem_ld_wait(va);
                             append_chunk(va, col0 + 32 * c, th,
@@ -794,7 +795,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if (a.stats) c_prune += clock64() - p0;
                 }
             }
-            if (a.argmin_out) {
+            if (argmin) {
                 if (valid && ok)
                     a.argmin_out[row * PARTS + part] =
                         ((unsigned long long)float_key(top.v[0]) << 32) | (unsigned long long)best;
@@ -1081,7 +1082,7 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.argmin_out = argmin_out;
     if (argmin_out && (plan.k != 1 || resume)) return cudaErrorInvalidValue;
     if (resume && !theta_io) return cudaErrorInvalidValue;
-    auto kern = a.k == 1    ? tensor_candidates_kernel<1, 0>
+    auto kern = a.k == 1    ? (argmin_out ? tensor_candidates_kernel<1, 3> : tensor_candidates_kernel<1, 0>)
                 : a.k <= 16 ? (a.thr_only ? tensor_candidates_kernel<16, 1>
                                : a.collect ? tensor_candidates_kernel<16, 2>
                                            : tensor_candidates_kernel<16, 0>)
