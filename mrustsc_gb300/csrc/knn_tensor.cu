@@ -1086,7 +1086,9 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
                 : a.k <= 16 ? (a.thr_only ? tensor_candidates_kernel<16, 1>
                                : a.collect ? tensor_candidates_kernel<16, 2>
                                            : tensor_candidates_kernel<16, 0>)
-                : a.k <= 32 ? tensor_candidates_kernel<32, 0>
+                : a.k <= 32 ? (a.thr_only ? tensor_candidates_kernel<32, 1>
+                               : a.collect ? tensor_candidates_kernel<32, 2>
+                                           : tensor_candidates_kernel<32, 0>)
                             : tensor_candidates_kernel<0, 0>;
     cudaError_t e = set_smem_limit(ctx, (const void*)kern, (int)SMEM_BYTES);
     if (e != cudaSuccess) return e;
