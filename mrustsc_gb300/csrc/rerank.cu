@@ -474,6 +474,21 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
     const int k = a.k;
     const bool cosine = a.metric == SCRUST_METRIC_COSINE;
     const int64_t q = input_row(a, slot);
+    // The common case: positions 0..k all start a group, so the first k are
+    // singletons and the sort's order and FP32 values are final.
+    if (!cosine && k < 63 && (S & ((2ull << k) - 1)) == ((2ull << k) - 1)) {
+        if (lane < k) {
+            const uint32_t id = key_id(key[0]);
+            a.out_idx[q * k + lane] = a.row_lo ? id - a.row_lo[q] : id;
+            a.out_dist[q * k + lane] = sqrtf(key_r(key[0]));
+        }
+        if (lane + 32 < k) {
+            const uint32_t id = key_id(key[1]);
+            a.out_idx[q * k + lane + 32] = a.row_lo ? id - a.row_lo[q] : id;
+            a.out_dist[q * k + lane + 32] = sqrtf(key_r(key[1]));
+        }
+        return 0;
+    }
     int gs[2], ge[2];
     bool grouped[2];
 #pragma unroll
