@@ -241,15 +241,13 @@ struct TopK {
 #pragma unroll
         for (int j = 0; j < K; j++) v[j] = j < K - k ? __int_as_float(0xff800000) : __int_as_float(0x7f800000);
     }
-    // x below v[K-1]: shifts the larger entries up by one (independent
-    // selects, no dependent chain).
+    // x below v[K-1]: the larger entries shift up by one.  With v ascending,
+    // the new v[j] is min(v[j], max(v[j-1], x)): two independent min/max per
+    // slot, no compare-and-select chain.
     __device__ __forceinline__ void insert(float x) {
-        bool gt[K];
 #pragma unroll
-        for (int j = 0; j < K; j++) gt[j] = v[j] > x;
-#pragma unroll
-        for (int j = K - 1; j > 0; j--) v[j] = gt[j - 1] ? v[j - 1] : (gt[j] ? x : v[j]);
-        v[0] = gt[0] ? x : v[0];
+        for (int j = K - 1; j > 0; j--) v[j] = fminf(v[j], fmaxf(v[j - 1], x));
+        v[0] = fminf(v[0], x);
     }
     __device__ __forceinline__ float kth() const { return v[K - 1]; }
     // Merges 32 ascending values in (f32 bit patterns): the K smallest of
