@@ -353,15 +353,15 @@ __device__ __forceinline__ float topk_chunk(uint32_t (&v)[32], int64_t colbase, 
             const uint32_t all = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(want));
             if ((threadIdx.x & 31) == 0) {
                 atomicAdd(a.stats + TS_TOPK_ENTER, 1ull);
-                atomicAdd(a.stats + (most >= 6u ? TS_TOPK_BULK : TS_TOPK_INSERTS),
-                          (unsigned long long)(most >= 6u ? 1u : most));
+                atomicAdd(a.stats + (most >= 9u ? TS_TOPK_BULK : TS_TOPK_INSERTS),
+                          (unsigned long long)(most >= 9u ? 1u : most));
                 atomicAdd(a.stats + TS_TOPK_ENTRANTS, (unsigned long long)all);
             }
         }
         // Many entrants in some lane (the first chunks of a row block): sort
         // the chunk and merge it in, with the warp converged; few: insert
         // them one by one.
-        if (most >= 6u) {
+        if (most >= 9u) {
             // The chunk is not needed after this: sort it in place.
 #pragma unroll
             for (int j = 0; j < 32; j++) v[j] = ((want >> j) & 1u) ? v[j] : 0x7f800000u;
