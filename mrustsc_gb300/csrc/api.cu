@@ -286,6 +286,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
     const float* rerank_xs = nullptr;
     const float* rerank_theta = nullptr;
     int rerank_stride = 0;  // floats per row of rerank_xs
+    bool rerank_ids_only = false;  // the lists were filled by collect passes (ids, no values)
     if (tensor) {
         const bool bf16 = o.precision == SCRUST_PRECISION_BF16;
         void* A16 = ws_get(ctx, SLOT_A16, (size_t)n_pad * 64 * 2, &e);
@@ -352,6 +353,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
             // the final thresholds.  Larger k: the passes keep lists.
             const bool split = k <= 32;
             const int mode = split ? kPassThresholds : kPassFull;
+            rerank_ids_only = split;
             if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
                                               &first, false, order.theta, nullptr, ctx->d_stats, nullptr, mode)) !=
                 cudaSuccess)
@@ -437,8 +439,8 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
 
     const float* xr = ref ? xcentred : xwork;
     if ((e = launch_rerank(ctx, plan, xr, xr, norm2, norm2, norm64, norm64, x, x, bounds, lists, perm, rerank_xs,
-                           rerank_theta, out_idx, out_dist, nullptr, nullptr, nullptr, rerank_stride)) !=
-        cudaSuccess)
+                           rerank_theta, out_idx, out_dist, nullptr, nullptr, nullptr, rerank_stride,
+                           rerank_ids_only)) != cudaSuccess)
         return cuda_fail(st, e, "knn_rerank");
     mark(ctx, PH_RERANK);
     return ok(st);

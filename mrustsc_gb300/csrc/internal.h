@@ -289,7 +289,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
                           const uint32_t* perm, const float* xs, const float* theta, uint32_t* out_idx,
                           float* out_dist, const uint32_t* row_lo = nullptr, const uint32_t* row_hi = nullptr,
-                          const float* xr_list = nullptr, int xs_stride = 0);
+                          const float* xr_list = nullptr, int xs_stride = 0, bool ids_only = false);
 // order.cu: row blocks sorted by decreasing count (stable) into `order`;
 // `scratch` holds work_order_scratch(items) bytes.
 size_t work_order_scratch(int items);

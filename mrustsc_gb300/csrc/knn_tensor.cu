@@ -692,8 +692,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                 while (mask) {
                                     const int j = __ffs(mask) - 1;
                                     mask &= mask - 1;
-                                    ids[cnt] = (uint32_t)(col0 + 32 * c + j);
-                                    vals[cnt] = __int_as_float(0xff800000);
+                                    ids[cnt] = (uint32_t)(col0 + 32 * c + j);  // ids only: no values
                                     cnt++;
                                 }
                             }
@@ -760,8 +759,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                     const long long p0 = a.stats ? clock64() : 0;
                     n_prune += __popc(need);
                     if constexpr (TOPK > 0) {
+                        // A collected list holds only columns below its fixed
+                        // threshold (and no values): nothing to compact.
                         if (cnt >= (uint32_t)cap)
-                            take_prune(PruneResult{th, compact_lane(ids, vals, min(cnt, (uint32_t)a.lists.ctot), th)},
+                            take_prune(PruneResult{th, collect ? min(cnt, (uint32_t)a.lists.ctot)
+                                                               : compact_lane(ids, vals, min(cnt, (uint32_t)a.lists.ctot), th)},
                                        a, row, th, cnt, n_ovf);
                         __syncwarp();
                     } else {
@@ -784,7 +786,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                     n_prune += __popc(need);
                     if constexpr (TOPK > 0) {
                         if (cnt > (uint32_t)a.final_cap)
-                            take_prune(PruneResult{th, compact_lane(ids, vals, min(cnt, (uint32_t)a.lists.ctot), th)},
+                            take_prune(PruneResult{th, collect ? min(cnt, (uint32_t)a.lists.ctot)
+                                                               : compact_lane(ids, vals, min(cnt, (uint32_t)a.lists.ctot), th)},
                                        a, row, th, cnt, n_ovf);
                         __syncwarp();
                     } else {

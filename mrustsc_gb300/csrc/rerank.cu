@@ -41,6 +41,7 @@ struct RerankArgs {
     const uint32_t* perm;  // list row / list entry -> input row, or null
     const float* xs;       // working rows in list order (ordered solves), or null
     const float* xr_list;  // reference rows indexed by list entry (xs for a self solve)
+    int ids_only;          // the lists hold ids only (collected below their thresholds): keep every entry
     int xs_stride;         // floats per row of xs and xr_list
     int xs_v4;             // rows padded with zeros to a multiple of 4 floats, 16-byte aligned
     const uint32_t* row_lo;  // per input row: first row of its solve (a batch of solves), or null
@@ -288,7 +289,7 @@ __device__ int sorted_row(const RerankArgs& a, int64_t slot, unsigned long long*
                 if ((int64_t)id >= a.nr) {  // never written by a candidate kernel: refuse to read it
                     atomicExch(a.err + DERR_CANDIDATES, 1);
                 } else {
-                    keep = a.lists.vals[base + p] < theta;
+                    keep = a.ids_only || a.lists.vals[base + p] < theta;
                 }
             }
             const uint32_t ballot = __ballot_sync(0xffffffffu, keep);
@@ -374,7 +375,8 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
 #pragma unroll
             for (int r = 0; r < 2; ++r) {
                 sid[l][r] = a.lists.ids[base0 + l * (int64_t)a.lists.ctot + lane + 32 * r];
-                sval[l][r] = a.lists.vals[base0 + l * (int64_t)a.lists.ctot + lane + 32 * r];
+                sval[l][r] = a.ids_only ? __int_as_float(0xff800000)
+                                        : a.lists.vals[base0 + l * (int64_t)a.lists.ctot + lane + 32 * r];
             }
     }
     if (ovf) return 2;
@@ -424,7 +426,7 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
                 const int64_t at = base0 + list[r] * (int64_t)a.lists.ctot + pos[r];
                 have[r] = true;
                 eid[r] = a.lists.ids[at];
-                eval[r] = a.lists.vals[at];
+                eval[r] = a.ids_only ? __int_as_float(0xff800000) : a.lists.vals[at];
             }
         }
     }
@@ -716,7 +718,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
                           const uint32_t* perm, const float* xs, const float* theta, uint32_t* out_idx,
                           float* out_dist, const uint32_t* row_lo, const uint32_t* row_hi, const float* xr_list,
-                          int xs_stride) {
+                          int xs_stride, bool ids_only) {
     cudaError_t e;
     uint32_t* fb_rows = (uint32_t*)ws_get(ctx, SLOT_FALLBACK_ROWS, sizeof(uint32_t) * (size_t)plan.nq, &e);
     if (!fb_rows) return e;
@@ -738,6 +740,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.xs = xs;
     a.xr_list = xr_list ? xr_list : xs;
     a.xs_stride = xs_stride > 0 ? xs_stride : plan.d;
+    a.ids_only = ids_only ? 1 : 0;
     a.xs_v4 = !xr_list && xs && a.xs_stride % 4 == 0 && ((uintptr_t)xs & 15) == 0;
     a.theta = theta;
     a.row_lo = row_lo;

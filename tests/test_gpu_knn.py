@@ -199,6 +199,31 @@ def test_many_duplicates_take_the_fallback(scrust, oracle, form):
     assert idx[100].tolist() == list(range(101, 116))
 
 
+@pytest.mark.parametrize("k", [5, 15])
+def test_tie_groups_of_copies_and_mirror_pairs(scrust, oracle, k):
+    """Tie groups of both kinds, on a 1/16 lattice where every difference is
+    exact: mirror pairs r + e, r - e (equal distances from r, different rows:
+    ordered by FP64 then id) and triple copies (same rows: the sort's id order
+    and the FP32 value stand).  Every form gives the FP64 ids and the same
+    distance bits."""
+    g = np.random.default_rng(31)
+    x = (g.integers(-64, 64, size=(1200, 8)) / 16.0).astype(np.float32)
+    for r in range(40):
+        e = (g.integers(1, 4, size=8) / 64.0).astype(np.float32)
+        x[200 + 2 * r] = x[r] + e
+        x[201 + 2 * r] = x[r] - e
+    for r in range(40, 80):
+        x[400 + 3 * (r - 40):403 + 3 * (r - 40)] = x[r] + np.float32(1.0 / 32.0)
+    outs = {}
+    for form in FORMS:
+        idx, dist = scrust.knn(x, k, "auto", **kw(form))
+        assert_exact(oracle, x, k, idx, dist)
+        outs[form] = (idx, dist)
+    for form in FORMS[1:]:
+        np.testing.assert_array_equal(outs[form][0], outs["plain"][0])
+        np.testing.assert_array_equal(outs[form][1], outs["plain"][1])
+
+
 def test_knot_below_resolution_collapses_like_the_reference(scrust, oracle):
     x = refdata.audit_embedding(150, 8, 21)
     x[:10] = x[0] + np.float32(1e-7) * np.arange(10, dtype=np.float32)[:, None]
