@@ -170,6 +170,56 @@ __global__ void directed_kernel(const uint32_t* __restrict__ idx, const float* _
     }
 }
 
+// directed_kernel for k <= G (G = 16 or 32): G lanes per row, one neighbour
+// each.  A lane's place in the sorted row is the number of the row's kept
+// entries before it in (column, input position) order, found with G
+// shuffles; the same weights, the same stable order, no local memory.
+template <int G>
+__global__ void __launch_bounds__(256) directed_group_kernel(const uint32_t* __restrict__ idx,
+                                                             const float* __restrict__ dist, int64_t n, int k,
+                                                             const float* __restrict__ sigmas,
+                                                             const float* __restrict__ rhos,
+                                                             uint32_t* __restrict__ dcol, float* __restrict__ dw,
+                                                             uint32_t* __restrict__ dcnt,
+                                                             uint32_t* __restrict__ ekey,
+                                                             unsigned long long* __restrict__ eval) {
+    const int lane = threadIdx.x & 31;
+    const int g = lane / G, j = lane % G;
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const bool row_ok = i < n;
+    uint32_t nb = 0;
+    float wt = 0.f;
+    bool kept = false;
+    if (row_ok && j < k) {
+        nb = idx[i * k + j];
+        if ((int64_t)nb != i) {
+            const float sigma = sigmas[i], rho = rhos[i];
+            const float offset = __fsub_rn(dist[i * k + j], rho);
+            wt = (offset <= 0.f || sigma == 0.f) ? 1.0f : expf(__fdiv_rn(-offset, sigma));
+            kept = wt != 0.f;
+        }
+    }
+    const unsigned long long key = kept ? ((unsigned long long)nb << 32) | (uint32_t)j : ~0ull;
+    int rank = 0;
+#pragma unroll
+    for (int o = 0; o < G; ++o) rank += __shfl_sync(0xffffffffu, key, g * G + o) < key;
+    const uint32_t group_bits = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (G * g));
+    const int m = __popc(__ballot_sync(0xffffffffu, kept) & group_bits);
+    if (!row_ok) return;
+    if (j == 0) dcnt[i] = (uint32_t)m;
+    if (kept) {
+        const int64_t slot = i * k + rank;
+        dcol[slot] = nb;
+        dw[slot] = wt;
+        ekey[slot] = nb;
+        eval[slot] = ((unsigned long long)(uint32_t)i << 32) | __float_as_uint(wt);
+    }
+    if (j < k && j >= m) {  // unused slots sort last
+        ekey[i * k + j] = (uint32_t)n;
+        eval[i * k + j] = 0ull;
+    }
+}
+
 // Bucket starts of the edges sorted by target row: start[j] = the number of
 // keys below j, for j in [0, n] (keys are at most n; n marks unused slots).
 // Position p writes the starts of the rows in (key[p-1], key[p]]; the last
@@ -559,8 +609,15 @@ int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float
     unsigned long long* valB = valA + E;
 
     if ((e = launch_smooth_knn(ctx, dist, n, k, sig, rho)) != cudaSuccess) return cuda_fail(st, e, "smooth_knn");
-    directed_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(idx, dist, n, k, sig, rho, dcol, dw, dcnt, keyA,
-                                                                 valA);
+    if (k <= 16)
+        directed_group_kernel<16><<<(unsigned)((n * 16 + 255) / 256), 256, 0, s>>>(idx, dist, n, k, sig, rho, dcol,
+                                                                                  dw, dcnt, keyA, valA);
+    else if (k <= 32)
+        directed_group_kernel<32><<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(idx, dist, n, k, sig, rho, dcol,
+                                                                                  dw, dcnt, keyA, valA);
+    else
+        directed_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(idx, dist, n, k, sig, rho, dcol, dw, dcnt, keyA,
+                                                                     valA);
     scan_launches += 3 /* smooth_knn */ + 1 /* directed */ + 2 /* merges */;
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "directed weights");
     // Stable radix sort of the edge slots by target row.
