@@ -79,6 +79,14 @@ cudaError_t set_smem_limit(scrust_context* ctx, const void* func, int bytes) {
     return e;
 }
 
+cudaError_t set_smem_carveout(scrust_context* ctx, const void* func, int percent) {
+    for (const void* f : ctx->carveouts)
+        if (f == func) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+    if (e == cudaSuccess) ctx->carveouts.push_back(func);
+    return e;
+}
+
 bool encode_2d(scrust_context* ctx, CUtensorMap* map, CUtensorMapDataType dtype, void* base,
                uint64_t inner, uint64_t outer, uint64_t row_bytes, uint32_t box_inner,
                uint32_t box_outer, CUtensorMapSwizzle swizzle) {

@@ -95,6 +95,7 @@ struct scrust_context {
     cudaEvent_t ev[7] = {};             // phase boundaries: prep | candidates | rerank | connectivities,
     bool ev_recorded[7] = {};           // and inside candidates: first sweep pass | second-pass tile lists
     std::vector<std::pair<const void*, int>> smem_limits;  // dynamic shared memory limits already set
+    std::vector<const void*> carveouts;                      // kernels whose shared-memory carveout is set
 };
 
 struct scrust_csr {
@@ -132,6 +133,9 @@ int32_t cuda_fail(scrust_status* st, cudaError_t e, const char* what);
 // Raises a kernel's dynamic shared memory limit once per context (so that
 // launches can be captured into a CUDA graph afterwards).
 cudaError_t set_smem_limit(scrust_context* ctx, const void* func, int bytes);
+// Preferred shared-memory carveout (percent of the unified L1/shared memory),
+// set once per context and kernel.
+cudaError_t set_smem_carveout(scrust_context* ctx, const void* func, int percent);
 
 // Workspace access (may cudaMalloc; call with the context lock held).
 void* ws_get(scrust_context* ctx, Slot slot, size_t bytes, cudaError_t* err);

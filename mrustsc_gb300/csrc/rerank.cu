@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a
 // manifold in high dimension) is finished by a second pass with room for
 // RS_BIG_KEYS; beyond that, by the fallback.
 constexpr int RS_WARPS = 8;
-constexpr int RS_KEYS = 256;
+constexpr int RS_KEYS = 128;
 constexpr int RS_BIG_WARPS = 4;
 constexpr int RS_BIG_KEYS = 2048;
 
@@ -773,6 +773,11 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     if (xs && theta) {
         const size_t smem_s = (size_t)RS_WARPS * (2 * RS_KEYS * sizeof(unsigned long long) + RS_KEYS);
         const unsigned blocks = (unsigned)((plan.nq + RS_WARPS - 1) / RS_WARPS);
+        // Most rows need no shared memory (the register path): leave the rest
+        // of the SM's unified memory to L1, which caches the candidate rows
+        // that neighbouring rows share.
+        static_assert(RS_WARPS * (2 * RS_KEYS * 8 + RS_KEYS) <= 24 * 1024, "rerank block smem");
+        if ((e = set_smem_carveout(ctx, (const void*)rerank_sorted_kernel, 40)) != cudaSuccess) return e;
         rerank_sorted_kernel<<<blocks, RS_WARPS * 32, smem_s, ctx->stream>>>(a);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         const size_t smem_b = (size_t)RS_BIG_WARPS * (2 * RS_BIG_KEYS * sizeof(unsigned long long) + RS_BIG_KEYS);
