@@ -361,23 +361,21 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
     const int segs = a.lists.segments;
     if (segs > 32) return 3;
     // The row's header, its own coordinates and -- with two lists, the
-    // common case -- the first 64 slots of both lists are read at once (the
+    // common case -- the first 32 slots of both lists are read at once (the
     // lists hold at least 64 slots each); only then is anything tested.
+    // Slots 32..63 of a list are read only when it holds more than 32.
     const uint32_t ovf = a.lists.overflow[slot];
     const int cl = lane < segs ? (int)min(a.lists.cnt[slot * segs + lane], (uint32_t)a.lists.ctot) : 0;
     const float tl = lane < segs ? a.theta[slot * segs + lane] : __int_as_float(0x7f800000);
     const int64_t base0 = slot * segs * (int64_t)a.lists.ctot;
-    uint32_t sid[2][2];
-    float sval[2][2];
+    uint32_t sid[2][2] = {{0u, 0u}, {0u, 0u}};
+    float sval[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
     if (segs == 2) {
 #pragma unroll
-        for (int l = 0; l < 2; ++l)
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                sid[l][r] = a.lists.ids[base0 + l * (int64_t)a.lists.ctot + lane + 32 * r];
-                sval[l][r] = a.ids_only ? __int_as_float(0xff800000)
-                                        : a.lists.vals[base0 + l * (int64_t)a.lists.ctot + lane + 32 * r];
-            }
+        for (int l = 0; l < 2; ++l) {
+            sid[l][0] = a.lists.ids[base0 + l * (int64_t)a.lists.ctot + lane];
+            sval[l][0] = a.ids_only ? __int_as_float(0xff800000) : a.lists.vals[base0 + l * (int64_t)a.lists.ctot + lane];
+        }
     }
     if (ovf) return 2;
     float theta = tl;
@@ -391,6 +389,13 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
         const int c0 = __shfl_sync(0xffffffffu, cl, 0), c1 = __shfl_sync(0xffffffffu, cl, 1);
         m0 = c0 + c1;
         if (m0 > 64) return 3;
+#pragma unroll
+        for (int l = 0; l < 2; ++l)
+            if ((l == 0 ? c0 : c1) > 32) {
+                sid[l][1] = a.lists.ids[base0 + l * (int64_t)a.lists.ctot + lane + 32];
+                sval[l][1] = a.ids_only ? __int_as_float(0xff800000)
+                                        : a.lists.vals[base0 + l * (int64_t)a.lists.ctot + lane + 32];
+            }
         // Position e = lane + 32 r: list 0 slot e below c0, else list 1 slot e - c0.
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
