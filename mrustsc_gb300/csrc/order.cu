@@ -561,31 +561,33 @@ __global__ void __launch_bounds__(256) tile_lists_kernel(const uint32_t* __restr
 
 // Operand rows (128 bytes each) and their per-row terms moved into list
 // order; padding rows are zero like the operand kernel writes them.
+// Eight lanes per row: lane q of a row copies the row's q-th 16-byte word of
+// A and B (a warp writes four whole 128-byte rows at a time).
 __global__ void gather_operands_kernel(const uint4* __restrict__ A0, const uint4* __restrict__ B0,
                                        const float* __restrict__ bA0, const float* __restrict__ eps0,
                                        const uint32_t* __restrict__ perm, int64_t n, int64_t n_pad,
                                        uint4* __restrict__ A16, uint4* __restrict__ B16, float* __restrict__ bA,
                                        float* __restrict__ eps) {
-    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t s = t >> 3;
+    const int q = (int)(t & 7);
     if (s >= n_pad) return;
-    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
     if (s < n) {
         const int64_t r = perm[s];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            A16[s * 8 + q] = A0[r * 8 + q];
-            B16[s * 8 + q] = B0[r * 8 + q];
+        A16[s * 8 + q] = A0[r * 8 + q];
+        B16[s * 8 + q] = B0[r * 8 + q];
+        if (q == 0) {
+            bA[s] = bA0[r];
+            eps[s] = eps0[r];
         }
-        bA[s] = bA0[r];
-        eps[s] = eps0[r];
     } else {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            A16[s * 8 + q] = z;
-            B16[s * 8 + q] = z;
+        const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+        A16[s * 8 + q] = z;
+        B16[s * 8 + q] = z;
+        if (q == 0) {
+            bA[s] = 0.f;
+            eps[s] = 0.f;
         }
-        bA[s] = 0.f;
-        eps[s] = 0.f;
     }
 }
 
@@ -604,9 +606,23 @@ __global__ void narrow_kernel(const unsigned long long* __restrict__ vals, int i
     if (i < items) out[i] = (uint32_t)vals[i];
 }
 
+// One thread per 4-float group of an output row (stride is a multiple of 4
+// for the padded layout; otherwise one float per thread).
 __global__ void gather_rows_kernel(const float* __restrict__ x, const uint32_t* __restrict__ perm, int64_t n, int d,
                                    int stride, float* __restrict__ xs) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((stride & 3) == 0) {
+        const int groups = stride >> 2;
+        if (i >= n * groups) return;
+        const int64_t s = i / groups;
+        const int t0 = (int)(i - s * groups) * 4;
+        const uint32_t r = perm[s];
+        float v[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) v[e] = (r == 0xffffffffu || t0 + e >= d) ? 0.f : x[(int64_t)r * d + t0 + e];
+        reinterpret_cast<float4*>(xs + s * stride)[t0 >> 2] = make_float4(v[0], v[1], v[2], v[3]);
+        return;
+    }
     if (i >= n * stride) return;
     const int64_t s = i / stride, t = i % stride;
     const uint32_t r = perm[s];
@@ -652,7 +668,8 @@ cudaError_t sort_by_work(scrust_context* ctx, const uint32_t* counts, int items,
 
 cudaError_t launch_gather_rows(const float* x, const uint32_t* perm, int64_t n, int d, int stride, float* xs,
                                cudaStream_t s) {
-    gather_rows_kernel<<<(unsigned)((n * stride + 255) / 256), 256, 0, s>>>(x, perm, n, d, stride, xs);
+    const int64_t threads = (stride & 3) == 0 ? n * (stride >> 2) : n * stride;
+    gather_rows_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(x, perm, n, d, stride, xs);
     return cudaGetLastError();
 }
 
@@ -795,7 +812,7 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     if ((e = sort_by_work(ctx, prio_cnt, items, base + o_ws, (uint32_t*)(base + o_po))) != cudaSuccess)
         return cuda_fail(st, e, "ordering: work order");
     // The operands in list order (bounds follow in the caller).
-    gather_operands_kernel<<<(unsigned)((n_pad + 127) / 128), 128, 0, s>>>(
+    gather_operands_kernel<<<(unsigned)((n_pad * 8 + 255) / 256), 256, 0, s>>>(
         (const uint4*)A0, (const uint4*)B0, bA0, eps0, perm, n, n_pad, (uint4*)A16, (uint4*)B16, bA, beps);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: operands");
     ctx->launches += 1;
