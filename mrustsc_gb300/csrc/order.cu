@@ -298,6 +298,17 @@ __global__ void prio_tiles_kernel(const uint32_t* __restrict__ cell_of_pos, int6
 
 __device__ __forceinline__ float op_float(__half v) { return __half2float(v); }
 __device__ __forceinline__ float op_float(__nv_bfloat16 v) { return __bfloat162float(v); }
+// A 16-bit operand value from the low half of a word.
+template <class T>
+__device__ __forceinline__ float op_bits(uint32_t w);
+template <>
+__device__ __forceinline__ float op_bits<__half>(uint32_t w) {
+    return __half2float(__ushort_as_half((unsigned short)(w & 0xffffu)));
+}
+template <>
+__device__ __forceinline__ float op_bits<__nv_bfloat16>(uint32_t w) {
+    return __bfloat162float(__ushort_as_bfloat16((unsigned short)(w & 0xffffu)));
+}
 
 // Balls of one tile: the whole tile and each of its cell segments (runs of
 // rows of one cell; a cell lies in one region of the data, while a tile
@@ -336,6 +347,16 @@ __global__ void __launch_bounds__(256) tile_balls_kernel(const T* __restrict__ o
     const bool valid = j < n;
     const int rows = (int)min((int64_t)256, n - (int64_t)tile * 256);
     const T* row = ops + j * 64;
+    // The row's 64 16-bit values, read once as eight 16-byte words.
+    uint32_t rw[32];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const uint4 u = valid ? reinterpret_cast<const uint4*>(row)[q] : make_uint4(0u, 0u, 0u, 0u);
+        rw[4 * q] = u.x;
+        rw[4 * q + 1] = u.y;
+        rw[4 * q + 2] = u.z;
+        rw[4 * q + 3] = u.w;
+    }
     // Segment of each row: the number of run heads at or before it, less one.
     const bool head = valid && (threadIdx.x == 0 || cell_of_pos[j] != cell_of_pos[j - 1]);
     const uint32_t hb = __ballot_sync(0xffffffffu, head);
@@ -358,10 +379,13 @@ __global__ void __launch_bounds__(256) tile_balls_kernel(const T* __restrict__ o
     const int seg = min(before + __popc(hb & lanemask_lt()) + (head ? 1 : 0) - 1, kSegMax - 1);
     if (head && seg == before + __popc(hb & lanemask_lt())) sstart[seg] = threadIdx.x;
     if (threadIdx.x == 0) sstart[nseg] = rows;
-    for (int t = 0; t < d; ++t) {
-        float v = valid ? op_float(row[t]) : 0.f;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) part[w][t] = v;
+#pragma unroll
+    for (int t = 0; t < 64; ++t) {
+        if (t < d) {
+            float v = valid ? op_bits<T>(rw[t >> 1] >> (16 * (t & 1))) : 0.f;
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) part[w][t] = v;
+        }
     }
     __syncthreads();
     if (threadIdx.x < d) {
@@ -385,11 +409,14 @@ __global__ void __launch_bounds__(256) tile_balls_kernel(const T* __restrict__ o
         // the last place below the exact value, so scaling by
         // 1 + (d + 4) 2^-23 (rounded up) bounds it from above.
         float r2 = 0.f, s2 = 0.f;
-        for (int t = 0; t < d; ++t) {
-            const float v = op_float(row[t]);
-            const float df = v - centre[t], ds = v - scentre[seg][t];
-            r2 = fmaf(df, df, r2);
-            s2 = fmaf(ds, ds, s2);
+#pragma unroll
+        for (int t = 0; t < 64; ++t) {
+            if (t < d) {
+                const float v = op_bits<T>(rw[t >> 1] >> (16 * (t & 1)));
+                const float df = v - centre[t], ds = v - scentre[seg][t];
+                r2 = fmaf(df, df, r2);
+                s2 = fmaf(ds, ds, s2);
+            }
         }
         const float grow = 1.0f + (float)(d + 4) * 1.1920929e-07f;
         r2 = __fmul_ru(r2, grow);
