@@ -49,8 +49,8 @@ __global__ void anchors_kernel(const float* __restrict__ x, int d, int64_t n, in
 // diagonal is +inf.
 __global__ void __launch_bounds__(256) anchor_dist_kernel(const float* __restrict__ anc, int m, int d,
                                                           float* __restrict__ dist) {
-    __shared__ __align__(16) float As[64][64];
-    __shared__ __align__(16) float Bs[64][64];
+    __shared__ __align__(16) float As[64][64 + 4];  // padded as in segment_pairs_kernel
+    __shared__ __align__(16) float Bs[64][64 + 4];
     const int i0 = blockIdx.y * 64, j0 = blockIdx.x * 64;
     const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
     float acc[4][4] = {};
@@ -486,8 +486,10 @@ __global__ void __launch_bounds__(256) segment_pairs_kernel(const float* __restr
                                                             const uint32_t* __restrict__ fo,
                                                             const uint32_t* __restrict__ S_ptr, int d, int words,
                                                             uint32_t* __restrict__ bitmap) {
-    __shared__ __align__(16) float As[64][SP];
-    __shared__ __align__(16) float Bs[64][SP];
+    // Rows padded by 4 floats: the transposing stores (consecutive t, same
+    // r) then spread over 8 banks instead of one; float4 reads stay aligned.
+    __shared__ __align__(16) float As[64][SP + 4];
+    __shared__ __align__(16) float Bs[64][SP + 4];
     const int S = (int)*S_ptr;
     const int nb = (S + SP - 1) / SP;
     const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
