@@ -327,10 +327,11 @@ __device__ __forceinline__ float topk_chunk(uint32_t (&v)[32], int64_t colbase, 
                     if ((valid >> j) & 1u) mv = fminf(mv, f_of(v[j]));
             }
             if (mv < top.v[0]) {
-                int jj = 0;
+                // The first valid column holding the minimum.
+                uint32_t eq = 0;
 #pragma unroll
-                for (int j = 31; j >= 0; j--)
-                    if (((valid >> j) & 1u) && f_of(v[j]) == mv) jj = j;
+                for (int j = 0; j < 32; j++) eq |= (f_of(v[j]) == mv) ? (1u << j) : 0u;
+                const int jj = __ffs(eq & valid) - 1;
                 top.v[0] = mv;
                 best = (uint32_t)(colbase + jj);
                 if (keep_threshold) th = fminf(th, bnd.theta_f32(mv));
