@@ -348,7 +348,6 @@ __device__ __forceinline__ float topk_chunk(uint32_t (&v)[32], int64_t colbase, 
 #pragma unroll
         for (int j = 0; j < 32; j++) want |= (f_of(v[j]) < lim) ? (1u << j) : 0u;
         want &= valid;
-        const float old = top.kth();
         const uint32_t most = __reduce_max_sync(0xffffffffu, (uint32_t)__popc(want));
         if (a.stats) {
             const uint32_t all = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(want));
@@ -376,8 +375,8 @@ __device__ __forceinline__ float topk_chunk(uint32_t (&v)[32], int64_t colbase, 
                 if (x < top.kth()) top.insert(x);
             }
         }
-        const float kth = top.kth();
-        if (kth < old) th = fminf(th, bnd.theta_f32(kth));
+        // (The threshold follows the k-th smallest once per tile, in the
+        // caller: its f32 bound costs a directed square root.)
     }
     return m;
 }
@@ -699,6 +698,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             }
                         }
                     } else if constexpr (TOPK <= 16) {
+                        const float kth0 = top.kth();
                         uint32_t vb[32];
                         tmem_ld32(tbase, va);
                         tmem_ld_wait(va);
@@ -712,14 +712,17 @@ __global__ void __launch_bounds__(THREADS, 1)
                         cm[2] = topk_chunk(va, col0 + 64, th, row, a, top, bnd, best, !argmin);
                         tmem_ld_wait(vb);
                         cm[3] = topk_chunk(vb, col0 + 96, th, row, a, top, bnd, best, !argmin);
+                        if (TOPK > 1 && top.kth() < kth0) th = fminf(th, bnd.theta_f32(top.kth()));
                     } else {
                         // A top-32 leaves no registers for a second chunk in flight.
+                        const float kth0 = top.kth();
 #pragma unroll
                         for (int c = 0; c < 4; ++c) {
                             tmem_ld32(tbase + 32 * c, va);
                             tmem_ld_wait(va);
                             cm[c] = topk_chunk(va, col0 + 32 * c, th, row, a, top, bnd, best, !argmin);
                         }
+                        if (top.kth() < kth0) th = fminf(th, bnd.theta_f32(top.kth()));
                     }
                     const unsigned long long o2 = ld_shared_volatile_u64(other_th);
                     if ((o2 & 0xffffffff00000000ull) == tag) th = fminf(th, __uint_as_float((uint32_t)o2));
