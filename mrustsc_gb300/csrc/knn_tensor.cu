@@ -29,6 +29,13 @@
 // The two accumulators ping-pong: the epilogue drains half 0 of tile j while
 // the tensor core computes half 1 of tile j, so each B tile is read once per
 // 256 query rows.  Every wait is bounded (tma.cuh).
+//
+// The kernel is compiled once per (top-k size, pass kind).  PASS 1 only
+// tightens thresholds with a register top-k, PASS 2 only collects ids below
+// fixed thresholds, PASS 3 keeps each row's nearest column (no lists), and
+// PASS 0 takes the kind from its arguments.  A specialised pass carries none
+// of the others' code, which matters because the epilogue is held to 96
+// registers (18 warps on an SM) and its ALU pipe is the bottleneck.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
