@@ -119,6 +119,32 @@ def test_neighbors_graph_in_one_pass(scrust, oracle):
     assert_same_csr(conn, oracle.connectivities(idx, dist))
 
 
+def test_host_graphs_held_and_freed_out_of_order(scrust, oracle):
+    """Several downloaded graphs alive at once, of growing and shrinking
+    sizes, freed in another order than made: each handle keeps its own host
+    arrays (pinned slabs taken from and returned to the library's pool)."""
+    import ctypes
+
+    from mrustsc_gb300 import _lib
+
+    L = _lib.lib()
+    ctx = _lib.context(0)
+    opts = _lib.options(form="tensor")
+    st = _lib.Status()
+    handles, refs = [], []
+    for n in (3000, 900, 5000, 900):
+        x = synthetic.mixture(n, 30, clusters=5, dup_frac=0.01, seed=n)
+        idx = np.empty((n, 15), np.uint32)
+        dist = np.empty((n, 15), np.float32)
+        out = ctypes.c_void_p()
+        _lib.check(L.scrust_cuda_neighbors_graph(ctx, _lib.ptr(x), n, 30, 15, ctypes.byref(opts), _lib.ptr(idx),
+                                                 _lib.ptr(dist), ctypes.byref(out), ctypes.byref(st)), st)
+        handles.append(out)
+        refs.append(oracle.connectivities(idx, dist))
+    for i in (1, 3, 0, 2):
+        assert_same_csr(_lib.csr_host_arrays(handles[i]), refs[i])
+
+
 def test_pp_neighbors_end_to_end(oracle):
     from mrustsc_gb300 import pp
     from mrustsc_gb300.anndata_lite import AnnData
