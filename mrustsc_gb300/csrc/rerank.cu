@@ -567,7 +567,7 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
     return 0;
 }
 
-__global__ void __launch_bounds__(RS_WARPS * 32) rerank_sorted_kernel(RerankArgs a) {
+__global__ void __launch_bounds__(RS_WARPS * 32, 6) rerank_sorted_kernel(RerankArgs a) {
     extern __shared__ unsigned long long rs_smem[];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -782,7 +782,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
         // of the SM's unified memory to L1, which caches the candidate rows
         // that neighbouring rows share.
         static_assert(RS_WARPS * (2 * RS_KEYS * 8 + RS_KEYS) <= 24 * 1024, "rerank block smem");
-        if ((e = set_smem_carveout(ctx, (const void*)rerank_sorted_kernel, 40)) != cudaSuccess) return e;
+        if ((e = set_smem_carveout(ctx, (const void*)rerank_sorted_kernel, 50)) != cudaSuccess) return e;
         rerank_sorted_kernel<<<blocks, RS_WARPS * 32, smem_s, ctx->stream>>>(a);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         const size_t smem_b = (size_t)RS_BIG_WARPS * (2 * RS_BIG_KEYS * sizeof(unsigned long long) + RS_BIG_KEYS);
