@@ -296,9 +296,11 @@ SCRUST_API int32_t scrust_cuda_phase_times(scrust_context* context, float* ms, i
 /* Kernel counters (observability).  enable = 1 turns collection on (later
  * calls accumulate), enable = 0 turns it off.  Writes up to max_words
  * counters accumulated since the previous read and resets them; returns how
- * many it wrote.  For the tensor form: appends, prunes, overflow rows,
- * epilogue wait / busy cycles, MMA wait cycles (B tiles, accumulators),
- * producer wait cycles, tiles, prune cycles. */
+ * many it wrote.  For the tensor form, by index: 0 appends, 1 prunes,
+ * 2 overflow rows, 3 epilogue wait cycles, 5/6 MMA wait cycles (B tiles,
+ * accumulators), 7 producer wait cycles, 8 tiles, 9 prune cycles, and for the
+ * register top-k 12 chunks with an entrant, 13 bulk merges, 14 insertion
+ * rounds, 15 entrants; 4, 10 and 11 are unused. */
 SCRUST_API int32_t scrust_cuda_kernel_stats(scrust_context* context, int32_t enable, uint64_t* out,
                                             int32_t max_words);
 

@@ -109,15 +109,14 @@ enum TensorStat : int {
     TS_APPENDS = 0,        // candidates appended to lists
     TS_PRUNES = 1,         // warp-cooperative prunes
     TS_OVERFLOWS = 2,      // rows sent to the exact fallback
-    TS_EPI_WAIT = 3,       // epilogue cycles waiting for an accumulator (lane 0 of each warp)
-    TS_EPI_BUSY = 4,       // epilogue cycles draining accumulators
+    TS_EPI_WAIT = 3,       // epilogue cycles waiting for an accumulator (lane 0 of each warp; PASS 0 only)
+    // 4: unused (always 0)
     TS_MMA_WAIT_FULL = 5,  // MMA issuer cycles waiting for B tiles
     TS_MMA_WAIT_EMPTY = 6, // MMA issuer cycles waiting for a drained accumulator
     TS_TMA_WAIT = 7,       // producer cycles waiting for a free stage
     TS_TILES = 8,          // (work item, B tile) pairs
     TS_PRUNE_CYCLES = 9,   // epilogue cycles spent in prunes
-    TS_LD_CYCLES = 10,     // epilogue cycles from issuing TMEM loads to their completion
-    TS_APPEND_CALLS = 11,  // 32-column chunks that had survivors in some lane (per warp)
+    // 10, 11: unused (always 0)
     TS_TOPK_ENTER = 12,    // register top-k: 32-column chunks with an entrant in some lane (per warp)
     TS_TOPK_BULK = 13,     // register top-k: chunks sorted and merged in bulk (per warp)
     TS_TOPK_INSERTS = 14,  // register top-k: one-by-one insertion rounds (per warp)
