@@ -158,7 +158,8 @@ SCRUST_API int32_t scrust_cuda_connectivities_device(scrust_context* context, co
                                           const float* distances, uint64_t n, uint32_t k,
                                           scrust_csr** out, scrust_status* status);
 
-/* Per-row sigma and rho of umap's smooth_knn_dist (host pointers). */
+/* Per-row sigma and rho of umap's smooth_knn_dist (host pointers), the
+ * global mean summed in the reference's own f32 order. */
 SCRUST_API int32_t scrust_cuda_smooth_knn_distances(scrust_context* context, const float* distances,
                                          uint64_t n, uint32_t k, float* sigmas, float* rhos,
                                          scrust_status* status);
@@ -199,11 +200,18 @@ SCRUST_API int32_t scrust_cuda_synchronize(scrust_context* context, scrust_statu
  * `sigmas` and `rhos` (n).  The computation's only scratch is a fixed 33 KB
  * array compiled into the library (held by every GPU that loads it until the
  * process exits), so n * k is limited to 16,777,216; larger inputs return
- * SCRUST_INVALID_PARAMETER.  Enqueued on `stream` (a cudaStream_t; NULL is
- * the legacy default stream) without synchronising.  The first call on each
- * device looks up the array's device address, so make it before any stream
- * capture.  All calls on a device share the array: calls that overlap on the
- * GPU race on it and must be ordered by the caller. */
+ * SCRUST_INVALID_PARAMETER.  The work runs on the GPU that holds the three
+ * buffers (buffers on different GPUs, or in host memory, return
+ * SCRUST_INVALID_PARAMETER), enqueued on `stream` (a cudaStream_t of that
+ * GPU; NULL is its legacy default stream) without synchronising; the calling
+ * thread's current device is left as it was.  The first call on each device
+ * looks up the array's device address and keeps it for the process's life,
+ * so make that call before any stream capture and do not use the entry point
+ * across a cudaDeviceReset.  All calls on a device share the array: calls
+ * that overlap on the GPU race on it and must be ordered by the caller.  The
+ * global mean (the sigma floor of rows whose neighbours all sit at distance
+ * 0) is an FP64 sum here, within a few 1e-6 relative of the reference's f32
+ * sum that scrust_cuda_smooth_knn_distances reproduces. */
 SCRUST_API int32_t scrust_cuda_smooth_knn_distances_noalloc(const float* distances, uint64_t n, uint32_t k,
                                                             float* sigmas, float* rhos, void* stream,
                                                             scrust_status* status);

@@ -649,7 +649,9 @@ scrust_context* scrust_cuda_context_create(int32_t device, scrust_status* st) {
         fail(st, SCRUST_NO_GPU, "CUDA device %d is not compute capability 10.3 (sm_103a)", device);
         return nullptr;
     }
-    if (cudaSetDevice(device) != cudaSuccess) {
+    DeviceGuard device_guard(device);
+    int current = -1;
+    if (cudaGetDevice(&current) != cudaSuccess || current != device) {
         cudaGetLastError();
         fail(st, SCRUST_NO_GPU, "cannot select CUDA device %d", device);
         return nullptr;
@@ -689,7 +691,7 @@ scrust_context* scrust_cuda_context_create(int32_t device, scrust_status* st) {
 
 void scrust_cuda_context_destroy(scrust_context* ctx) {
     if (!ctx) return;
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (int i = 0; i < SLOT_COUNT; i++)
         if (ctx->ws.ptr[i]) cudaFree(ctx->ws.ptr[i]);
@@ -726,7 +728,7 @@ int32_t scrust_cuda_knn_device(scrust_context* ctx, const float* x, uint64_t n, 
     if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
     if (!x || !out_idx || !out_dist) return fail(st, SCRUST_SHAPE, "expected non-null device pointers");
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     return knn_device_impl(ctx, x, n, d, k, opt, out_idx, out_dist, st);
 }
 
@@ -738,7 +740,7 @@ int32_t scrust_cuda_knn(scrust_context* ctx, const float* x, uint64_t n, uint64_
     if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
     if (!x || !out_idx || !out_dist) return fail(st, SCRUST_SHAPE, "expected non-null host pointers");
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaError_t e;
     float* dx = (float*)ws_get(ctx, SLOT_HOST_IN, sizeof(float) * n * d, &e);
     uint32_t* di = (uint32_t*)ws_get(ctx, SLOT_HOST_IDX, sizeof(uint32_t) * n * k, &e);
@@ -765,7 +767,7 @@ int32_t scrust_cuda_connectivities_device(scrust_context* ctx, const uint32_t* i
     if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
     if (!idx || !dist || !out) return fail(st, SCRUST_SHAPE, "expected non-null pointers");
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     return conn_device_impl(ctx, idx, dist, n, k, true, out, st);
 }
 
@@ -783,7 +785,7 @@ int32_t scrust_cuda_connectivities(scrust_context* ctx, const uint32_t* idx, con
                         (unsigned long long)n);
     if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaError_t e;
     uint32_t* di = (uint32_t*)ws_get(ctx, SLOT_HOST_IDX, sizeof(uint32_t) * n * k, &e);
     float* dd = (float*)ws_get(ctx, SLOT_HOST_DIST, sizeof(float) * n * k, &e);
@@ -809,14 +811,14 @@ int32_t scrust_cuda_smooth_knn_distances(scrust_context* ctx, const float* dist,
     if (!dist || !sigmas || !rhos) return fail(st, SCRUST_SHAPE, "expected non-null pointers");
     if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaError_t e;
     float* dd = (float*)ws_get(ctx, SLOT_HOST_DIST, sizeof(float) * n * k, &e);
     float* so = (float*)ws_get(ctx, SLOT_CONN_G, sizeof(float) * 2 * n, &e);
     if (!dd || !so) return cuda_fail(st, e, "workspace");
     if ((e = cudaMemcpyAsync(dd, dist, sizeof(float) * n * k, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
         return cuda_fail(st, e, "upload");
-    if ((e = launch_smooth_knn(ctx, dd, (int64_t)n, (int)k, so, so + n)) != cudaSuccess)
+    if ((e = launch_smooth_knn(ctx, dd, (int64_t)n, (int)k, so, so + n, true)) != cudaSuccess)
         return cuda_fail(st, e, "smooth_knn");
     if ((e = cudaMemcpyAsync(sigmas, so, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
         (e = cudaMemcpyAsync(rhos, so + n, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess)
@@ -833,7 +835,7 @@ int32_t scrust_cuda_neighbors_graph_device(scrust_context* ctx, const float* x, 
     if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
     if (!x || !out_idx || !out_dist || !conn) return fail(st, SCRUST_SHAPE, "expected non-null pointers");
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     if ((rc = knn_device_impl(ctx, x, n, d, k, opt, out_idx, out_dist, st))) return rc;
     return conn_device_impl(ctx, out_idx, out_dist, n, k, false, conn, st);
 }
@@ -847,7 +849,7 @@ int32_t scrust_cuda_neighbors_graph(scrust_context* ctx, const float* x, uint64_
     if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
     if (!x || !out_idx || !out_dist || !conn) return fail(st, SCRUST_SHAPE, "expected non-null pointers");
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaError_t e;
     float* dx = (float*)ws_get(ctx, SLOT_HOST_IN, sizeof(float) * n * d, &e);
     uint32_t* di = (uint32_t*)ws_get(ctx, SLOT_HOST_IDX, sizeof(uint32_t) * n * k, &e);
@@ -889,7 +891,7 @@ int32_t scrust_cuda_neighbors_graph(scrust_context* ctx, const float* x, uint64_
 int32_t scrust_cuda_synchronize(scrust_context* ctx, scrust_status* st) {
     if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     return collect_device_errors(ctx, st);
 }
 
@@ -903,7 +905,7 @@ uint64_t scrust_csr_nnz(const scrust_csr* c) {
     scrust_csr* m = const_cast<scrust_csr*>(c);
     if (c->owner) {
         std::lock_guard<std::mutex> lock(c->owner->mu);
-        cudaSetDevice(c->owner->device);
+        DeviceGuard device_guard(c->owner->device);
         if (cudaMemcpyAsync(&nnz, c->buf.indptr + c->n_rows, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                             c->owner->stream) == cudaSuccess &&
             cudaStreamSynchronize(c->owner->stream) == cudaSuccess)
@@ -941,7 +943,7 @@ void scrust_cuda_set_timing(scrust_context* ctx, int32_t enable) {
 int32_t scrust_cuda_phase_times(scrust_context* ctx, float* ms, int32_t max_phases) {
     if (!ctx || !ms) return 0;
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
         cudaGetLastError();
         return 0;
@@ -979,7 +981,7 @@ uint64_t scrust_cuda_launch_count(const scrust_context* ctx) { return ctx ? ctx-
 int32_t scrust_cuda_kernel_stats(scrust_context* ctx, int32_t enable, uint64_t* out, int32_t max_words) {
     if (!ctx) return 0;
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     if (enable && !ctx->d_stats) {
         if (cudaMalloc(&ctx->d_stats, 16 * sizeof(unsigned long long)) != cudaSuccess) {
             cudaGetLastError();

@@ -260,7 +260,7 @@ int32_t scrust_cuda_knn_batch_device(scrust_context* ctx, const float* x, const 
     scrust_knn_options_default(&o);
     if (opt) o = *opt;
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaError_t e;
     void* table = ws_get(ctx, SLOT_BATCH_TABLE, sizeof(SampleRow) * rows.size(), &e);
     if (!table) return cuda_fail(st, e, "workspace");
@@ -286,7 +286,7 @@ int32_t scrust_cuda_knn_batch(scrust_context* ctx, const float* x, const uint64_
     float* dd;
     {
         std::lock_guard<std::mutex> lock(ctx->mu);
-        cudaSetDevice(ctx->device);
+        DeviceGuard device_guard(ctx->device);
         cudaError_t e;
         dx = (float*)ws_get(ctx, SLOT_HOST_IN, sizeof(float) * (size_t)n_total * d, &e);
         di = (uint32_t*)ws_get(ctx, SLOT_HOST_IDX, sizeof(uint32_t) * (size_t)n_total * k, &e);
@@ -298,7 +298,7 @@ int32_t scrust_cuda_knn_batch(scrust_context* ctx, const float* x, const uint64_
     }
     if ((rc = scrust_cuda_knn_batch_device(ctx, dx, row_offsets, n_samples, d, k, opt, di, dd, st))) return rc;
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaError_t e;
     if ((e = cudaMemcpyAsync(out_idx, di, sizeof(uint32_t) * (size_t)n_total * k, cudaMemcpyDeviceToHost,
                              ctx->stream)) != cudaSuccess ||
@@ -339,7 +339,7 @@ scrust_batch_plan* scrust_cuda_batch_plan_create(scrust_context* ctx, const uint
     p->out_idx = out_idx;
     p->out_dist = out_dist;
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaError_t e = cudaMalloc(&p->table, sizeof(SampleRow) * rows.size());
     if (e == cudaSuccess)
         e = cudaMemcpy(p->table, rows.data(), sizeof(SampleRow) * rows.size(), cudaMemcpyHostToDevice);
@@ -426,7 +426,7 @@ scrust_batch_plan* scrust_cuda_batch_plan_create(scrust_context* ctx, const uint
 int32_t scrust_cuda_batch_plan_launch(scrust_batch_plan* p, scrust_status* st) {
     if (!p) return fail(st, SCRUST_SHAPE, "expected a batch plan");
     std::lock_guard<std::mutex> lock(p->ctx->mu);
-    cudaSetDevice(p->ctx->device);
+    DeviceGuard device_guard(p->ctx->device);
     const cudaError_t e = cudaGraphLaunch(p->exec, p->ctx->stream);
     if (e != cudaSuccess) return cuda_fail(st, e, "batch plan: launch");
     p->ctx->launches += 1;
@@ -446,7 +446,7 @@ void scrust_cuda_batch_plan_destroy(scrust_batch_plan* p) {
     if (!p) return;
     {
         std::lock_guard<std::mutex> lock(p->ctx->mu);
-        cudaSetDevice(p->ctx->device);
+        DeviceGuard device_guard(p->ctx->device);
         cudaStreamSynchronize(p->ctx->stream);
         if (p->exec) cudaGraphExecDestroy(p->exec);
         if (p->graph) cudaGraphDestroy(p->graph);

@@ -9,8 +9,8 @@
 // Every f32 operation is written with explicit round-to-nearest intrinsics so
 // nothing is contracted into an fma, matching the reference's uncontracted Rust
 // arithmetic; exp is CUDA's expf.  Sums of a row use ndarray 0.16.1's
-// unrolled_fold order (crates/scrust-core/src/neighbors.rs:248,290); the global
-// mean is an FP64 sum rounded to f32.
+// unrolled_fold order (crates/scrust-core/src/neighbors.rs:248,290), the global
+// mean included (unrolled_mean_kernel).
 #include <math.h>
 
 #include <algorithm>
@@ -53,30 +53,66 @@ __global__ void check_ids_kernel(const uint32_t* __restrict__ idx, int64_t total
         if ((int64_t)idx[i] >= n) atomicExch(err + DERR_BAD_INDEX, 1);
 }
 
-__global__ void sum_partial_kernel(const float* __restrict__ x, int64_t total, double* __restrict__ partial) {
-    __shared__ double ws[32];
-    double s = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (int64_t)gridDim.x * blockDim.x)
-        s += (double)x[i];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += ws[w];
-        partial[blockIdx.x] = t;
+// The global mean distance of crates/scrust-core/src/neighbors.rs:248,
+// `distances.sum() / (n * k) as f32`, in the reference's own rounding: ndarray
+// 0.16.1 sums a contiguous array with unrolled_fold, eight sequential f32
+// chains over the elements i = j (mod 8) of the first 8 * floor(len / 8),
+// combined as ((p0+p4), (p1+p5), (p2+p6), (p3+p7)) into the accumulator, then
+// the tail added in order.  Eight dependent chains cannot be split without
+// changing the rounding, so one block runs them: lanes 0..7 of warp 0 add
+// from shared memory while the other warps stage the next tile.
+constexpr int FOLD_THREADS = 256;
+constexpr int FOLD_TILE = 8192;  // floats per staged tile; two tiles of shared memory
+constexpr size_t FOLD_SMEM_BYTES = sizeof(float) * 2 * FOLD_TILE;
+
+__device__ __forceinline__ void fold_stage(const float* __restrict__ x, int64_t t0, int cnt, float* dst, int tid,
+                                           int nthreads, bool vec) {
+    if (vec) {
+        const int c4 = cnt >> 2;
+        const float4* src = reinterpret_cast<const float4*>(x + t0);
+        float4* d4 = reinterpret_cast<float4*>(dst);
+        for (int i = tid; i < c4; i += nthreads) d4[i] = __ldg(src + i);
+        for (int i = (c4 << 2) + tid; i < cnt; i += nthreads) dst[i] = __ldg(x + t0 + i);
+    } else {
+        for (int i = tid; i < cnt; i += nthreads) dst[i] = __ldg(x + t0 + i);
     }
 }
 
-// One warp: strided f64 sums of the block partials, then a fixed tree.
-__global__ void mean_final_kernel(const double* __restrict__ partial, int blocks, int64_t total,
-                                  float* __restrict__ mean) {
-    double t = 0.0;
-    for (int b = threadIdx.x; b < blocks; b += 32) t += partial[b];
+__global__ void __launch_bounds__(FOLD_THREADS) unrolled_mean_kernel(const float* __restrict__ x, int64_t len,
+                                                                     float* __restrict__ mean) {
+    extern __shared__ float fold_buf[];  // 2 * FOLD_TILE
+    const int tid = threadIdx.x;
+    const int64_t body = len & ~(int64_t)7;
+    const int64_t tiles = (body + FOLD_TILE - 1) / FOLD_TILE;
+    const bool vec = (reinterpret_cast<uintptr_t>(x) & 15) == 0;
+    float p = 0.f;  // chain tid of the fold (lanes 0..7 of warp 0)
+    if (tiles > 0) fold_stage(x, 0, (int)min((int64_t)FOLD_TILE, body), fold_buf, tid, FOLD_THREADS, vec);
+    __syncthreads();
+    for (int64_t t = 0; t < tiles; ++t) {
+        const float* cur = fold_buf + (t & 1) * FOLD_TILE;
+        const int cnt = (int)min((int64_t)FOLD_TILE, body - t * FOLD_TILE);
+        if (tid >= 32) {
+            if (t + 1 < tiles)
+                fold_stage(x, (t + 1) * FOLD_TILE, (int)min((int64_t)FOLD_TILE, body - (t + 1) * FOLD_TILE),
+                           fold_buf + ((t + 1) & 1) * FOLD_TILE, tid - 32, FOLD_THREADS - 32, vec);
+        } else if (tid < 8) {
+            // cnt is a multiple of 8: FOLD_TILE is, and so is body.
+#pragma unroll 8
+            for (int j = tid; j < cnt; j += 8) p = __fadd_rn(p, cur[j]);
+        }
+        __syncthreads();
+    }
+    if (tid < 32) {
+        const float q = __shfl_down_sync(0xffffffffu, p, 4);  // lane j < 4 gets p_{j+4}
+        const float pair = __fadd_rn(p, q);
+        float acc = 0.f;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (threadIdx.x == 0) *mean = __fdiv_rn(__double2float_rn(t), (float)total);
+        for (int j = 0; j < 4; ++j) acc = __fadd_rn(acc, __shfl_sync(0xffffffffu, pair, j));
+        if (tid == 0) {
+            for (int64_t i = body; i < len; ++i) acc = __fadd_rn(acc, x[i]);
+            *mean = __fdiv_rn(acc, __ll2float_rn(len));
+        }
+    }
 }
 
 __global__ void smooth_knn_kernel(const float* __restrict__ dist, int64_t n, int k, double target,
@@ -112,7 +148,10 @@ __global__ void smooth_knn_kernel(const float* __restrict__ dist, int64_t n, int
             mid = high >= fmax ? __fmul_rn(mid, 2.0f) : __fdiv_rn(__fadd_rn(low, high), 2.0f);
         }
     }
-    float reference = rho > 0.f ? __fdiv_rn(unrolled_sum(row, k), (float)(k + 1)) : *mean;
+    // Only rows whose neighbours all sit at distance 0 use the global mean;
+    // their weights are 1 whatever sigma is, so callers that report no sigma
+    // pass no mean (such a row's sigma is then the bisection's last mid).
+    float reference = rho > 0.f ? __fdiv_rn(unrolled_sum(row, k), (float)(k + 1)) : (mean ? *mean : 0.f);
     sigmas[i] = fmaxf(mid, __fmul_rn(1e-3f, reference));
     rhos[i] = rho;
 }
@@ -527,18 +566,22 @@ cudaError_t radix_sort_pairs(scrust_context* ctx, uint32_t* kA, unsigned long lo
 int radix_blocks(int64_t n) { return (int)((n + RS_TILE - 1) / RS_TILE); }
 
 cudaError_t launch_smooth_knn(scrust_context* ctx, const float* dist, int64_t n, int k, float* sigmas,
-                              float* rhos) {
-    cudaError_t e;
+                              float* rhos, bool report_sigmas) {
+    cudaError_t e = cudaSuccess;
     const int64_t total = n * (int64_t)k;
-    const int blocks = (int)std::min<int64_t>(1024, (total + 255) / 256);
-    double* partial = (double*)ws_get(ctx, SLOT_MISC, sizeof(double) * 1024 + 64, &e);
-    if (!partial) return e;
-    float* mean = (float*)(partial + 1024);
-    sum_partial_kernel<<<blocks, 256, 0, ctx->stream>>>(dist, total, partial);
-    mean_final_kernel<<<1, 32, 0, ctx->stream>>>(partial, blocks, total, mean);
+    float* mean = nullptr;
+    if (report_sigmas) {
+        mean = (float*)ws_get(ctx, SLOT_MISC, 64, &e);
+        if (!mean) return e;
+        if ((e = set_smem_limit(ctx, (const void*)unrolled_mean_kernel, (int)FOLD_SMEM_BYTES)) != cudaSuccess)
+            return e;
+        unrolled_mean_kernel<<<1, FOLD_THREADS, FOLD_SMEM_BYTES, ctx->stream>>>(dist, total, mean);
+        ctx->launches += 1;
+    }
     const double target = log2((double)(k + 1));
     smooth_knn_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(dist, n, k, target, mean,
                                                                            sigmas, rhos);
+    ctx->launches += 1;
     return cudaGetLastError();
 }
 
@@ -556,7 +599,7 @@ int32_t run_query_connectivities(scrust_context* ctx, const uint32_t* idx, const
     float* sig = (float*)a;
     float* rho = sig + q;
     uint32_t* dcnt = (uint32_t*)(rho + q);  // q + 1
-    if ((e = launch_smooth_knn(ctx, dist, q, k, sig, rho)) != cudaSuccess) return cuda_fail(st, e, "smooth_knn");
+    if ((e = launch_smooth_knn(ctx, dist, q, k, sig, rho, false)) != cudaSuccess) return cuda_fail(st, e, "smooth_knn");
     query_rows_kernel<<<(unsigned)((q + 127) / 128), 128, 0, s>>>(idx, dist, q, k, sig, rho, dcol, dw, dcnt);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "query rows");
     if ((e = cudaMemsetAsync(dcnt + q, 0, sizeof(uint32_t), s)) != cudaSuccess) return cuda_fail(st, e, "memset");
@@ -565,7 +608,7 @@ int32_t run_query_connectivities(scrust_context* ctx, const uint32_t* idx, const
     query_csr_kernel<<<(unsigned)((q + 127) / 128), 128, 0, s>>>(dcol, dw, dcnt, out->indptr, q, k, out->indices,
                                                                 out->values);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "query csr");
-    ctx->launches += 5;
+    ctx->launches += 2;
     return ok(st);
 }
 
@@ -608,7 +651,7 @@ int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float
     uint32_t* keyB = keyA + E;
     unsigned long long* valB = valA + E;
 
-    if ((e = launch_smooth_knn(ctx, dist, n, k, sig, rho)) != cudaSuccess) return cuda_fail(st, e, "smooth_knn");
+    if ((e = launch_smooth_knn(ctx, dist, n, k, sig, rho, false)) != cudaSuccess) return cuda_fail(st, e, "smooth_knn");
     if (k <= 16)
         directed_group_kernel<16><<<(unsigned)((n * 16 + 255) / 256), 256, 0, s>>>(idx, dist, n, k, sig, rho, dcol,
                                                                                   dw, dcnt, keyA, valA);
@@ -618,7 +661,7 @@ int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float
     else
         directed_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(idx, dist, n, k, sig, rho, dcol, dw, dcnt, keyA,
                                                                      valA);
-    scan_launches += 3 /* smooth_knn */ + 1 /* directed */ + 2 /* merges */;
+    scan_launches += 1 /* directed */ + 2 /* merges */;
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "directed weights");
     // Stable radix sort of the edge slots by target row.
     int bits = 1;

@@ -138,7 +138,7 @@ int32_t scrust_cuda_knn_rows_device(scrust_context* ctx, const float* x, uint64_
     if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
     if (!x || !out_idx || !out_dist) return fail(st, SCRUST_SHAPE, "expected non-null device pointers");
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     const bool bf16 = opt && opt->precision == SCRUST_PRECISION_BF16;
     Reference ref;
     int32_t rc = reference_prepare(ctx, x, (int64_t)n, (int)d, bf16, &ref, st);

@@ -66,6 +66,29 @@ struct Workspace {
     size_t bytes[SLOT_COUNT] = {};
 };
 
+// Makes `device` current for the scope of a public entry point and gives the
+// calling thread its previous device back on return, so a call on a context
+// never changes which device the caller's own CUDA work goes to.
+class DeviceGuard {
+public:
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&prev_) != cudaSuccess) {
+            cudaGetLastError();
+            prev_ = -1;
+        }
+        if (prev_ != device) cudaSetDevice(device);
+    }
+    ~DeviceGuard() {
+        int now = -1;
+        if (prev_ >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev_) cudaSetDevice(prev_);
+    }
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+
+private:
+    int prev_ = -1;
+};
+
 struct CsrBuffers {
     uint32_t* indptr = nullptr;
     uint32_t* indices = nullptr;
@@ -305,8 +328,12 @@ cudaError_t launch_gather_rows(const float* x, const uint32_t* perm, int64_t n, 
 inline int padded_row_floats(int d) { return (d + 3) / 4 * 4; }
 
 // conn.cu
+// Per-row sigma and rho.  `report_sigmas`: also compute the global mean that
+// the sigma of a row with all neighbours at distance 0 takes (one more,
+// latency-bound launch); without it such rows' sigmas are not the
+// reference's, and nothing built from them (weights, graphs) changes.
 cudaError_t launch_smooth_knn(scrust_context* ctx, const float* dist, int64_t n, int k,
-                              float* sigmas, float* rhos);
+                              float* sigmas, float* rhos, bool report_sigmas);
 int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n,
                            int k, bool validate, CsrBuffers* out, scrust_status* st);
 // Rows of the directed fuzzy set of query rows against a reference (no

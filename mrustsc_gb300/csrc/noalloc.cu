@@ -14,11 +14,22 @@
 // That array is part of the loaded module: every GPU that loads the library
 // holds its 33 KB until the process exits.  Its device address is looked up
 // once per device with cudaGetSymbolAddress (host code cannot use the
-// array's name as a device address) on the first call made with that device
-// current.  Every call on a device shares the one array; calls whose work
-// overlaps on the GPU (different streams, no ordering between them) race on
-// it and may read each other's partial sums.  Each call writes every scratch
-// entry it reads before reading it, so nothing needs clearing between calls.
+// array's name as a device address) on the first call that works on that
+// device, and kept for the life of the process, so the entry point must not
+// be used across a cudaDeviceReset of that device.  The device is the one
+// that holds the caller's buffers (all three must be on the same device, and
+// a non-default stream must belong to it); the calling thread's current
+// device is set to it for the call and given back afterwards.  Every call on
+// a device shares the one array; calls whose work overlaps on the GPU
+// (different streams, no ordering between them) race on it and may read each
+// other's partial sums.  Each call writes every scratch entry it reads before
+// reading it, so nothing needs clearing between calls.
+//
+// The global mean (used only for the sigma of a row whose neighbours all sit
+// at distance 0) is summed here in FP64 from per-chunk partials, while the
+// reference sums in f32 in ndarray's unrolled order (which the regular entry
+// point reproduces); the two means differ by a few 1e-6 relative at the
+// largest accepted size, inside the 1e-5 sigma tolerance.
 #include <math.h>
 
 #include <mutex>
@@ -144,12 +155,20 @@ __global__ void noalloc_smooth_kernel(const float* __restrict__ dist, int64_t n,
     rhos[i] = rho;
 }
 
-// The scratch array's device address for the current device, looked up on the
-// first call made with that device current.
-int32_t scratch_for_current_device(double** out, scrust_status* st) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail(st, e, "smooth_knn_noalloc: current device");
+// The device that holds a caller buffer, or -1 when it is not device memory.
+int device_of(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) ? a.device : -1;
+}
+
+// The scratch array's device address on device `dev` (which is current),
+// looked up on the first call that works on that device.
+int32_t scratch_for_device(int dev, double** out, scrust_status* st) {
+    cudaError_t e = cudaSuccess;
     if (dev < 0 || dev >= kMaxDevices)
         return fail(st, SCRUST_NO_GPU, "device %d is beyond the %d devices this entry point tracks", dev,
                     kMaxDevices);
@@ -183,10 +202,28 @@ extern "C" int32_t scrust_cuda_smooth_knn_distances_noalloc(const float* distanc
                     "n * k must be at most %lld for the allocation-free entry point (its scratch is a fixed "
                     "device array), got %llu x %u",
                     (long long)kMaxEntries, (unsigned long long)n, k);
-    double* scratch = nullptr;
-    int32_t rc = scratch_for_current_device(&scratch, st);
-    if (rc) return rc;
+    const int dev = device_of(distances);
+    if (dev < 0 || device_of(sigmas) != dev || device_of(rhos) != dev)
+        return fail(st, SCRUST_INVALID_PARAMETER,
+                    "expected distances, sigmas and rhos in the device memory of one GPU, got buffers on devices "
+                    "%d, %d and %d (-1: not device memory)",
+                    dev, device_of(sigmas), device_of(rhos));
     cudaStream_t s = (cudaStream_t)stream;
+    if (s) {
+        int sdev = -1;
+        if (cudaStreamGetDevice(s, &sdev) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(st, SCRUST_INVALID_PARAMETER, "expected a valid CUDA stream");
+        }
+        if (sdev != dev)
+            return fail(st, SCRUST_INVALID_PARAMETER,
+                        "expected a stream of device %d, which holds the buffers, got a stream of device %d", dev,
+                        sdev);
+    }
+    DeviceGuard device_guard(dev);
+    double* scratch = nullptr;
+    int32_t rc = scratch_for_device(dev, &scratch, st);
+    if (rc) return rc;
     const int partials = (int)((total + kChunk - 1) / kChunk);
     noalloc_partial_kernel<<<partials, kThreads, 0, s>>>(distances, (int64_t)total, scratch);
     noalloc_mean_kernel<<<1, kThreads, 0, s>>>(scratch, partials, (int64_t)total);

@@ -153,7 +153,7 @@ void launch_batch(scrust_server* sv, ServeSlot& sl) {
     const uint64_t q = sl.cells;
     sl.launch_code = SCRUST_OK;
     std::lock_guard<std::mutex> lock(ctx->mu);
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaError_t e = cudaSuccess;
     int32_t rc = SCRUST_OK;
     if (!sl.h_q.grow(q * d) || !sl.h_idx.grow(q * k) || !sl.h_dist.grow(q * k) || !sl.h_ptr.grow(q + 1) ||
@@ -205,7 +205,7 @@ void finish_batch(scrust_server* sv, ServeSlot& sl) {
     std::string msg = sl.launch_msg;
     if (rc == SCRUST_OK) {
         std::lock_guard<std::mutex> lock(sl.ctx->mu);
-        cudaSetDevice(sl.ctx->device);
+        DeviceGuard device_guard(sl.ctx->device);
         rc = collect_device_errors(sl.ctx, &st);
         if (rc) msg = st.message;
     }
@@ -251,7 +251,7 @@ void finish_batch(scrust_server* sv, ServeSlot& sl) {
 }
 
 void scheduler(scrust_server* sv) {
-    cudaSetDevice(sv->device);
+    DeviceGuard device_guard(sv->device);
     for (;;) {
         bool progressed = false;
         for (ServeSlot& sl : sv->slots)
@@ -364,6 +364,7 @@ scrust_server* scrust_serve_create(int32_t device, const float* atlas, uint64_t 
         return nullptr;
     }
     sv->device = device;
+    DeviceGuard create_guard(device);  // the slots' events and the atlas live on `device`
     sv->m = m;
     sv->d = (int)d;
     sv->k = (int)k;
@@ -388,7 +389,7 @@ scrust_server* scrust_serve_create(int32_t device, const float* atlas, uint64_t 
     {
         scrust_context* c0 = sv->slots[0].ctx;
         std::lock_guard<std::mutex> lock(c0->mu);
-        cudaSetDevice(device);
+        DeviceGuard device_guard(device);
         cudaStream_t s = c0->stream;
         e = cudaMalloc(&sv->atlas, sizeof(float) * m * d);
         if (e == cudaSuccess) e = cudaMalloc(&sv->means, sizeof(double) * d * (mean_blocks + 1));
@@ -528,7 +529,7 @@ void scrust_serve_destroy(scrust_server* sv) {
     }
     sv->cv_work.notify_all();
     if (sv->worker.joinable()) sv->worker.join();
-    cudaSetDevice(sv->device);
+    DeviceGuard device_guard(sv->device);
     destroy_server(sv);
 }
 

@@ -429,6 +429,29 @@ static double sq_dist_f64(const float* a, const float* b, int64_t d) {
     return s;
 }
 
+/* The same sum, abandoned once a partial sum exceeds `limit`: the terms are
+ * non-negative and round-to-nearest addition of a non-negative term never
+ * decreases the sum, so the full sum would exceed `limit` too.  Returns the
+ * full sum when it is at most `limit` (then bit-equal to sq_dist_f64). */
+static double sq_dist_f64_below(const float* a, const float* b, int64_t d, double limit) {
+    double s = 0.0;
+    int64_t t = 0;
+    for (; t + 8 <= d; t += 8) {
+        for (int64_t u = t; u < t + 8; u++) {
+            double diff = (double)a[u] - (double)b[u];
+            double p = diff * diff;
+            s = s + p;
+        }
+        if (s > limit) return s;
+    }
+    for (; t < d; t++) {
+        double diff = (double)a[t] - (double)b[t];
+        double p = diff * diff;
+        s = s + p;
+    }
+    return s;
+}
+
 /*
  * The FP64 ground truth of tests/test_neighbors_audit.py:52-61:
  * d = sqrt(max(sum (x_i - x_j)^2, 0)) in float64, k non-self neighbours
@@ -455,9 +478,16 @@ int oracle_knn_fp64_rows(const float* x, int64_t n, int64_t d, int64_t k, const 
             for (int64_t r = 0; r < nrows; r++) {
                 int64_t q = rows ? rows[r] : r;
                 int64_t have = 0;
+                /* Once k are held, a column whose squared distance exceeds
+                 * the k-th's by a relative 1e-12 has a strictly larger square
+                 * root (its relative gap, ~5e-13, is far above the double
+                 * rounding of sqrt), so it can neither enter nor tie: such
+                 * columns are dropped early.  The result is unchanged. */
+                double limit = INFINITY;
                 for (int64_t j = 0; j < n; j++) {
                     if (j == q) continue;
-                    double s = sq_dist_f64(x + q * d, x + j * d, d);
+                    double s = sq_dist_f64_below(x + q * d, x + j * d, d, limit);
+                    if (s > limit) continue;
                     double v = sqrt(s > 0.0 ? s : 0.0);
                     pair_f64 cnd = {v, (uint32_t)j};
                     if (have == k) {
@@ -473,6 +503,10 @@ int oracle_knn_fp64_rows(const float* x, int64_t n, int64_t d, int64_t k, const 
                     }
                     top[s2] = cnd;
                     have++;
+                    if (have == k) {
+                        double kth = top[k - 1].d;
+                        limit = kth * kth * (1.0 + 1e-12);
+                    }
                 }
                 for (int64_t t = 0; t < k; t++) {
                     idx[r * k + t] = top[t].id;
@@ -574,6 +608,9 @@ int oracle_smooth_knn(const float* dist, int64_t n, int64_t k, float* sigmas, fl
     const int64_t width = k + 1;
     const double target = log2((double)width);
     const float mean_distance = oracle_unrolled_sum_f32(dist, n * k) / (float)(n * k);
+    /* Rows are independent: threads split them, the arithmetic per row is
+     * the sequential one below. */
+#pragma omp parallel for schedule(static)
     for (int64_t r = 0; r < n; r++) {
         const float* row = dist + r * k;
         float rho = 0.0f;

@@ -1,8 +1,8 @@
 """Regenerate the golden fixtures in this folder from the reference's own tests.
 
-Run once in a container that has the reference checkout:
+Run once where a checkout of the reference (the scrust repository) exists:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the scrust checkout>
 
 It reads the scanpy constants the reference pins in
 crates/scrust-core/src/neighbors.rs:498-544 (ten sample cells of
@@ -69,7 +69,9 @@ def parse(neighbors_rs: str) -> dict:
 
 
 def main(argv: list[str]) -> None:
-    root = pathlib.Path(argv[1] if len(argv) > 1 else "/root/reference")
+    if len(argv) != 2:
+        raise SystemExit("usage: make_golden.py <path of the scrust checkout>")
+    root = pathlib.Path(argv[1])
     text = (root / "crates/scrust-core/src/neighbors.rs").read_text()
     out = HERE / "scanpy_reference_embedding_300x20.json"
     out.write_text(json.dumps(parse(text), indent=1) + "\n")

@@ -75,3 +75,31 @@ def test_two_gloo_ranks_equal_one_process(tmp_path, oracle):
     np.testing.assert_array_equal(got["indptr"], indptr)
     np.testing.assert_array_equal(got["cols"], cols)
     np.testing.assert_array_equal(got["vals"], vals)
+
+
+def test_default_row_solver_runs_on_the_ranks_current_device(monkeypatch):
+    """With no solver passed, each rank solves its rows on its own GPU (the
+    current CUDA device of its process), never on device 0 by default."""
+    import torch
+
+    seen = {}
+
+    def fake_upload(x, device):
+        seen["upload"] = device
+        return torch.from_numpy(np.ascontiguousarray(x))
+
+    def fake_rows_device(xd, k, r0, r1, precision="fp16"):
+        seen["rows"] = (r0, r1)
+        return torch.zeros((r1 - r0, k), dtype=torch.int32), torch.zeros((r1 - r0, k), dtype=torch.float32)
+
+    monkeypatch.setattr(torch.cuda, "current_device", lambda: 3)
+    monkeypatch.setattr(distributed, "_upload", fake_upload)
+    monkeypatch.setattr(distributed, "knn_rows_device", fake_rows_device)
+    monkeypatch.setattr(distributed, "gather_rows", lambda block, n, world, group=None: block)
+    monkeypatch.setattr(distributed, "_collective_device", lambda group: torch.device("cpu"))
+    x = np.zeros((10, 4), np.float32)
+    distributed.neighbors_sharded(x, 2, rank=1, world=2, connectivities=lambda i, d: None)
+    assert seen == {"upload": 3, "rows": (5, 10)}
+    seen.clear()
+    distributed.knn_rows_gpu(x, 2, 0, 5)
+    assert seen == {"upload": 3, "rows": (0, 5)}

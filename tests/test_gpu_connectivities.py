@@ -48,12 +48,35 @@ def test_connectivities_match_the_oracle(scrust, oracle, seed):
     assert_same_csr(ours, oracle.connectivities(fi, fd))
 
 
-def test_smooth_knn_matches_the_oracle(scrust, oracle):
+@pytest.mark.parametrize("duplicates", [False, True])
+def test_smooth_knn_matches_the_oracle(scrust, oracle, duplicates):
     x = synthetic.plain_small(seed=2)
+    if duplicates:
+        x[:40] = x[0]  # 40 rows whose neighbours all sit at distance 0
     _, dist = scrust.knn(x, 15, "auto")
     s_gpu, r_gpu = scrust.smooth_knn_distances(dist)
     s_ref, r_ref = oracle.smooth_knn(dist)
     np.testing.assert_array_equal(r_gpu, r_ref)
+    np.testing.assert_allclose(s_gpu, s_ref, rtol=1e-5)
+    # Such rows take the global mean, summed in the reference's own f32 order:
+    # their sigmas are the same bits.
+    zero = r_ref == 0
+    assert zero.sum() == (40 if duplicates else 0)
+    np.testing.assert_array_equal(s_gpu[zero], s_ref[zero])
+
+
+@pytest.mark.parametrize(("n", "k"), [(100_003, 15), (7, 3), (1, 9)])
+def test_global_mean_in_the_reference_order(scrust, oracle, n, k):
+    """The mean over many staged tiles, with a tail beyond the eight chains and
+    inputs shorter than one chain step, bit-equal to the unrolled fold."""
+    rng = np.random.default_rng(n)
+    dist = np.sort(rng.gamma(2.0, 1.5, size=(n, k)).astype(np.float32), axis=1)
+    dist[::11] = 0.0
+    s_gpu, r_gpu = scrust.smooth_knn_distances(dist)
+    s_ref, r_ref = oracle.smooth_knn(dist)
+    np.testing.assert_array_equal(r_gpu, r_ref)
+    zero = r_ref == 0
+    np.testing.assert_array_equal(s_gpu[zero], s_ref[zero])
     np.testing.assert_allclose(s_gpu, s_ref, rtol=1e-5)
 
 
