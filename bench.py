@@ -12,8 +12,15 @@ pinned memory and the kNN rows and connectivities CSR read back every step.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--form plain|tensor]
     python bench.py --impl reference      # the reference CPU path (restated)
 
-For N > 1 launch with torch.distributed.run; every rank builds its own
-replica graph (no data-path collective), so scaling is weak.
+Outside the timed regions the default run also checks the bench graph
+against the C oracle (10,000 random cells plus every zero-distance and
+near-tie cell against the FP64 kNN; the whole connectivities CSR against the
+restated connectivities), replays the serving workload at its fixed offered
+load for its p50/p99 latency, and times the reference CPU path on a sample.
+
+For N > 1 launch with torch.distributed.run; by default every rank builds its
+own replica graph (no data-path collective, weak scaling); with
+--parallelism sharded the ranks share one graph by rows (strong scaling).
 """
 
 from __future__ import annotations
@@ -37,6 +44,11 @@ sys.path.insert(0, str(ROOT))
 WORKLOAD = {"name": "knn_graph_1M_x50_k15", "n": 1_000_000, "d": 50, "k": 15, "clusters": 200,
             "dup_frac": 0.01, "seed": 0}
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+# DRAM bytes (read + write) of the tensor sweep's launches in one step, from
+# an ncu capture of this workload (profiles/tensor_sweep_1M_x50_k15.md gives
+# the command); keyed by (cells, dims, k).
+SWEEP_TRAFFIC: dict = {}
+SWEEP_TRAFFIC_NOTE = "dram__bytes_read.sum + dram__bytes_write.sum over the sweep launches of one step (ncu)"
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
 
 
@@ -52,6 +64,13 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-recall", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--serve-seconds", type=float, default=3.0)
+    p.add_argument("--parity-rows", type=int, default=10_000,
+                   help="random cells checked against the FP64 oracle (plus every zero-distance and near-tie cell)")
+    p.add_argument("--vs-plain", action="store_true", help="also solve with the plain form and compare")
+    p.add_argument("--parallelism", choices=["replicas", "sharded"], default="replicas",
+                   help="N > 1: independent replica graphs (weak scaling) or one graph sharded by rows (strong)")
     p.add_argument("--workload", choices=["precision", "batching", "serving", "scale"], default="precision",
                    help="precision: the 1M x 50 graph build (default); batching: 64 samples in one graph launch "
                         "against 64 sequential plain launches; serving: the resident-atlas query service; "
@@ -127,25 +146,40 @@ def make_data(n: int, seed: int):
 
 # --------------------------------------------------------------------------- reference arm
 
-def cpu_reference_step(x: np.ndarray, k: int, rows: np.ndarray):
-    """The restated reference CPU path on a bounded sample: kNN of `rows` against all
-    cells (neighbors.rs:35-101) and the connectivities of that sample's graph."""
+def cpu_config(n: int) -> dict:
+    """The GPU arm's config keys, so both arms name the same workload."""
+    return {"workload": WORKLOAD["name"], "n_cells": n, "dims": WORKLOAD["d"], "k": WORKLOAD["k"],
+            "clusters": WORKLOAD["clusters"], "dup_frac": WORKLOAD["dup_frac"], "mode": "exact"}
+
+
+def cpu_reference_step(engine, k: int, rows: np.ndarray):
+    """The reference CPU path (neighbors.rs:35-101 with its tile product on a
+    BLAS SGEMM, as candle runs it) on a bounded sample: kNN of `rows` against
+    all cells and the connectivities of that sample's graph (:208-372)."""
     from oracle import oracle
 
-    idx, dist = oracle.knn_reference_cpu_rows(x, k, rows)
+    idx, dist = engine.knn_rows(k, rows)
     sub = (idx % len(rows)).astype(np.uint32)
     oracle.connectivities(sub, dist)
 
 
-def calibrate_rows(x, k, seconds: float, cap: int = 50_000) -> tuple[np.ndarray, float]:
+def calibrate_rows(engine, k, seconds: float, n: int, cap: int = 200_000) -> np.ndarray:
     rng = np.random.default_rng(123)
-    probe = np.sort(rng.choice(len(x), 64, replace=False))
+    probe = np.sort(rng.choice(n, min(n, 2 * engine.tile_rows), replace=False))
+    cpu_reference_step(engine, k, probe)  # first call: BLAS threads and buffers
     t0 = time.perf_counter()
-    cpu_reference_step(x, k, probe)
+    cpu_reference_step(engine, k, probe)
     per_row = (time.perf_counter() - t0) / len(probe)
-    nrows = int(max(64, min(cap, len(x), seconds / max(per_row, 1e-9))))
-    rows = np.sort(rng.choice(len(x), nrows, replace=False))
-    return rows, per_row
+    nrows = int(max(64, min(cap, n, seconds / max(per_row, 1e-9))))
+    return np.sort(rng.choice(n, nrows, replace=False))
+
+
+def cpu_sample_text(rows: int, n: int, secs: float, cores: int, engine) -> str:
+    flop = 2.0 * rows * n * WORKLOAD["d"]
+    return (f"{rows} query cells against all {n} (kNN + sample-graph connectivities) per step: the reference "
+            f"CPU path restated (no Rust toolchain), tile product on numpy's BLAS SGEMM, affine/snap/selection "
+            f"in C, {cores} threads; centring and norms once per workload, outside the steps; "
+            f"{secs:.2f} s per step, {flop / secs / 1e9:.0f} GFLOP/s in the tile products")
 
 
 def run_reference(args):
@@ -157,26 +191,25 @@ def run_reference(args):
     oracle.build()
     n, k = args.n, WORKLOAD["k"]
     x = make_data(n, WORKLOAD["seed"])
+    engine = oracle.ExpansionCPU(x)
     step_seconds = min(10.0, max(2.0, 150.0 / max(1, args.steps + args.warmup)))
-    rows, _ = calibrate_rows(x, k, step_seconds)
+    rows = calibrate_rows(engine, k, step_seconds, n)
     for _ in range(args.warmup):
-        cpu_reference_step(x, k, rows)
+        cpu_reference_step(engine, k, rows)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        cpu_reference_step(x, k, rows)
+        cpu_reference_step(engine, k, rows)
         times.append(time.perf_counter() - t0)
     ms = 1e3 * statistics.mean(times)
     value = len(rows) / (ms / 1e3)
     cores = oracle.num_threads()
-    sample = (f"{len(rows)} query cells against all {n} (kNN + connectivities of the sample graph) "
-              f"per step, restated reference CPU path (no Rust toolchain: port of neighbors.rs), {cores} threads")
     line = {"metric": "kNN-graph cells/s", "value": value, "unit": "cells/s", "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": WORKLOAD["name"], "n_cells": n, "dims": WORKLOAD["d"], "k": k},
-            "cpu_baseline": {"value": value, "unit": "cells/s", "cores": cores, "kind": "port", "sample": sample},
+            "impl": "reference", "config": cpu_config(n),
+            "cpu_baseline": {"value": value, "unit": "cells/s", "cores": cores, "kind": "port",
+                             "sample": cpu_sample_text(len(rows), n, ms / 1e3, cores, engine)},
             "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -184,35 +217,71 @@ def run_reference(args):
 
 # --------------------------------------------------------------------------- our arm
 
-def fp64_recall(torch, xd, idx_dev, k: int, nrows: int = 256, seed: int = 5):
-    """Exact-row fraction and recall against an FP64 reference computed here with torch
-    (expansion to shortlist, difference form to rank, lowest index on ties)."""
-    n = xd.shape[0]
-    g = np.random.default_rng(seed)
-    rows = torch.as_tensor(np.sort(g.choice(n, nrows, replace=False)), device=xd.device)
-    X = xd.double()
-    A = X[rows]
-    nx = (X * X).sum(1)
-    exact, hit = 0, 0
-    for c0 in range(0, nrows, 32):
-        r = rows[c0:c0 + 32]
-        Ab = A[c0:c0 + 32]
-        d2 = (Ab * Ab).sum(1, keepdim=True) + nx[None, :] - 2.0 * Ab @ X.T
-        d2[torch.arange(len(r), device=xd.device), r] = float("inf")
-        cand = torch.topk(d2, k + 32, largest=False).indices
-        diff = X[cand] - Ab[:, None, :]
-        dd = (diff * diff).sum(-1)
-        dd = torch.where(cand == r[:, None], torch.full_like(dd, float("inf")), dd)
-        order = torch.argsort(cand, dim=1)
-        cand = torch.gather(cand, 1, order)
-        dd = torch.gather(dd, 1, order)
-        o2 = torch.argsort(dd, dim=1, stable=True)
-        truth = torch.gather(cand, 1, o2)[:, :k]
-        ours = idx_dev[r].long()
-        exact += int((truth == ours).all(1).sum())
-        for t_row, o_row in zip(truth.cpu().numpy(), ours.cpu().numpy()):
-            hit += len(set(t_row.tolist()) & set(o_row.tolist()))
-    return exact / nrows, hit / (nrows * k)
+def parity_leg(torch, L, ctx, x, xd, k: int, form: str, idx_dev, dist_dev, n_random: int) -> tuple[dict, dict]:
+    """The bench graph against the C oracle, outside every timed region: the
+    kNN rows of `n_random` random cells plus every cell with a neighbour at
+    distance 0 plus every cell whose k-th and (k+1)-th neighbours are within
+    1e-5 relative (from one k+1 solve), against the FP64 exact kNN; and the
+    whole connectivities CSR, built again through the host API, against the
+    oracle's connectivities of the same kNN graph."""
+    from mrustsc_gb300 import _scrust
+    from oracle import oracle, parity
+
+    oracle.build()
+    n, d = x.shape
+    st = _lib_status()
+    i1 = torch.empty((n, k + 1), dtype=torch.int32, device=xd.device)
+    d1 = torch.empty((n, k + 1), dtype=torch.float32, device=xd.device)
+    opts = _lib_options(form)
+    check(L.scrust_cuda_knn_device(ctx, xd.data_ptr(), n, d, k + 1, ctypes.byref(opts), i1.data_ptr(),
+                                   d1.data_ptr(), ctypes.byref(st)), st)
+    check(L.scrust_cuda_synchronize(ctx, ctypes.byref(st)), st)
+    idx = idx_dev.cpu().numpy().view(np.uint32)
+    dist = dist_dev.cpu().numpy()
+    rows, kinds = parity.select_rows(n, dist, d1.cpu().numpy(), n_random=n_random, seed=0)
+    t0 = time.perf_counter()
+    rep = parity.knn_rows_report(x, k, idx, dist, rows)
+    rep.update(kinds)
+    rep["oracle_s"] = time.perf_counter() - t0
+    rep["ok"] = parity.knn_rows_ok(rep)
+    hi, hd, csr = _scrust.neighbors_graph(x, k, form=form)
+    t0 = time.perf_counter()
+    crep = parity.connectivities_report(hi, hd, csr)
+    crep["oracle_s"] = time.perf_counter() - t0
+    crep["knn_same_as_bench_graph"] = bool(np.array_equal(hi, idx) and np.array_equal(hd, dist))
+    crep["ok"] = parity.connectivities_ok(crep) and crep["knn_same_as_bench_graph"]
+    return rep, crep
+
+
+def _lib_status():
+    from mrustsc_gb300 import _lib
+
+    return _lib.Status()
+
+
+def _lib_options(form: str):
+    from mrustsc_gb300 import _lib
+
+    return _lib.options(form=form)
+
+
+def check(rc, st):
+    from mrustsc_gb300 import _lib
+
+    _lib.check(rc, st)
+
+
+def phase_bytes(form: str, n: int, d: int, k: int, nnz: int) -> dict:
+    """Algorithmic bytes of the memory-bound phases: what each must read and
+    write at least once.  prep: the embedding read, the candidate operands
+    written (two n x 64 16-bit arrays in the tensor form, the transposed
+    centred rows in the plain form); rerank: every row's coordinates read and
+    the n x k ids and distances written; connectivities: the n x k graph read
+    and the CSR (indptr, columns, values) written."""
+    n_pad = (n + 255) // 256 * 256
+    operands = 2 * n_pad * 64 * 2 if form == "tensor" else ((d + 3) // 4 * 4) * n_pad * 4
+    return {"prep": n * d * 4 + operands, "rerank": n * d * 4 + n * k * 8,
+            "connectivities": n * k * 8 + (n + 1) * 4 + nnz * 8}
 
 
 def run_ours(args):
@@ -229,6 +298,8 @@ def run_ours(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     build.build()
+    if args.parallelism == "sharded" and world > 1:
+        return run_sharded(args, world, rank, local)
     L = _lib.lib()
     form = args.form or ("tensor" if getattr(_lib, "TENSOR_FORM_READY", False) else "plain")
     n, d, k = args.n, WORKLOAD["d"], WORKLOAD["k"]
@@ -287,30 +358,40 @@ def run_ours(args):
         torch.distributed.barrier()
     value = world * n / (ms_step / 1e3)
 
+    # One more (untimed) step for the graph's size.
+    out = ctypes.c_void_p()
+    _lib.check(L.scrust_cuda_neighbors_graph_device(ctx, xd.data_ptr(), n, d, k, ctypes.byref(opts), idx.data_ptr(),
+                                                    dst.data_ptr(), ctypes.byref(out), ctypes.byref(st)), st)
+    nnz = int(L.scrust_csr_nnz(out))
+    L.scrust_csr_free(out)
+
     ph = np.array(phases) if phases and len(phases[0]) == 6 else np.zeros((1, 6))
     ph_mean = ph.mean(0)
     cand_ms = float(ph_mean[1])
     pk, pk_kind = peaks()
+    hbm = float(pk["hbm_gbs"])
     if form == "tensor":
-        # The dominant kernel is the tensor sweep (knn_candidates_tc): its two
+        # The dominant kernel is the tensor sweep (knn_candidates_tc): its
         # passes are timed by the library's events on its stream (the
         # candidates phase less the building of the second pass's tile
         # lists).  Its unit of work is one (256-row block, 256-column tile)
         # pair, 2 * 256 * 256 * d algorithmic flops; the pairs it computes are
         # counted by the kernel's own counters in one extra, untimed step.
         sweep_ms = cand_ms - float(ph_mean[5]) if ph_mean[4] > 0 else cand_ms
-        out = (ctypes.c_uint64 * 16)()
-        L.scrust_cuda_kernel_stats(ctx, 1, out, 16)
+        cnt = (ctypes.c_uint64 * 16)()
+        L.scrust_cuda_kernel_stats(ctx, 1, cnt, 16)
         step()
         _lib.check(L.scrust_cuda_synchronize(ctx, ctypes.byref(st)), st)
-        L.scrust_cuda_kernel_stats(ctx, 0, out, 16)
-        tiles = int(out[8])
+        L.scrust_cuda_kernel_stats(ctx, 0, cnt, 16)
+        tiles = int(cnt[8])
         blocks = (n + 255) // 256
         flops = tiles * 2.0 * 256 * 256 * d
         achieved = flops / (sweep_ms / 1e3) / 1e12
+        traffic = SWEEP_TRAFFIC.get((n, d, k))
         roof = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
-                "frac": achieved / pk["bf16_tflops"], "traffic": None,
-                "kernel": "tensor_candidates_kernel (knn_candidates_tc), both sweep passes",
+                "frac": achieved / pk["bf16_tflops"], "traffic": traffic,
+                "traffic_note": SWEEP_TRAFFIC_NOTE if traffic else None,
+                "kernel": "tensor_candidates_kernel (knn_candidates_tc), all sweep passes",
                 "kernel_ms": sweep_ms, "units": "(256-row block, 256-column tile) pairs computed",
                 "units_per_step": tiles, "flops_per_unit": 2 * 256 * 256 * d,
                 "brute_force_units": blocks * blocks, "peak_source": f"bf16 burst, {pk_kind}"}
@@ -322,25 +403,31 @@ def run_ours(args):
         roof = {"bound": "fp32_cuda_core", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak, "traffic": None, "kernel": "plain_candidates_kernel",
                 "peak_source": f"{sm_count} SMs x 128 FP32 lanes x 2 x {pk.get('sm_max_mhz', 2070.0)} MHz"}
+    pb = phase_bytes(form, n, d, k, nnz)
+    phase_ms = {"prep": float(ph_mean[0]), "rerank": float(ph_mean[2]), "connectivities": float(ph_mean[3])}
+    phases_gbs = {name: {"bytes": pb[name], "ms": phase_ms[name],
+                         "gbs": pb[name] / (phase_ms[name] / 1e3) / 1e9 if phase_ms[name] > 0 else None,
+                         "frac_of_hbm": (pb[name] / (phase_ms[name] / 1e3) / 1e9) / hbm if phase_ms[name] > 0 else None}
+                  for name in phase_ms}
 
     line = {"metric": "kNN-graph cells/s", "value": value, "unit": "cells/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if form == "plain" else "f16",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD["name"], "n_cells": n, "dims": d, "k": k,
-                       "clusters": WORKLOAD["clusters"], "dup_frac": WORKLOAD["dup_frac"], "form": form,
-                       "mode": "exact", "parallelism": f"replicas{world}",
+            "config": {**cpu_config(n), "form": form, "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (200 MB embedding, >1 GB candidate lists per step)"},
             "phases_ms": {"prep": float(ph_mean[0]), "candidates": float(ph_mean[1]),
                           "rerank": float(ph_mean[2]), "connectivities": float(ph_mean[3]),
                           "candidates_first_pass": float(ph_mean[4]),
                           "candidates_tile_lists": float(ph_mean[5])},
-            "gpu_launches": launches, "roofline": roof, "clocks": clk}
+            "phases_gbs": phases_gbs, "phases_gbs_peak": f"{hbm} GB/s, {pk_kind} copy bandwidth",
+            "graph_nnz": nnz, "gpu_launches": launches, "roofline": roof, "clocks": clk}
 
     if rank == 0 and not args.no_recall:
-        ex, rec = fp64_recall(torch, xd, idx, k)
-        line["recall_fp64_sample"] = {"rows": 256, "exact_rows": ex, "recall": rec}
-        if form == "tensor":
+        rep, crep = parity_leg(torch, L, ctx, x, xd, k, form, idx, dst, args.parity_rows)
+        line["recall_fp64_sample"] = rep
+        line["conn_check"] = crep
+        if form == "tensor" and args.vs_plain:
             idx_t = idx.clone()
             opts_p = _lib.options(form="plain")
             rc = L.scrust_cuda_knn_device(ctx, xd.data_ptr(), n, d, k, ctypes.byref(opts_p), idx.data_ptr(),
@@ -351,46 +438,108 @@ def run_ours(args):
 
     if rank == 0 and not args.no_e2e:
         # Pinned host buffers for the input and both neighbour arrays (the
-        # graph's host arrays come from the library's own pinned pool).
+        # graph's host arrays come from the library's own pinned pool).  The
+        # same K steps as the device-resident timing, each one call of the
+        # host API: upload, graph, download of the kNN rows and the CSR.
         xh = torch.from_numpy(x).pin_memory()
         ih = torch.empty((n, k), dtype=torch.int32).pin_memory()
         dh = torch.empty((n, k), dtype=torch.float32).pin_memory()
-        e2e_steps = max(1, min(args.steps, 3))
-        nnz = 0
+        e2e_steps = max(1, args.steps)
+        nnz_e = 0
         # One untimed call first: it sizes the device workspaces and the
         # pinned pool, as the warm-up steps do for the device-resident timing.
         out = ctypes.c_void_p()
         _lib.check(L.scrust_cuda_neighbors_graph(ctx, xh.data_ptr(), n, d, k, ctypes.byref(opts), ih.data_ptr(),
                                                  dh.data_ptr(), ctypes.byref(out), ctypes.byref(st)), st)
         L.scrust_csr_free(out)
-        t0 = time.perf_counter()
+        times = []
         for _ in range(e2e_steps):
+            t0 = time.perf_counter()
             out = ctypes.c_void_p()
             rc = L.scrust_cuda_neighbors_graph(ctx, xh.data_ptr(), n, d, k, ctypes.byref(opts), ih.data_ptr(),
                                                dh.data_ptr(), ctypes.byref(out), ctypes.byref(st))
             _lib.check(rc, st)
-            nnz = int(L.scrust_csr_nnz(out))
+            times.append(time.perf_counter() - t0)
+            nnz_e = int(L.scrust_csr_nnz(out))
             L.scrust_csr_free(out)
-        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        e2e_s = statistics.mean(times)
         line["e2e"] = {"value": n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": n * d * 4,
-                       "d2h_bytes_per_step": n * k * 8 + (n + 1) * 4 + nnz * 8, "ms_per_step": e2e_s * 1e3}
+                       "d2h_bytes_per_step": n * k * 8 + (n + 1) * 4 + nnz_e * 8, "ms_per_step": e2e_s * 1e3,
+                       "steps": e2e_steps, "ms_min": min(times) * 1e3, "ms_max": max(times) * 1e3}
+
+    if rank == 0 and world == 1 and not args.no_serving and args.n == WORKLOAD["n"]:
+        from mrustsc_gb300 import serving
+
+        line["serving"] = serving.fixed_load(duration_s=args.serve_seconds)
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle
 
         oracle.build()
-        rows, _ = calibrate_rows(x, k, args.cpu_seconds)
+        engine = oracle.ExpansionCPU(x)
+        rows = calibrate_rows(engine, k, args.cpu_seconds, n)
         t0 = time.perf_counter()
-        cpu_reference_step(x, k, rows)
+        cpu_reference_step(engine, k, rows)
         secs = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": len(rows) / secs, "unit": "cells/s", "cores": oracle.num_threads(),
-                                "kind": "port",
-                                "sample": f"{len(rows)} query cells against all {n}, restated reference CPU path "
-                                          f"(kNN + sample-graph connectivities), {secs:.1f} s"}
+        cores = oracle.num_threads()
+        line["cpu_baseline"] = {"value": len(rows) / secs, "unit": "cells/s", "cores": cores, "kind": "port",
+                                "sample": cpu_sample_text(len(rows), n, secs, cores, engine)}
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_sharded(args, world: int, rank: int, local: int):
+    """One graph sharded over the ranks (strong scaling): each rank solves its
+    block of rows against the whole embedding on its GPU, the rows are
+    gathered into device tensors with NCCL, and rank 0 builds the
+    connectivities.  A step ends when rank 0's graph is complete."""
+    import torch
+    import torch.distributed as dist
+
+    from mrustsc_gb300 import _lib, distributed
+
+    L = _lib.lib()
+    n, d, k = args.n, WORKLOAD["d"], WORKLOAD["k"]
+    x = make_data(n, WORKLOAD["seed"])
+    xd = torch.from_numpy(x).to(f"cuda:{local}")
+
+    def step():
+        res = distributed.neighbors_sharded_device(xd, k, rank, world)
+        if res[2] is not None:
+            _lib.check(L.scrust_cuda_synchronize(_lib.context(local), ctypes.byref(_lib.Status())), _lib.Status())
+            L.scrust_csr_free(res[2])
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    end.record()
+    end.synchronize()
+    clk = clocks.stop()
+    t = torch.tensor([start.elapsed_time(end) / args.steps], device=xd.device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_step = float(t.item())
+    dist.barrier()
+    dist.destroy_process_group()
+    if rank == 0:
+        line = {"metric": "kNN-graph cells/s", "value": n / (ms_step / 1e3), "unit": "cells/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+                "scaling": "strong", "vs_baseline": None, "dtype": "f16", "data": "synthetic",
+                "config": {**cpu_config(n), "form": "tensor", "parallelism": f"sharded{world}",
+                           "l2": "inputs larger than L2"},
+                "clocks": clk}
         print(json.dumps(line), flush=True)
     return 0
 
@@ -461,6 +610,7 @@ def run_batching(args):
                                                     ii.data_ptr(), dd.data_ptr(), ctypes.byref(st)), st)
         return run
 
+    graph_dist = dst.clone()
     seq_steps = max(1, min(args.steps, 3))
     ms_plain = timed(sequential(plain), seq_steps, 1)
     same = bool((graph_idx == idx).all().item())
@@ -480,6 +630,27 @@ def run_batching(args):
                                            ctypes.byref(opts), ih.data_ptr(), dh.data_ptr(), ctypes.byref(st)), st)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     flops = sum(2.0 * m * m * d for m in sizes)
+    parity_rep = None
+    if not args.no_recall:
+        # Every sample: 64 random rows and up to 64 rows with a zero-distance
+        # neighbour against the FP64 kNN of that sample (outside the timing).
+        from oracle import oracle, parity
+
+        oracle.build()
+        gi = graph_idx.cpu().numpy().view(np.uint32)
+        gd = graph_dist.cpu().numpy()
+        rng = np.random.default_rng(1)
+        rows_total, exact, worst = 0, 0, 0.0
+        for s_i, xs in enumerate(samples):
+            a, b = int(offsets[s_i]), int(offsets[s_i + 1])
+            rows = np.unique(np.concatenate([rng.choice(b - a, min(b - a, 64), replace=False),
+                                             np.nonzero(gd[a:b, 0] == 0)[0][:64]]))
+            rep = parity.knn_rows_report(xs, k, gi[a:b], gd[a:b], rows)
+            rows_total += rep["rows"]
+            exact += rep["exact_rows"]
+            worst = max(worst, rep["max_rel_dist_err"])
+        parity_rep = {"samples": len(samples), "rows": rows_total, "exact_rows": exact, "max_rel_dist_err": worst,
+                      "against": "FP64 exact kNN of each sample (C oracle)"}
     line = {"metric": "batched kNN cells/s (64 samples, one CUDA-graph launch)", "value": n / (ms_graph / 1e3),
             "unit": "cells/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_graph,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16" if prec.value == 0 else "bf16",
@@ -492,7 +663,7 @@ def run_batching(args):
                            "results_identical_to_sequential_plain": same},
             "autotuner": {"list_capacity": cap.value, "precision": "fp16" if prec.value == 0 else "bf16",
                           "tuned_ms": tuned.value, "plan_create_s": plan_s},
-            "gpu_launches": launches, "clocks": clk,
+            "gpu_launches": launches, "clocks": clk, "recall_fp64_sample": parity_rep,
             "e2e": {"value": n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": n * d * 4,
                     "d2h_bytes_per_step": n * k * 8, "ms_per_step": e2e_s * 1e3}}
     print(json.dumps(line), flush=True)

@@ -73,7 +73,11 @@ typedef struct scrust_csr scrust_csr;
 /* How candidates are generated before the exact rerank. */
 typedef enum scrust_form {
     SCRUST_FORM_PLAIN = 0,  /* FP32 tiled expansion on CUDA cores (the drop-in) */
-    SCRUST_FORM_TENSOR = 1  /* 16-bit tcgen05/TMEM candidate GEMM, FP32 accumulate */
+    SCRUST_FORM_TENSOR = 1, /* 16-bit tcgen05/TMEM candidate GEMM, FP32 accumulate */
+    /* The tensor form wherever it applies (exact mode, at most 61
+     * dimensions), else the plain form.  Both give the same lists; the
+     * tensor form is the faster one. */
+    SCRUST_FORM_AUTO = 2
 } scrust_form;
 
 typedef enum scrust_metric {
@@ -115,8 +119,10 @@ typedef struct scrust_knn_options {
     uint32_t reserved[8];
 } scrust_knn_options;
 
-/* Fills `options` with the defaults: plain form, Euclidean, exact, FP16,
- * automatic ordering. */
+/* Fills `options` with the defaults: automatic form, Euclidean, exact, FP16,
+ * automatic ordering.  A kNN call asked for the tensor form where it does not
+ * apply runs the plain form (the same lists) and says so in the status
+ * message while returning SCRUST_OK. */
 SCRUST_API void scrust_knn_options_default(scrust_knn_options* options);
 
 /* 1 when a CUDA device of compute capability 10.3 is usable, else 0. */

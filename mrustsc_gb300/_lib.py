@@ -20,13 +20,13 @@ LIB_PATH = pathlib.Path(__file__).resolve().parent / "libscrust_cuda.so"
 
 OK, SHAPE, INVALID_PARAMETER, NO_GPU, KERNEL, NOT_CONVERGED, OOM, TIMEOUT = range(8)
 
-FORM_PLAIN, FORM_TENSOR = 0, 1
+FORM_PLAIN, FORM_TENSOR, FORM_AUTO = 0, 1, 2
 TENSOR_FORM_READY = True
 METRIC_EUCLIDEAN, METRIC_COSINE = 0, 1
 MODE_EXACT, MODE_REFERENCE_SNAP = 0, 1
 PRECISION_FP16, PRECISION_BF16 = 0, 1
 
-FORMS = {"plain": FORM_PLAIN, "tensor": FORM_TENSOR}
+FORMS = {"plain": FORM_PLAIN, "tensor": FORM_TENSOR, "auto": FORM_AUTO}
 METRICS = {"euclidean": METRIC_EUCLIDEAN, "cosine": METRIC_COSINE}
 MODES = {"exact": MODE_EXACT, "reference_snap": MODE_REFERENCE_SNAP}
 PRECISIONS = {"fp16": PRECISION_FP16, "bf16": PRECISION_BF16}
@@ -194,7 +194,7 @@ def context(device: int = 0) -> int:
         return _CONTEXTS[device]
 
 
-def options(form: str | int = "plain", metric: str | int = "euclidean", mode: str | int = "exact",
+def options(form: str | int = "auto", metric: str | int = "euclidean", mode: str | int = "exact",
             precision: str | int = "fp16", list_capacity: int = 0, segments: int = 0,
             ordering: str | int = "auto") -> KnnOptions:
     o = KnnOptions()

@@ -65,7 +65,7 @@ def _k(k) -> int:
     return k
 
 
-def knn(embedding, k, device, *, metric: str = "euclidean", form: str = "plain", mode: str = "exact",
+def knn(embedding, k, device, *, metric: str = "euclidean", form: str = "auto", mode: str = "exact",
         precision: str = "fp16", ordering: str = "auto", list_capacity: int = 0, segments: int = 0):
     """Exact k nearest neighbours, self excluded, nearest first, ties to the smaller id.
 
@@ -129,7 +129,7 @@ def smooth_knn_distances(distances):
     return sig, rho
 
 
-def neighbors_graph(embedding, k, device="auto", *, metric: str = "euclidean", form: str = "plain",
+def neighbors_graph(embedding, k, device="auto", *, metric: str = "euclidean", form: str = "auto",
                     mode: str = "exact", precision: str = "fp16"):
     """kNN and connectivities in one device pass: (indices, distances, (indptr, cols, vals, n))."""
     x = _array2(embedding, np.float32, "embedding")

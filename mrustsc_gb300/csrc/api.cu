@@ -157,8 +157,8 @@ int32_t check_knn_args(uint64_t n, uint64_t d, uint32_t k, scrust_status* st) {
 
 int32_t check_options(const scrust_knn_options* o, scrust_status* st) {
     if (!o) return SCRUST_OK;
-    if (o->form != SCRUST_FORM_PLAIN && o->form != SCRUST_FORM_TENSOR)
-        return fail(st, SCRUST_INVALID_PARAMETER, "form must be plain or tensor, got %d", o->form);
+    if (o->form != SCRUST_FORM_PLAIN && o->form != SCRUST_FORM_TENSOR && o->form != SCRUST_FORM_AUTO)
+        return fail(st, SCRUST_INVALID_PARAMETER, "form must be plain, tensor or auto, got %d", o->form);
     if (o->metric != SCRUST_METRIC_EUCLIDEAN && o->metric != SCRUST_METRIC_COSINE)
         return fail(st, SCRUST_INVALID_PARAMETER, "metric must be euclidean or cosine, got %d", o->metric);
     if (o->mode != SCRUST_MODE_EXACT && o->mode != SCRUST_MODE_REFERENCE_SNAP)
@@ -227,10 +227,27 @@ int32_t alloc_lists(scrust_context* ctx, int64_t rows_pad, Lists* lists, scrust_
 
 namespace {
 
-// Whether a solve runs the tensor form: it is asked for, the mode is exact,
-// and the row plus the three norm columns fits one 64-wide operand row.
+// Whether the tensor form applies: the mode is exact and the row plus the
+// three norm columns fits one 64-wide operand row.
+bool tensor_form_applies(const scrust_knn_options& o, int d) {
+    return o.mode == SCRUST_MODE_EXACT && d + 3 <= 64;
+}
+
+// Whether a solve runs the tensor form: asked for (or automatic) and applies.
 bool uses_tensor_form(const scrust_knn_options& o, int d) {
-    return o.form == SCRUST_FORM_TENSOR && o.mode == SCRUST_MODE_EXACT && d + 3 <= 64;
+    return (o.form == SCRUST_FORM_TENSOR || o.form == SCRUST_FORM_AUTO) && tensor_form_applies(o, d);
+}
+
+// Success, noting in the message when an explicit tensor-form request ran the
+// plain form instead.
+int32_t ok_form(scrust_status* st, const scrust_knn_options* opt, int d) {
+    ok(st);
+    if (st && opt && opt->form == SCRUST_FORM_TENSOR && !tensor_form_applies(*opt, d))
+        snprintf(st->message, sizeof(st->message),
+                 "ran the plain form: the tensor form needs exact mode and at most 61 dimensions, got %s mode "
+                 "and %d dimensions",
+                 opt->mode == SCRUST_MODE_EXACT ? "exact" : "reference_snap", d);
+    return SCRUST_OK;
 }
 
 // The kNN solve on device pointers, enqueued on ctx->stream.
@@ -451,7 +468,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
                            rerank_ids_only)) != cudaSuccess)
         return cuda_fail(st, e, "knn_rerank");
     mark(ctx, PH_RERANK);
-    return ok(st);
+    return ok_form(st, opt, d);
 }
 
 int32_t take_csr_buffers(scrust_context* ctx, uint64_t rows, uint64_t nnz_cap, CsrBuffers* out,
@@ -613,7 +630,7 @@ void scrust_knn_options_default(scrust_knn_options* o) {
     if (!o) return;
     memset(o, 0, sizeof(*o));
     o->struct_size = sizeof(*o);
-    o->form = SCRUST_FORM_PLAIN;
+    o->form = SCRUST_FORM_AUTO;
     o->metric = SCRUST_METRIC_EUCLIDEAN;
     o->mode = SCRUST_MODE_EXACT;
     o->precision = SCRUST_PRECISION_FP16;
@@ -754,7 +771,8 @@ int32_t scrust_cuda_knn(scrust_context* ctx, const float* x, uint64_t n, uint64_
         (e = cudaMemcpyAsync(out_dist, dd, sizeof(float) * n * k, cudaMemcpyDeviceToHost, ctx->stream)) !=
             cudaSuccess)
         return cuda_fail(st, e, "download");
-    return collect_device_errors(ctx, st);
+    if ((rc = collect_device_errors(ctx, st))) return rc;
+    return ok_form(st, opt, (int)d);
 }
 
 int32_t scrust_cuda_connectivities_device(scrust_context* ctx, const uint32_t* idx, const float* dist, uint64_t n,
@@ -837,7 +855,8 @@ int32_t scrust_cuda_neighbors_graph_device(scrust_context* ctx, const float* x, 
     std::lock_guard<std::mutex> lock(ctx->mu);
     DeviceGuard device_guard(ctx->device);
     if ((rc = knn_device_impl(ctx, x, n, d, k, opt, out_idx, out_dist, st))) return rc;
-    return conn_device_impl(ctx, out_idx, out_dist, n, k, false, conn, st);
+    if ((rc = conn_device_impl(ctx, out_idx, out_dist, n, k, false, conn, st))) return rc;
+    return ok_form(st, opt, (int)d);
 }
 
 int32_t scrust_cuda_neighbors_graph(scrust_context* ctx, const float* x, uint64_t n, uint64_t d, uint32_t k,
@@ -885,7 +904,8 @@ int32_t scrust_cuda_neighbors_graph(scrust_context* ctx, const float* x, uint64_
         return cuda_fail(st, e, "download");
     }
     if (rc) return rc;
-    return collect_device_errors(ctx, st);
+    if ((rc = collect_device_errors(ctx, st))) return rc;
+    return ok_form(st, opt, (int)d);
 }
 
 int32_t scrust_cuda_synchronize(scrust_context* ctx, scrust_status* st) {

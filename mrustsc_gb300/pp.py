@@ -16,7 +16,7 @@ METRICS = ("euclidean", "cosine")
 
 
 def neighbors(adata, *, n_neighbors: int = 15, use_rep: str = "X_pca", device: str = "auto",
-              metric: str = "euclidean", form: str = "plain") -> None:
+              metric: str = "euclidean", form: str = "auto") -> None:
     """Build the k-nearest-neighbour graph and its UMAP connectivities."""
     if n_neighbors < 2:
         raise ValueError(f"n_neighbors must be at least 2, got {n_neighbors}")
@@ -24,7 +24,7 @@ def neighbors(adata, *, n_neighbors: int = 15, use_rep: str = "X_pca", device: s
         raise ValueError(f"metric must be one of {list(METRICS)}, got {metric!r}")
     extension = _extension()
     # scanpy counts the cell itself among its n_neighbors; the core does not.
-    kwargs = {} if metric == "euclidean" and form == "plain" else {"metric": metric, "form": form}
+    kwargs = {} if metric == "euclidean" and form == "auto" else {"metric": metric, "form": form}
     indices, distances = extension.knn(_representation(adata, use_rep), n_neighbors - 1, device, **kwargs)
     indices = np.asarray(indices)
     distances = np.asarray(distances, dtype=_VALUE_DTYPE)

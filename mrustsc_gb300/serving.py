@@ -99,33 +99,50 @@ def _replay(server: Server, times, queries):
     return np.asarray(lat), time.perf_counter() - t0
 
 
+def fixed_load(duration_s: float = 3.0, rate: float = 200.0, m: int = 500_000, d: int = 50, k: int = 15,
+               slots: int = 2, max_batch_cells: int = 65536, seed: int = 1) -> dict:
+    """One replay of the serving workload at a fixed offered load: a seeded
+    Poisson stream (`rate` requests/s for `duration_s`, query sizes
+    log-uniform in [1, 20,000]) against an m x d atlas of 100 clusters.
+    Returns p50/p99/mean latency (ms, submit to answer), answered cells/s,
+    the service's counters (batches, most batches on the GPU at once, ...)
+    and the workload's shape."""
+    from . import synthetic
+
+    atlas, centres = synthetic.serving_atlas(seed=0, m=m, d=d)
+    times, counts = synthetic.poisson_arrivals(rate, duration_s, seed=seed)
+    queries = [synthetic.serving_queries(centres, int(c), seed=100 + i) for i, c in enumerate(counts)]
+    cells = int(counts.sum())
+    with Server(atlas, k, slots=slots, max_batch_cells=max_batch_cells) as sv:
+        sv.query(queries[0][:8])  # warm-up: workspaces and kernels
+        lat, wall = _replay(sv, times, queries)
+        st = sv.stats()
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "cells_per_s": cells / wall, "wall_s": wall,
+            "requests": len(times), "query_cells": cells, "rate_per_s": rate, "duration_s": duration_s,
+            "atlas_cells": m, "k": k, "slots": slots, "batches": st["batches"],
+            "max_batches_in_flight": st["max_batches_in_flight"], "answered": st["requests"]}
+
+
 def bench_main(args) -> int:
     """Serving workload: a 500,000 x 50 atlas (100 clusters) resident in HBM; Poisson arrivals
     at 200 requests/s; query sizes log-uniform in [1, 20,000]; k = 15 plus connectivity rows.
     Continuous batching (2 slots) against per-request launches (1 slot, one request per batch)."""
-    from . import build, synthetic
+    from . import build
 
     build.build()
     m, d, k = 500_000, 50, 15
     rate, duration = 200.0, float(getattr(args, "serve_seconds", 0) or 5.0)
-    atlas, centres = synthetic.serving_atlas(seed=0, m=m, d=d)
-    times, counts = synthetic.poisson_arrivals(rate, duration, seed=1)
-    queries = [synthetic.serving_queries(centres, int(c), seed=100 + i) for i, c in enumerate(counts)]
-    cells = int(counts.sum())
     result = {}
     for name, slots, max_cells in (("continuous", 2, 65536), ("per_request", 1, 1)):
-        with Server(atlas, k, slots=slots, max_batch_cells=max_cells) as sv:
-            sv.query(queries[0][:8])  # warm-up: workspaces and kernels
-            lat, wall = _replay(sv, times, queries)
-            st = sv.stats()
-        result[name] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                        "mean_ms": float(lat.mean()), "cells_per_s": cells / wall, "wall_s": wall, **st}
+        result[name] = fixed_load(duration, rate, m, d, k, slots=slots, max_batch_cells=max_cells)
     c = result["continuous"]
     line = {"metric": "serving p99 latency at 200 req/s (500k x 50 atlas, k = 15)", "value": c["p99_ms"],
-            "unit": "ms", "n_gpus": 1, "steps": len(times), "warmup": 1, "ms_per_step": c["mean_ms"],
+            "unit": "ms", "n_gpus": 1, "steps": c["requests"], "warmup": 1, "ms_per_step": c["mean_ms"],
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f16", "data": "synthetic",
             "config": {"workload": "serving_500k_x50_k15", "atlas_cells": m, "dims": d, "k": k,
-                       "rate_per_s": rate, "duration_s": duration, "requests": len(times), "query_cells": cells,
+                       "rate_per_s": rate, "duration_s": duration, "requests": c["requests"],
+                       "query_cells": c["query_cells"],
                        "query_sizes": "log-uniform [1, 20000], seed 1", "budget": "150 GiB"},
             "p50_ms": c["p50_ms"], "p99_ms": c["p99_ms"], "cells_per_s": c["cells_per_s"],
             "comparator": result["per_request"], "continuous": c}

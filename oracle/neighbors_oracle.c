@@ -350,6 +350,67 @@ int oracle_knn_reference_cpu_rows(const float* x, int64_t n, int64_t d, int64_t 
 }
 
 /*
+ * The reference CPU path split where a BLAS takes over, for timing it on the
+ * host the way it runs (candle hands the tile product of neighbors.rs:74 to
+ * gemm's SGEMM microkernels):
+ *   oracle_centred_norms   centred coordinates (neighbors.rs:144-162) and
+ *                          squared norms (:62, sequential f32 sums);
+ *   oracle_expansion_select  given G = T . P^T for a tile of query rows (the
+ *                          caller's SGEMM), raw = (-2 G) + (|a|^2 + |b|^2),
+ *                          the snap below (D+2) eps (|a|^2 + |b|^2) (:75-82)
+ *                          and select_nearest (:171-191), rows in parallel.
+ */
+int oracle_centred_norms(const float* x, int64_t n, int64_t d, float* c, float* sq) {
+    int rc = check_knn_args(n, d, 1 < n ? 1 : 0);
+    if (rc) return rc;
+    rc = oracle_centred(x, n, d, c);
+    if (rc) return rc;
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < n; r++) {
+        float s = 0.0f;
+        for (int64_t t = 0; t < d; t++) {
+            float v = c[r * d + t] * c[r * d + t];
+            s = s + v;
+        }
+        sq[r] = s;
+    }
+    return ORACLE_OK;
+}
+
+int oracle_expansion_select(const float* g, int64_t h, int64_t n, int64_t d, const int64_t* rows,
+                            const float* sq, int64_t k, uint32_t* idx, float* dist) {
+    int rc = check_knn_args(n, d, k);
+    if (rc) return rc;
+    const float resolution = ((float)d + 2.0f) * F32_EPS;
+    int failed = 0;
+#pragma omp parallel
+    {
+        float* row = (float*)malloc(sizeof(float) * (size_t)n);
+        pair_f32* buf = (pair_f32*)malloc(sizeof(pair_f32) * (size_t)n);
+        if (!row || !buf) {
+#pragma omp atomic write
+            failed = 1;
+        } else {
+#pragma omp for schedule(dynamic, 1)
+            for (int64_t r = 0; r < h; r++) {
+                const int64_t i = rows[r];
+                const float* gr = g + r * n;
+                for (int64_t col = 0; col < n; col++) {
+                    float sums = sq[i] + sq[col];
+                    float raw = (-2.0f * gr[col]) + sums;
+                    float floor_ = sums * resolution;
+                    row[col] = raw < floor_ ? 0.0f : raw;
+                }
+                select_nearest(row, n, i, k, buf, idx + r * k, dist + r * k);
+            }
+        }
+        free(row);
+        free(buf);
+    }
+    return failed ? ORACLE_OOM : ORACLE_OK;
+}
+
+/*
  * CPU twin of the reference's Metal kernel, knn.rs:282-313 with
  * centre_and_norms (:135-158): centred coordinates, norms by an fmaf chain,
  * the difference form sum fma(a-b, a-b) in dimension order (:223-232), the
@@ -487,6 +548,63 @@ int oracle_knn_fp64_rows(const float* x, int64_t n, int64_t d, int64_t k, const 
                 for (int64_t j = 0; j < n; j++) {
                     if (j == q) continue;
                     double s = sq_dist_f64_below(x + q * d, x + j * d, d, limit);
+                    if (s > limit) continue;
+                    double v = sqrt(s > 0.0 ? s : 0.0);
+                    pair_f64 cnd = {v, (uint32_t)j};
+                    if (have == k) {
+                        pair_f64 w = top[k - 1];
+                        if (!(v < w.d || (v == w.d && cnd.id < w.id))) continue;
+                        have--;
+                    }
+                    int64_t s2 = have;
+                    while (s2 > 0 &&
+                           (v < top[s2 - 1].d || (v == top[s2 - 1].d && cnd.id < top[s2 - 1].id))) {
+                        top[s2] = top[s2 - 1];
+                        s2--;
+                    }
+                    top[s2] = cnd;
+                    have++;
+                    if (have == k) {
+                        double kth = top[k - 1].d;
+                        limit = kth * kth * (1.0 + 1e-12);
+                    }
+                }
+                for (int64_t t = 0; t < k; t++) {
+                    idx[r * k + t] = top[t].id;
+                    if (d64) d64[r * k + t] = top[t].d;
+                    if (dist) dist[r * k + t] = (float)top[t].d;
+                }
+            }
+        }
+        free(top);
+    }
+    return failed ? ORACLE_OOM : ORACLE_OK;
+}
+
+/*
+ * FP64 exact kNN of query rows against reference rows (the serving form's
+ * semantics: no self-exclusion, ids index the reference): the same
+ * dimension-order FP64 sum, sqrt, (d, id) order and exact early exit as
+ * oracle_knn_fp64_rows.  Outputs (nq, k).
+ */
+int oracle_knn_fp64_cross(const float* q, int64_t nq, const float* ref, int64_t nr, int64_t d, int64_t k,
+                          uint32_t* idx, double* d64, float* dist) {
+    if (nq <= 0 || nr <= 0 || d <= 0) return ORACLE_SHAPE;
+    if (k <= 0 || k > nr) return ORACLE_INVALID_PARAMETER;
+    int failed = 0;
+#pragma omp parallel
+    {
+        pair_f64* top = (pair_f64*)malloc(sizeof(pair_f64) * (size_t)(k + 1));
+        if (!top) {
+#pragma omp atomic write
+            failed = 1;
+        } else {
+#pragma omp for schedule(dynamic, 4)
+            for (int64_t r = 0; r < nq; r++) {
+                int64_t have = 0;
+                double limit = INFINITY;
+                for (int64_t j = 0; j < nr; j++) {
+                    double s = sq_dist_f64_below(q + r * d, ref + j * d, d, limit);
                     if (s > limit) continue;
                     double v = sqrt(s > 0.0 ? s : 0.0);
                     pair_f64 cnd = {v, (uint32_t)j};

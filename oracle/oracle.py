@@ -8,8 +8,10 @@ library never imports it.
 
 Functions mirror the reference files they restate:
   knn_reference_cpu  crates/scrust-core/src/neighbors.rs:29-101, 171-191
+  ExpansionCPU       the same with the tile product on a BLAS SGEMM
   knn_metal_twin     crates/scrust-gpu/src/kernels/knn.rs:135-158, 282-313
   knn_fp64           tests/test_neighbors_audit.py:52-61
+  knn_fp64_cross_c   the same for query rows against reference rows
   smooth_knn         crates/scrust-core/src/neighbors.rs:239-298
   connectivities     crates/scrust-core/src/neighbors.rs:208-372
 """
@@ -68,6 +70,9 @@ def _lib():
             lib.oracle_knn_metal_twin.argtypes = [f32p, i64, i64, i64, u32p, f32p]
             lib.oracle_knn_fp64_rows.argtypes = [f32p, i64, i64, i64, i64p, i64, u32p, f64p, f32p]
             lib.oracle_knn_cosine_fp64_rows.argtypes = [f32p, i64, i64, i64, i64p, i64, u32p, f64p, f32p]
+            lib.oracle_knn_fp64_cross.argtypes = [f32p, i64, f32p, i64, i64, i64, u32p, f64p, f32p]
+            lib.oracle_centred_norms.argtypes = [f32p, i64, i64, f32p, f32p]
+            lib.oracle_expansion_select.argtypes = [f32p, i64, i64, i64, i64p, f32p, i64, u32p, f32p]
             lib.oracle_smooth_knn.argtypes = [f32p, i64, i64, f32p, f32p]
             lib.oracle_connectivities.argtypes = [u32p, f32p, i64, i64, u32p, u32p, f32p, i64p]
             lib.oracle_directed_weights.argtypes = [u32p, f32p, i64, i64, f32p]
@@ -124,6 +129,41 @@ def knn_reference_cpu_rows(x, k: int, rows):
                                                 _p(idx, ctypes.c_uint32), _p(dist, ctypes.c_float)),
            "knn_reference_cpu_rows")
     return idx, dist
+
+
+class ExpansionCPU:
+    """The reference CPU kNN (neighbors.rs:29-101) with its tile product on a
+    BLAS, as candle runs it: centred coordinates and squared norms are made
+    once (the setup of knn_tiled), then each tile of query rows is one SGEMM
+    (numpy's BLAS, all host threads) followed by the affine, snap and
+    selection in C (all host threads).  Used to time the reference's CPU path
+    on a sample of query rows; tiles are MAX_TILE_ELEMENTS = 64 Mi wide as in
+    neighbors.rs:30."""
+
+    TILE_ELEMENTS = 64 * 1024 * 1024
+
+    def __init__(self, x):
+        x = _f32(x)
+        self.n, self.d = x.shape
+        self.c = np.zeros_like(x)
+        self.sq = np.zeros(self.n, np.float32)
+        _check(_lib().oracle_centred_norms(_p(x, ctypes.c_float), self.n, self.d, _p(self.c, ctypes.c_float),
+                                           _p(self.sq, ctypes.c_float)), "centred_norms")
+        self.ct = np.ascontiguousarray(self.c.T)
+        self.tile_rows = max(1, self.TILE_ELEMENTS // max(1, self.n))
+
+    def knn_rows(self, k: int, rows):
+        rows = np.ascontiguousarray(rows, dtype=np.int64)
+        idx = np.zeros((len(rows), k), np.uint32)
+        dist = np.zeros((len(rows), k), np.float32)
+        for a in range(0, len(rows), self.tile_rows):
+            r = rows[a:a + self.tile_rows]
+            g = np.ascontiguousarray(self.c[r] @ self.ct, dtype=np.float32)
+            _check(_lib().oracle_expansion_select(_p(g, ctypes.c_float), len(r), self.n, self.d,
+                                                  _p(r, ctypes.c_int64), _p(self.sq, ctypes.c_float), k,
+                                                  _p(idx[a:], ctypes.c_uint32), _p(dist[a:], ctypes.c_float)),
+                   "expansion_select")
+        return idx, dist
 
 
 def knn_metal_twin(x, k: int):
@@ -218,6 +258,23 @@ def exact_knn_numpy(x, k: int):
         order = sorted((j for j in range(n) if j != cell), key=lambda j: (d[cell, j], j))
         indices[cell] = order[:k]
     return indices, np.take_along_axis(d, indices, 1)
+
+
+def knn_fp64_cross_c(queries, reference, k: int):
+    """Exact k nearest reference rows of every query row in FP64 (the C
+    restatement, any size): (idx u32, d64 f64, dist f32), the semantics of
+    tests/test_neighbors_audit.py:52-61 for a query-versus-reference solve
+    with no self-exclusion and the lowest reference index on ties."""
+    q = _f32(queries)
+    r = _f32(reference)
+    nq, d = q.shape
+    idx = np.zeros((nq, k), np.uint32)
+    d64 = np.zeros((nq, k), np.float64)
+    dist = np.zeros((nq, k), np.float32)
+    _check(_lib().oracle_knn_fp64_cross(_p(q, ctypes.c_float), nq, _p(r, ctypes.c_float), r.shape[0], d, k,
+                                        _p(idx, ctypes.c_uint32), _p(d64, ctypes.c_double),
+                                        _p(dist, ctypes.c_float)), "knn_fp64_cross")
+    return idx, d64, dist
 
 
 def knn_fp64_cross(queries, reference, k: int):

@@ -1,6 +1,8 @@
 """Connectivities on the GPU against the oracle's restatement of
 crates/scrust-core/src/neighbors.rs:208-372: CSR structure bit-exact, values
-within 1e-5 absolute, sigma/rho within 1e-5 relative; plus the reference's own
+within 1e-5 absolute, rho exact, sigma within 1e-5 relative (5e-5 on large
+random inputs, where expf's last ulp can move the bisection's stop by one
+step), the global mean in the reference's own f32 order; plus the reference's own
 golden vectors (neighbors.rs:498-590) and invariants (:468-491), and the
 pp.neighbors surface end to end."""
 
@@ -19,6 +21,12 @@ from mrustsc_gb300 import synthetic
 pytestmark = pytest.mark.gpu
 
 CONN_ATOL = 1e-5
+# The bisection stops once |cardinality - log2(k + 1)| < 1e-5; CUDA's expf and
+# the host's expf differ by an ulp on some terms, which can move that stop by
+# one step on a few rows of a large random input.  Both stopping points lie
+# within the 1e-5 band, so sigma moves by at most about 2e-5 relative (and a
+# weight exp(-o / sigma) by less than 1e-5 absolute).
+SIGMA_BISECTION_RTOL = 5e-5
 GOLDEN = pathlib.Path(__file__).resolve().parent / "golden" / "scanpy_reference_embedding_300x20.json"
 
 
@@ -77,7 +85,7 @@ def test_global_mean_in_the_reference_order(scrust, oracle, n, k):
     np.testing.assert_array_equal(r_gpu, r_ref)
     zero = r_ref == 0
     np.testing.assert_array_equal(s_gpu[zero], s_ref[zero])
-    np.testing.assert_allclose(s_gpu, s_ref, rtol=1e-5)
+    np.testing.assert_allclose(s_gpu, s_ref, rtol=SIGMA_BISECTION_RTOL)
 
 
 def test_scanpy_golden_vectors_through_the_gpu(scrust):

@@ -274,3 +274,38 @@ def test_scale_workload_sampled_rows_match_fp64(scrust, oracle, form):
     assert_exact(oracle, x, 30, idx, dist, rows=rows)
     ci, cd = scrust.knn(x, 30, "auto", metric="cosine", **kw(form))
     assert_exact(oracle, x, 30, ci, cd, rows=rows[:150], metric="cosine")
+
+
+def test_default_form_runs_the_tensor_sweep_and_notes_fallbacks(scrust, oracle):
+    """The default options pick the tensor form where it applies (exact mode,
+    d <= 61: the sweep's own tile counter moves); an explicit tensor request
+    it cannot serve runs the plain form, returns OK and says so."""
+    import ctypes
+
+    from mrustsc_gb300 import _lib
+
+    L = _lib.lib()
+    ctx = _lib.context(0)
+    st = _lib.Status()
+    opts = _lib.KnnOptions()
+    L.scrust_knn_options_default(ctypes.byref(opts))
+    assert opts.form == _lib.FORM_AUTO
+    x = synthetic.mixture(3000, 50, clusters=6, dup_frac=0.01, seed=41)
+    idx = np.empty((3000, 15), np.uint32)
+    dist = np.empty((3000, 15), np.float32)
+    cnt = (ctypes.c_uint64 * 16)()
+    L.scrust_cuda_kernel_stats(ctx, 1, cnt, 16)
+    _lib.check(L.scrust_cuda_knn(ctx, _lib.ptr(x), 3000, 50, 15, ctypes.byref(opts), _lib.ptr(idx), _lib.ptr(dist),
+                                 ctypes.byref(st)), st)
+    L.scrust_cuda_kernel_stats(ctx, 0, cnt, 16)
+    assert cnt[8] > 0  # (row block, column tile) pairs of the tensor sweep
+    assert st.message.decode() == ""
+    assert_exact(oracle, x, 15, idx, dist)
+    x100 = synthetic.mixture(800, 100, clusters=4, dup_frac=0.01, seed=42)
+    tensor = _lib.options(form="tensor")
+    idx = np.empty((800, 15), np.uint32)
+    dist = np.empty((800, 15), np.float32)
+    rc = L.scrust_cuda_knn(ctx, _lib.ptr(x100), 800, 100, 15, ctypes.byref(tensor), _lib.ptr(idx), _lib.ptr(dist),
+                           ctypes.byref(st))
+    assert rc == _lib.OK and "ran the plain form" in st.message.decode()
+    assert_exact(oracle, x100, 15, idx, dist)

@@ -96,3 +96,51 @@ def test_metric_is_forwarded_and_recorded(core):
     assert adata.uns["neighbors"]["params"]["metric"] == "cosine"
     with pytest.raises(ValueError):
         pp.neighbors(adata, metric="manhattan")
+
+
+class RecordingBackend(FakeCore):
+    """Stands in for this backend in the routing tests (no GPU needed)."""
+
+    def gpu_available(self):
+        return True
+
+
+@pytest.mark.parametrize("device", ["auto", "gpu", "cuda", "metal"])
+def test_core_routes_non_cpu_knn_to_this_backend(device):
+    from mrustsc_gb300.core import Core
+
+    real, ours = FakeCore(), RecordingBackend()
+    core = Core(real, device_setting=lambda: "auto", backend=ours)
+    x = np.zeros((6, 3), np.float32)
+    core.knn(x, 2, device)
+    core.connectivities(np.zeros((6, 2), np.uint32), np.ones((6, 2), np.float32))
+    assert [c[0] for c in ours.calls] == ["knn", "connectivities"] and real.calls == []
+    assert ours.args_of("knn")[2] == device
+
+
+def test_core_routes_cpu_to_the_reference_module():
+    from mrustsc_gb300.core import Core
+
+    real, ours = FakeCore(), RecordingBackend()
+    core = Core(real, device_setting=lambda: "cpu", backend=ours)
+    x = np.zeros((6, 3), np.float32)
+    core.knn(x, 2, "cpu")
+    core.connectivities(np.zeros((6, 2), np.uint32), np.ones((6, 2), np.float32))
+    assert [c[0] for c in real.calls] == ["knn", "connectivities"] and ours.calls == []
+    # every other attribute is the reference module's
+    real.pca = lambda *a: "pca"
+    assert core.pca() == "pca"
+
+
+def test_unmodified_neighbors_surface_through_the_core_on_cpu(monkeypatch):
+    """pp.neighbors(device="cpu") through the swapped module reaches the
+    reference's own core (a FakeCore here), arguments unchanged."""
+    from mrustsc_gb300 import core as core_mod
+
+    real, ours = FakeCore(), RecordingBackend()
+    swapped = core_mod.Core(real, device_setting=lambda: "cpu", backend=ours)
+    monkeypatch.setattr(pp, "_extension", lambda: swapped)
+    adata = _adata()
+    pp.neighbors(adata, n_neighbors=4, device="cpu")
+    assert real.args_of("knn")[1:] == (3, "cpu") and ours.calls == []
+    assert adata.obsp["distances"].shape == (N_OBS, N_OBS)
