@@ -547,8 +547,10 @@ def run_sharded(args, world: int, rank: int, local: int):
 # --------------------------------------------------------------------------- batching
 
 def run_batching(args):
-    """64 samples (sizes log-uniform in [500, 50,000], 4-20 clusters each, k = 15): one CUDA-graph
-    launch of the batched tensor sweep, against 64 sequential plain-form launches on the same data."""
+    """64 samples (sizes log-uniform in [500, 50,000], 4-20 clusters each, k = 15): every sample's graph
+    (kNN + UMAP connectivities) in one CUDA-graph launch of the batched tensor sweep and the batch's
+    fuzzy union, against the kNN-only plan, 64 sequential plain launches and 64 sequential tensor
+    launches on the same data."""
     import torch
 
     from mrustsc_gb300 import _lib, build, synthetic
@@ -567,16 +569,23 @@ def run_batching(args):
     xd = torch.from_numpy(x).cuda()
     idx = torch.empty((n, k), dtype=torch.int32, device="cuda")
     dst = torch.empty((n, k), dtype=torch.float32, device="cuda")
+    gidx = torch.empty((n, k), dtype=torch.int32, device="cuda")
+    gdst = torch.empty((n, k), dtype=torch.float32, device="cuda")
     st = _lib.Status()
     opts = _lib.options(form="tensor")
     t0 = time.perf_counter()
+    gplan = L.scrust_cuda_batch_plan_create_graphs(ctx, _lib.ptr(offsets), len(samples), d, k, ctypes.byref(opts),
+                                                   xd.data_ptr(), gidx.data_ptr(), gdst.data_ptr(), ctypes.byref(st))
+    if not gplan:
+        raise RuntimeError(st.message.decode())
+    plan_s = time.perf_counter() - t0
     plan = L.scrust_cuda_batch_plan_create(ctx, _lib.ptr(offsets), len(samples), d, k, ctypes.byref(opts),
                                            xd.data_ptr(), idx.data_ptr(), dst.data_ptr(), ctypes.byref(st))
     if not plan:
         raise RuntimeError(st.message.decode())
-    plan_s = time.perf_counter() - t0
     cap, prec, tuned = ctypes.c_uint32(), ctypes.c_int32(), ctypes.c_float()
-    L.scrust_cuda_batch_plan_choice(plan, ctypes.byref(cap), ctypes.byref(prec), ctypes.byref(tuned))
+    L.scrust_cuda_batch_plan_choice(gplan, ctypes.byref(cap), ctypes.byref(prec), ctypes.byref(tuned))
+    width = int(L.scrust_cuda_batch_plan_topk_width(gplan))
 
     def timed(fn, steps, warmup):
         for _ in range(warmup):
@@ -593,11 +602,30 @@ def run_batching(args):
     clocks = ClockSampler(0)
     clocks.start()
     launches0 = L.scrust_cuda_launch_count(ctx)
-    ms_graph = timed(lambda: _lib.check(L.scrust_cuda_batch_plan_launch(plan, ctypes.byref(st)), st),
-                     args.steps, args.warmup)
+    ms_graphs = timed(lambda: _lib.check(L.scrust_cuda_batch_plan_launch(gplan, ctypes.byref(st)), st),
+                      args.steps, args.warmup)
     launches = int(L.scrust_cuda_launch_count(ctx) - launches0)
     clk = clocks.stop()
-    graph_idx = idx.clone()
+    ms_knn = timed(lambda: _lib.check(L.scrust_cuda_batch_plan_launch(plan, ctypes.byref(st)), st),
+                   args.steps, args.warmup)
+    _lib.check(L.scrust_cuda_synchronize(ctx, ctypes.byref(st)), st)
+    # The graph plan's CSR, read through the CUDA array interface.
+    ip, ix, vl = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    L.scrust_cuda_batch_plan_graph(gplan, ctypes.byref(ip), ctypes.byref(ix), ctypes.byref(vl))
+
+    class DeviceView:
+        def __init__(self, ptr, count, typestr):
+            self.__cuda_array_interface__ = {"shape": (count,), "typestr": typestr, "data": (ptr, False),
+                                             "version": 2}
+
+    def grab(ptr, count, typestr):
+        return torch.as_tensor(DeviceView(ptr.value, count, typestr), device="cuda").cpu().numpy()
+
+    indptr = grab(ip, n + 1, "<u4")
+    nnz = int(indptr[-1])
+    cols, vals = grab(ix, nnz, "<u4"), grab(vl, nnz, "<f4")
+    graph_idx = gidx.clone()
+    graph_dist = gdst.clone()
 
     plain = _lib.options(form="plain")
     views = [(xd[int(offsets[s]):int(offsets[s + 1])], idx[int(offsets[s]):int(offsets[s + 1])],
@@ -610,30 +638,41 @@ def run_batching(args):
                                                     ii.data_ptr(), dd.data_ptr(), ctypes.byref(st)), st)
         return run
 
-    graph_dist = dst.clone()
     seq_steps = max(1, min(args.steps, 3))
     ms_plain = timed(sequential(plain), seq_steps, 1)
     same = bool((graph_idx == idx).all().item())
     ms_tensor_seq = timed(sequential(opts), seq_steps, 1)
     L.scrust_cuda_batch_plan_destroy(plan)
+    L.scrust_cuda_batch_plan_destroy(gplan)
 
-    # e2e through the host-pointer batch call: upload, solve, download, from and
-    # into pinned host buffers (one untimed call first, as for the main e2e).
+    # e2e through the host-pointer batch graph call: upload, graphs, download of
+    # the kNN rows and the CSR, from and into pinned host buffers (one untimed
+    # call first, as for the main e2e).
     ih = torch.empty((n, k), dtype=torch.int32).pin_memory()
     dh = torch.empty((n, k), dtype=torch.float32).pin_memory()
     xh = torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = max(1, args.steps)
+    e2e_nnz = 0
+    times = []
     for it in range(e2e_steps + 1):
-        if it == 1:
-            t0 = time.perf_counter()
-        _lib.check(L.scrust_cuda_knn_batch(ctx, xh.data_ptr(), _lib.ptr(offsets), len(samples), d, k,
-                                           ctypes.byref(opts), ih.data_ptr(), dh.data_ptr(), ctypes.byref(st)), st)
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+        t0 = time.perf_counter()
+        out = ctypes.c_void_p()
+        _lib.check(L.scrust_cuda_neighbors_graph_batch(ctx, xh.data_ptr(), _lib.ptr(offsets), len(samples), d, k,
+                                                       ctypes.byref(opts), ih.data_ptr(), dh.data_ptr(),
+                                                       ctypes.byref(out), ctypes.byref(st)), st)
+        e2e_nnz = int(L.scrust_csr_nnz(out))
+        L.scrust_csr_free(out)
+        if it:
+            times.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(times)
     flops = sum(2.0 * m * m * d for m in sizes)
-    parity_rep = None
+    parity_rep = conn_rep = None
     if not args.no_recall:
         # Every sample: 64 random rows and up to 64 rows with a zero-distance
-        # neighbour against the FP64 kNN of that sample (outside the timing).
+        # neighbour against the FP64 kNN of that sample, and the sample's whole
+        # CSR against the restated connectivities of its kNN graph (outside
+        # the timing).
+        from mrustsc_gb300._scrust import split_batch_graph
         from oracle import oracle, parity
 
         oracle.build()
@@ -641,31 +680,41 @@ def run_batching(args):
         gd = graph_dist.cpu().numpy()
         rng = np.random.default_rng(1)
         rows_total, exact, worst = 0, 0, 0.0
-        for s_i, xs in enumerate(samples):
-            a, b = int(offsets[s_i]), int(offsets[s_i + 1])
-            rows = np.unique(np.concatenate([rng.choice(b - a, min(b - a, 64), replace=False),
-                                             np.nonzero(gd[a:b, 0] == 0)[0][:64]]))
-            rep = parity.knn_rows_report(xs, k, gi[a:b], gd[a:b], rows)
+        c_ok, c_err = 0, 0.0
+        for s_i, (xs, (si, sd, csr)) in enumerate(zip(samples, split_batch_graph(offsets, gi, gd, indptr, cols,
+                                                                                 vals))):
+            rows = np.unique(np.concatenate([rng.choice(len(xs), min(len(xs), 64), replace=False),
+                                             np.nonzero(sd[:, 0] == 0)[0][:64]]))
+            rep = parity.knn_rows_report(xs, k, si, sd, rows)
             rows_total += rep["rows"]
             exact += rep["exact_rows"]
             worst = max(worst, rep["max_rel_dist_err"])
+            crep = parity.connectivities_report(si, sd, csr)
+            c_ok += int(parity.connectivities_ok(crep))
+            c_err = max(c_err, crep["max_abs_err"] or float("inf"))
         parity_rep = {"samples": len(samples), "rows": rows_total, "exact_rows": exact, "max_rel_dist_err": worst,
                       "against": "FP64 exact kNN of each sample (C oracle)"}
-    line = {"metric": "batched kNN cells/s (64 samples, one CUDA-graph launch)", "value": n / (ms_graph / 1e3),
-            "unit": "cells/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_graph,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16" if prec.value == 0 else "bf16",
-            "data": "synthetic",
+        conn_rep = {"samples": len(samples), "samples_equal": c_ok, "max_abs_err": c_err, "nnz": nnz,
+                    "against": "restated connectivities of each sample's kNN graph (C oracle)"}
+    line = {"metric": "batched kNN-graph cells/s (64 samples, kNN + connectivities, one CUDA-graph launch)",
+            "value": n / (ms_graphs / 1e3), "unit": "cells/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_graphs, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f16" if prec.value == 0 else "bf16", "data": "synthetic",
             "config": {"workload": "batching_64_samples_k15", "samples": len(samples), "cells": n, "dims": d, "k": k,
                        "sizes": "log-uniform [500, 50000], seed 0", "sum_2n2d_flop": flops,
                        "l2": "inputs and lists larger than L2"},
-            "comparator": {"sequential_plain_ms": ms_plain, "sequential_tensor_ms": ms_tensor_seq,
-                           "speedup_vs_sequential_plain": ms_plain / ms_graph,
-                           "results_identical_to_sequential_plain": same},
-            "autotuner": {"list_capacity": cap.value, "precision": "fp16" if prec.value == 0 else "bf16",
-                          "tuned_ms": tuned.value, "plan_create_s": plan_s},
-            "gpu_launches": launches, "clocks": clk, "recall_fp64_sample": parity_rep,
+            "comparator": {"knn_only_plan_ms": ms_knn, "graphs_over_knn_only": ms_graphs / ms_knn,
+                           "sequential_plain_knn_ms": ms_plain, "sequential_tensor_knn_ms": ms_tensor_seq,
+                           "speedup_vs_sequential_plain": ms_plain / ms_graphs,
+                           "knn_identical_to_sequential_plain": same},
+            "autotuner": {"list_capacity": cap.value, "topk_width": width,
+                          "precision": "fp16" if prec.value == 0 else "bf16", "tuned_ms": tuned.value,
+                          "plan_create_s": plan_s,
+                          "fixed": "tile shape (2 x 128-row MMA halves x 256-column tiles, K = 64)"},
+            "gpu_launches": launches, "clocks": clk, "recall_fp64_sample": parity_rep, "conn_check": conn_rep,
             "e2e": {"value": n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": n * d * 4,
-                    "d2h_bytes_per_step": n * k * 8, "ms_per_step": e2e_s * 1e3}}
+                    "d2h_bytes_per_step": n * k * 8 + (n + 1) * 4 + e2e_nnz * 8, "ms_per_step": e2e_s * 1e3,
+                    "steps": e2e_steps}}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -28,6 +28,8 @@
  *                                    crates/scrust-core/src/sparse.rs:10-90
  *   scrust_cuda_neighbors_graph      the two FFI calls of python/scrust/pp/_basics.py:198,209
  *                                    fused into one device pass
+ *   scrust_cuda_umap                 scrust_core::umap::umap
+ *                                    crates/scrust-core/src/umap.rs:64
  * Entry points with no reference counterpart (new semantics, parity against
  * the FP64 oracle only): scrust_cuda_knn_batched (many samples in one launch)
  * and the scrust_serve_* query service (queries against a resident atlas).
@@ -250,10 +252,11 @@ SCRUST_API int32_t scrust_cuda_knn_batch_device(scrust_context* context, const f
                                                 const uint64_t* row_offsets, uint32_t n_samples, uint64_t d,
                                                 uint32_t k, const scrust_knn_options* options,
                                                 uint32_t* out_indices, float* out_distances, scrust_status* status);
-/* A plan fixes the layout and the device buffers, autotunes the list
- * capacity (when options->list_capacity is 0) and the operand precision on
- * this batch, and captures the whole solve in a CUDA graph.  Each launch is
- * one graph launch on the context stream. */
+/* A plan fixes the layout and the device buffers, autotunes the candidate
+ * over-provisioning (the list capacity, when options->list_capacity is 0),
+ * the sweep's register top-k width and the operand precision on this batch,
+ * and captures the whole solve in a CUDA graph.  Each launch is one graph
+ * launch on the context stream. */
 SCRUST_API scrust_batch_plan* scrust_cuda_batch_plan_create(scrust_context* context, const uint64_t* row_offsets,
                                                             uint32_t n_samples, uint64_t d, uint32_t k,
                                                             const scrust_knn_options* options,
@@ -263,6 +266,37 @@ SCRUST_API int32_t scrust_cuda_batch_plan_launch(scrust_batch_plan* plan, scrust
 /* The autotuner's choice and its time for one batch; returns 0 for NULL. */
 SCRUST_API int32_t scrust_cuda_batch_plan_choice(const scrust_batch_plan* plan, uint32_t* list_capacity,
                                                  int32_t* precision, float* tuned_ms);
+/* The register top-k width the autotuner chose for the sweep: 16 or 32, or 0
+ * for candidate lists alone (warp-cooperative prunes); -1 for NULL. */
+SCRUST_API int32_t scrust_cuda_batch_plan_topk_width(const scrust_batch_plan* plan);
+
+/* Graphs of many samples.  A plan made by scrust_cuda_batch_plan_create_graphs
+ * also builds every sample's UMAP connectivities inside the same captured
+ * launch: smooth_knn, exp weights and the fuzzy union of that sample's rows
+ * alone (crates/scrust-core/src/neighbors.rs:208-372 applied per sample),
+ * into one device CSR of sum(n_s) rows in input order whose column ids are
+ * relative to each sample's first row.  Sample s's own CSR is rows
+ * [row_offsets[s], row_offsets[s+1]): indptr over those rows less
+ * indptr[row_offsets[s]], and the entries between.  The arrays belong to the
+ * plan and hold the last launch's graph once the context stream has
+ * synchronised; nnz is indptr[sum(n_s)].  At most 2^31 graph entries. */
+SCRUST_API scrust_batch_plan* scrust_cuda_batch_plan_create_graphs(scrust_context* context, const uint64_t* row_offsets,
+                                                                   uint32_t n_samples, uint64_t d, uint32_t k,
+                                                                   const scrust_knn_options* options,
+                                                                   const float* embedding, uint32_t* out_indices,
+                                                                   float* out_distances, scrust_status* status);
+/* The device arrays of a graph plan's connectivities; returns 0 (and writes
+ * nothing) for a kNN-only plan. */
+SCRUST_API int32_t scrust_cuda_batch_plan_graph(const scrust_batch_plan* plan, const uint32_t** indptr,
+                                                const uint32_t** indices, const float** values);
+/* Host pointers, no plan: kNN of every sample (as scrust_cuda_knn_batch) and
+ * the batch's connectivities as a host CSR laid out as above (free it with
+ * scrust_csr_free). */
+SCRUST_API int32_t scrust_cuda_neighbors_graph_batch(scrust_context* context, const float* embedding,
+                                                     const uint64_t* row_offsets, uint32_t n_samples, uint64_t d,
+                                                     uint32_t k, const scrust_knn_options* options,
+                                                     uint32_t* out_indices, float* out_distances,
+                                                     scrust_csr** connectivities, scrust_status* status);
 SCRUST_API void scrust_cuda_batch_plan_destroy(scrust_batch_plan* plan);
 
 /* ---- Query service over a resident atlas (no reference counterpart) ----
@@ -297,6 +331,44 @@ SCRUST_API int32_t scrust_serve_wait(scrust_server* server, uint64_t ticket, uin
 SCRUST_API int32_t scrust_serve_stats(scrust_server* server, uint64_t* out, int32_t max_words);
 /* Answers what is pending, then stops the scheduler and frees everything. */
 SCRUST_API void scrust_serve_destroy(scrust_server* server);
+
+/* ---- UMAP layout of a connectivities graph ----
+ *
+ * Replaces scrust_core::umap::umap (crates/scrust-core/src/umap.rs:64) with
+ * its parameters (UmapParams, umap.rs:9-33).  The layout is umap-learn's SGD
+ * as the reference runs it -- the same curve fit, firing schedule, per-cell
+ * negative-sample streams, attraction, repulsion and clip -- but every epoch
+ * computes all moves from the layout as it stood when the epoch began and
+ * sums them per cell in a fixed order, so it is deterministic (the same bits
+ * on every run) where the reference's sequential sweep has no parallel form;
+ * and the random initial layout draws one stream per cell.  Errors mirror
+ * umap.rs:86-110: n_components or n_epochs of 0 and min_dist outside
+ * [0, 3 spread] -> INVALID_PARAMETER; an empty or non-square graph, or one
+ * with no edge strong enough to fire -> SHAPE.  n_components at most 16. */
+typedef struct scrust_umap_params {
+    uint32_t struct_size;          /* sizeof(scrust_umap_params) */
+    uint32_t n_components;         /* 2 */
+    uint32_t n_epochs;             /* 200 */
+    float min_dist;                /* 0.5 */
+    float spread;                  /* 1.0 */
+    float learning_rate;           /* 1.0 */
+    uint32_t negative_sample_rate; /* 5; 0 switches repulsion off */
+    uint32_t reserved0;
+    uint64_t seed;                 /* 0 */
+    uint32_t reserved[8];
+} scrust_umap_params;
+SCRUST_API void scrust_umap_params_default(scrust_umap_params* params);
+/* Host pointers: a CSR graph (n_rows + 1 indptr, indices and values of
+ * indptr[n_rows] entries) in, the (n_rows, n_components) f32 layout out. */
+SCRUST_API int32_t scrust_cuda_umap(scrust_context* context, const uint32_t* indptr, const uint32_t* indices,
+                                    const float* values, uint64_t n_rows, uint64_t n_cols,
+                                    const scrust_umap_params* params, float* out_embedding, scrust_status* status);
+/* Device pointers (nnz given), enqueued on the context stream after one
+ * synchronisation that checks the graph has an edge to fire. */
+SCRUST_API int32_t scrust_cuda_umap_device(scrust_context* context, const uint32_t* indptr, const uint32_t* indices,
+                                           const float* values, uint64_t n_rows, uint64_t n_cols, uint64_t nnz,
+                                           const scrust_umap_params* params, float* out_embedding,
+                                           scrust_status* status);
 
 /* Phase timing.  When enabled, each kNN / connectivities call records CUDA
  * events on the context stream around its phases; scrust_cuda_phase_times

@@ -51,6 +51,21 @@ class KnnOptions(ctypes.Structure):
     ]
 
 
+class UmapParams(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("n_components", ctypes.c_uint32),
+        ("n_epochs", ctypes.c_uint32),
+        ("min_dist", ctypes.c_float),
+        ("spread", ctypes.c_float),
+        ("learning_rate", ctypes.c_float),
+        ("negative_sample_rate", ctypes.c_uint32),
+        ("reserved0", ctypes.c_uint32),
+        ("seed", ctypes.c_uint64),
+        ("reserved", ctypes.c_uint32 * 8),
+    ]
+
+
 class ScrustError(RuntimeError):
     """A non-parameter failure reported by the CUDA library."""
 
@@ -122,6 +137,14 @@ _SIGNATURES = {
     "scrust_cuda_batch_plan_choice": (ctypes.c_int32, [_P, ctypes.POINTER(ctypes.c_uint32),
                                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float)]),
     "scrust_cuda_batch_plan_destroy": (None, [_P]),
+    "scrust_cuda_batch_plan_topk_width": (ctypes.c_int32, [_P]),
+    "scrust_cuda_batch_plan_create_graphs": (_P, [_P, _P, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32,
+                                                  ctypes.POINTER(KnnOptions), _P, _P, _P, ctypes.POINTER(Status)]),
+    "scrust_cuda_batch_plan_graph": (ctypes.c_int32, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P),
+                                                       ctypes.POINTER(_P)]),
+    "scrust_cuda_neighbors_graph_batch": (ctypes.c_int32, [_P, _P, _P, ctypes.c_uint32, ctypes.c_uint64,
+                                                            ctypes.c_uint32, ctypes.POINTER(KnnOptions), _P, _P,
+                                                            ctypes.POINTER(_P), ctypes.POINTER(Status)]),
     "scrust_serve_create": (_P, [ctypes.c_int32, _P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
                                  ctypes.POINTER(KnnOptions), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
                                  ctypes.POINTER(Status)]),
@@ -134,6 +157,11 @@ _SIGNATURES = {
                                                       ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(KnnOptions),
                                                       _P, _P, ctypes.POINTER(Status)]),
     "scrust_cuda_version": (ctypes.c_char_p, []),
+    "scrust_umap_params_default": (None, [ctypes.POINTER(UmapParams)]),
+    "scrust_cuda_umap": (ctypes.c_int32, [_P, _P, _P, _P, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(UmapParams),
+                                           _P, ctypes.POINTER(Status)]),
+    "scrust_cuda_umap_device": (ctypes.c_int32, [_P, _P, _P, _P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                                  ctypes.POINTER(UmapParams), _P, ctypes.POINTER(Status)]),
 }
 
 

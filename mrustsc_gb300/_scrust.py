@@ -185,3 +185,95 @@ def knn_batch(embeddings, k, device, *, metric: str = "euclidean", precision: st
     _lib.check(rc, st)
     return [(idx[int(offsets[s]):int(offsets[s + 1])], dist[int(offsets[s]):int(offsets[s + 1])])
             for s in range(len(mats))]
+
+
+def neighbors_graph_batch(embeddings, k, device="auto", *, metric: str = "euclidean", precision: str = "fp16",
+                          list_capacity: int = 0):
+    """kNN and UMAP connectivities of several independent samples in one pass.
+
+    Returns one (indices, distances, (indptr, cols, vals, n)) per sample, ids
+    and columns local to the sample; each equals `neighbors_graph` of that
+    sample alone with the tensor form.  No reference counterpart.
+    """
+    mats = [_array2(e, np.float32, "embedding") for e in embeddings]
+    if not mats:
+        raise _lib.ScrustValueError(_lib.SHAPE, "expected at least one sample")
+    d = mats[0].shape[1]
+    if any(m.shape[1] != d for m in mats):
+        raise _lib.ScrustValueError(_lib.SHAPE, "expected every sample to have the same number of dimensions")
+    k = _k(k)
+    dev = _device_index(device)
+    offsets = np.zeros(len(mats) + 1, dtype=np.uint64)
+    offsets[1:] = np.cumsum([m.shape[0] for m in mats])
+    x = np.ascontiguousarray(np.concatenate(mats, axis=0)) if len(mats) > 1 else mats[0]
+    n = int(offsets[-1])
+    L = _lib.lib()
+    st = _lib.Status()
+    opts = _lib.options(form="tensor", metric=metric, precision=precision, list_capacity=list_capacity)
+    valid = 0 < d <= 61 and 0 < k <= 128 and all(m.shape[0] > k for m in mats)
+    ctx = _lib.context(dev) if valid else None
+    idx = np.empty((n, k), dtype=np.uint32)
+    dist = np.empty((n, k), dtype=np.float32)
+    out = ctypes.c_void_p()
+    rc = L.scrust_cuda_neighbors_graph_batch(ctx, _lib.ptr(x) if x.size else None, _lib.ptr(offsets), len(mats), d, k,
+                                             ctypes.byref(opts), _lib.ptr(idx) if idx.size else None,
+                                             _lib.ptr(dist) if dist.size else None, ctypes.byref(out),
+                                             ctypes.byref(st))
+    _lib.check(rc, st)
+    indptr, cols, vals, _ = _lib.csr_host_arrays(out)
+    return split_batch_graph(offsets, idx, dist, indptr, cols, vals)
+
+
+def split_batch_graph(offsets, idx, dist, indptr, cols, vals):
+    """Per-sample (indices, distances, (indptr, cols, vals, n)) of a batch graph
+    laid out as scrust_cuda_neighbors_graph_batch returns it."""
+    res = []
+    for s in range(len(offsets) - 1):
+        a, b = int(offsets[s]), int(offsets[s + 1])
+        p0, p1 = int(indptr[a]), int(indptr[b])
+        res.append((idx[a:b], dist[a:b], ((indptr[a:b + 1] - indptr[a]).astype(np.uint32), cols[p0:p1],
+                                          vals[p0:p1], b - a)))
+    return res
+
+
+def _array1(obj, dtype, name: str) -> np.ndarray:
+    if not isinstance(obj, np.ndarray) or obj.ndim != 1 or obj.dtype != dtype:
+        raise ValueError(f"{name} must be a 1-D numpy array of {np.dtype(dtype)}")
+    return np.ascontiguousarray(obj)
+
+
+def umap(indptr, indices, values, n_cols, n_components, n_epochs, min_dist, spread, learning_rate,
+         negative_sample_rate, seed, device):
+    """UMAP layout of a CSR graph: (n, n_components) f32.  The reference's
+    signature (crates/scrust-py/src/embedding.rs:102-134); deterministic on
+    the GPU (the same bits on every run)."""
+    ip = _array1(indptr, np.uint32, "indptr")
+    ix = _array1(indices, np.uint32, "indices")
+    vl = _array1(values, np.float32, "values")
+    for name, v in (("n_cols", n_cols), ("n_components", n_components), ("n_epochs", n_epochs),
+                    ("negative_sample_rate", negative_sample_rate), ("seed", seed)):
+        if int(v) < 0:
+            raise OverflowError(f"can't convert negative int to unsigned ({name})")
+    dev = _device_index(device)
+    n = len(ip) - 1
+    if n < 0 or (n >= 0 and len(ix) != (int(ip[-1]) if n >= 0 and len(ip) else 0)) or len(vl) != len(ix):
+        raise _lib.ScrustValueError(_lib.SHAPE, "expected indptr of n + 1 entries ending at len(indices) == len(values)")
+    L = _lib.lib()
+    p = _lib.UmapParams()
+    L.scrust_umap_params_default(ctypes.byref(p))
+    p.n_components = int(n_components)
+    p.n_epochs = int(n_epochs)
+    p.min_dist = float(min_dist)
+    p.spread = float(spread)
+    p.learning_rate = float(learning_rate)
+    p.negative_sample_rate = int(negative_sample_rate)
+    p.seed = int(seed)
+    out = np.empty((max(n, 0), int(n_components)), dtype=np.float32)
+    st = _lib.Status()
+    valid = n > 0 and len(ix) > 0 and int(n_components) > 0 and int(n_epochs) > 0
+    ctx = _lib.context(dev) if valid else None
+    rc = L.scrust_cuda_umap(ctx, _lib.ptr(ip), _lib.ptr(ix) if ix.size else None, _lib.ptr(vl) if vl.size else None,
+                            max(n, 0), int(n_cols), ctypes.byref(p), _lib.ptr(out) if out.size else None,
+                            ctypes.byref(st))
+    _lib.check(rc, st)
+    return out

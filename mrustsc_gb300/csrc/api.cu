@@ -504,12 +504,14 @@ void return_csr_buffers(scrust_context* ctx, const CsrBuffers& b) {
     ctx->csr_pool.push_back(b);
 }
 
+// `distinct_rows`: the graph is one this library's kNN built (every row's ids
+// distinct), which the faster bucket transpose relies on.
 int32_t conn_device_impl(scrust_context* ctx, const uint32_t* idx, const float* dist, uint64_t n, uint32_t k,
-                         bool validate, scrust_csr** out, scrust_status* st) {
+                         bool validate, scrust_csr** out, scrust_status* st, bool distinct_rows = false) {
     CsrBuffers b;
     int32_t rc = take_csr_buffers(ctx, n, 2 * n * (uint64_t)k, &b, st);
     if (rc) return rc;
-    rc = run_connectivities(ctx, idx, dist, (int64_t)n, (int)k, validate, &b, st);
+    rc = run_connectivities(ctx, idx, dist, (int64_t)n, (int)k, validate, &b, st, distinct_rows);
     mark(ctx, PH_CONN);
     if (rc) {
         ctx->csr_pool.push_back(b);
@@ -619,6 +621,24 @@ int32_t csr_to_host(scrust_context* ctx, scrust_csr* dev, scrust_csr** out, scru
 }
 
 }  // namespace
+
+int32_t csr_take(scrust_context* ctx, uint64_t rows, uint64_t nnz_cap, CsrBuffers* out, scrust_status* st) {
+    return take_csr_buffers(ctx, rows, nnz_cap, out, st);
+}
+
+void csr_give(scrust_context* ctx, const CsrBuffers& b) {
+    if (b.indptr) ctx->csr_pool.push_back(b);
+}
+
+int32_t csr_download(scrust_context* ctx, const CsrBuffers& b, uint64_t rows, uint64_t cols, scrust_csr** out,
+                     scrust_status* st) {
+    scrust_csr dev;
+    dev.n_rows = rows;
+    dev.n_cols = cols;
+    dev.on_device = 1;
+    dev.buf = b;
+    return csr_to_host(ctx, &dev, out, st);
+}
 
 }  // namespace scrust
 
@@ -855,7 +875,7 @@ int32_t scrust_cuda_neighbors_graph_device(scrust_context* ctx, const float* x, 
     std::lock_guard<std::mutex> lock(ctx->mu);
     DeviceGuard device_guard(ctx->device);
     if ((rc = knn_device_impl(ctx, x, n, d, k, opt, out_idx, out_dist, st))) return rc;
-    if ((rc = conn_device_impl(ctx, out_idx, out_dist, n, k, false, conn, st))) return rc;
+    if ((rc = conn_device_impl(ctx, out_idx, out_dist, n, k, false, conn, st, true))) return rc;
     return ok_form(st, opt, (int)d);
 }
 
@@ -889,7 +909,7 @@ int32_t scrust_cuda_neighbors_graph(scrust_context* ctx, const float* x, uint64_
         return cuda_fail(st, e, "download");
     }
     scrust_csr* dev = nullptr;
-    if ((rc = conn_device_impl(ctx, di, dd, n, k, false, &dev, st))) {
+    if ((rc = conn_device_impl(ctx, di, dd, n, k, false, &dev, st, true))) {
         cudaStreamSynchronize(ctx->copy_stream);
         return rc;
     }

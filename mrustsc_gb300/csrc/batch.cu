@@ -9,9 +9,20 @@
 // each sample's neighbour lists and distances are the same bits as a solve
 // of that sample alone.
 //
-// A plan fixes the layout, the buffers and the options, autotunes the list
-// capacity and the operand precision on the actual batch, and captures the
-// whole sequence in a CUDA graph; each run is one graph launch.
+// Graphs: each sample's UMAP connectivities follow in the same sequence.  The
+// sample-local neighbour ids are made batch-global (sample offset added), so
+// the batch is one block-diagonal kNN graph; smooth_knn and the directed
+// weights are row-local and the fuzzy union of a block-diagonal graph is
+// block-diagonal, so one connectivities pass over the whole batch gives
+// every sample's rows exactly as a pass over that sample alone would.  A
+// last pass makes the column ids sample-local again.
+//
+// A plan fixes the layout, the buffers and the options, autotunes the
+// candidate over-provisioning (list capacity), the register top-k width and
+// the operand precision on the actual batch, and captures the whole sequence
+// in a CUDA graph; each run is one graph launch.  The tile shape (two 128-row
+// MMA halves against 256-column tiles, K = 64) is the sweep kernel's fixed
+// design and is not a tuning choice.
 #include <string.h>
 
 #include <algorithm>
@@ -34,6 +45,9 @@ struct scrust_batch_plan {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     float tuned_ms = 0.f;
+    int32_t topk_width = 0;            // the autotuner's register top-k width (0: by k, -1: lists)
+    bool graphs = false;               // the launch also builds the connectivities
+    scrust::CsrBuffers csr;            // the batch's connectivities (sample-local columns)
 };
 
 namespace scrust {
@@ -85,14 +99,34 @@ __global__ void batch_maps_kernel(const SampleRow* __restrict__ t, int S, int64_
 
 size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// Sample-local neighbour ids -> batch-global ids (the sample's first row added).
+__global__ void batch_global_ids_kernel(const uint32_t* __restrict__ idx, const uint32_t* __restrict__ row_lo,
+                                        int64_t n_total, int k, uint32_t* __restrict__ gidx) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_total * k) return;
+    gidx[s] = idx[s] + row_lo[s / k];
+}
+
+// Column ids of the batch's CSR back to sample-local ids.
+__global__ void batch_local_cols_kernel(const uint32_t* __restrict__ indptr, const uint32_t* __restrict__ row_lo,
+                                        int64_t n_total, uint32_t* __restrict__ cols) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_total) return;
+    const uint32_t lo = row_lo[i];
+    for (uint32_t p = indptr[i], e = indptr[i + 1]; p < e; ++p) cols[p] -= lo;
+}
+
 }  // namespace
 
 // Enqueues the batch solve on ctx->stream.  No allocation once the
 // workspace has grown to this batch's size and nothing that synchronises,
 // so a second call with the same arguments can be captured in a graph.
+// With `csr` non-null the sequence ends with every sample's connectivities
+// in it (sample-local columns, rows in input order).  `topk_width` is the
+// sweep's register top-k width (KnnPlan::topk_width).
 int32_t batch_enqueue(scrust_context* ctx, const float* x, const void* table, uint32_t S, int64_t n_total,
                       int64_t n_pad, int d, int k, const scrust_knn_options& o, uint32_t* out_idx, float* out_dist,
-                      scrust_status* st) {
+                      scrust_status* st, CsrBuffers* csr = nullptr, int topk_width = 0) {
     cudaStream_t s = ctx->stream;
     cudaError_t e = cudaSuccess;
     const int items = (int)(n_pad / 256);
@@ -168,6 +202,7 @@ int32_t batch_enqueue(scrust_context* ctx, const float* x, const void* table, ui
     plan.metric = o.metric;
     plan.mode = SCRUST_MODE_EXACT;
     plan.precision = o.precision;
+    plan.topk_width = topk_width;
     Lists lists;
     lists.cap = std::max<int>(o.list_capacity ? (int)o.list_capacity : 64, k + 32);
     lists.cap = (lists.cap + 3) / 4 * 4;
@@ -205,6 +240,18 @@ int32_t batch_enqueue(scrust_context* ctx, const float* x, const void* table, ui
         return cuda_fail(st, e, "batch: knn_rerank");
     ctx->launches += 1;  // the row gather (the rerank counts its own)
     mark(ctx, PH_RERANK);
+    if (!csr) return ok(st);
+    uint32_t* gidx = (uint32_t*)ws_get(ctx, SLOT_BATCH_GIDX, sizeof(uint32_t) * (size_t)n_total * k, &e);
+    if (!gidx) return cuda_fail(st, e, "batch: workspace");
+    batch_global_ids_kernel<<<(unsigned)((n_total * k + 255) / 256), 256, 0, s>>>(out_idx, row_lo, n_total, k, gidx);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "batch: global ids");
+    int32_t rc2 = run_connectivities(ctx, gidx, out_dist, n_total, k, false, csr, st, true);
+    if (rc2) return rc2;
+    batch_local_cols_kernel<<<(unsigned)((n_total + 255) / 256), 256, 0, s>>>(csr->indptr, row_lo, n_total,
+                                                                              csr->indices);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "batch: local columns");
+    ctx->launches += 2;
+    mark(ctx, PH_CONN);
     return ok(st);
 }
 
@@ -308,10 +355,61 @@ int32_t scrust_cuda_knn_batch(scrust_context* ctx, const float* x, const uint64_
     return collect_device_errors(ctx, st);
 }
 
-scrust_batch_plan* scrust_cuda_batch_plan_create(scrust_context* ctx, const uint64_t* row_offsets, uint32_t n_samples,
-                                                 uint64_t d, uint32_t k, const scrust_knn_options* opt,
-                                                 const float* x, uint32_t* out_idx, float* out_dist,
-                                                 scrust_status* st) {
+int32_t scrust_cuda_neighbors_graph_batch(scrust_context* ctx, const float* x, const uint64_t* row_offsets,
+                                          uint32_t n_samples, uint64_t d, uint32_t k,
+                                          const scrust_knn_options* opt, uint32_t* out_idx, float* out_dist,
+                                          scrust_csr** conn, scrust_status* st) {
+    std::vector<SampleRow> rows;
+    int64_t n_total = 0, n_pad = 0;
+    int32_t rc = check_batch(row_offsets, n_samples, d, k, opt, &rows, &n_total, &n_pad, st);
+    if (rc) return rc;
+    if (!ctx) return fail(st, SCRUST_NO_GPU, "no CUDA context (no usable GPU)");
+    if (!x || !out_idx || !out_dist || !conn) return fail(st, SCRUST_SHAPE, "expected non-null host pointers");
+    if ((uint64_t)n_total * k * 2 >= 0xffffffffull)
+        return fail(st, SCRUST_SHAPE, "expected fewer than 2^31 graph entries in a batch");
+    scrust_knn_options o;
+    scrust_knn_options_default(&o);
+    if (opt) o = *opt;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    DeviceGuard device_guard(ctx->device);
+    cudaError_t e;
+    float* dx = (float*)ws_get(ctx, SLOT_HOST_IN, sizeof(float) * (size_t)n_total * d, &e);
+    uint32_t* di = (uint32_t*)ws_get(ctx, SLOT_HOST_IDX, sizeof(uint32_t) * (size_t)n_total * k, &e);
+    float* dd = (float*)ws_get(ctx, SLOT_HOST_DIST, sizeof(float) * (size_t)n_total * k, &e);
+    void* table = ws_get(ctx, SLOT_BATCH_TABLE, sizeof(SampleRow) * rows.size(), &e);
+    if (!dx || !di || !dd || !table) return cuda_fail(st, e, "workspace");
+    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess ||
+        (e = cudaMemcpy(table, rows.data(), sizeof(SampleRow) * rows.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dx, x, sizeof(float) * (size_t)n_total * d, cudaMemcpyHostToDevice, ctx->stream)) !=
+            cudaSuccess)
+        return cuda_fail(st, e, "upload");
+    CsrBuffers b;
+    if ((rc = csr_take(ctx, (uint64_t)n_total, 2 * (uint64_t)n_total * k, &b, st))) return rc;
+    mark(ctx, PH_START);
+    rc = batch_enqueue(ctx, dx, table, n_samples, n_total, n_pad, (int)d, (int)k, o, di, dd, st, &b);
+    if (rc == SCRUST_OK &&
+        ((e = cudaMemcpyAsync(out_idx, di, sizeof(uint32_t) * (size_t)n_total * k, cudaMemcpyDeviceToHost,
+                              ctx->stream)) != cudaSuccess ||
+         (e = cudaMemcpyAsync(out_dist, dd, sizeof(float) * (size_t)n_total * k, cudaMemcpyDeviceToHost,
+                              ctx->stream)) != cudaSuccess))
+        rc = cuda_fail(st, e, "download");
+    if (rc == SCRUST_OK) rc = csr_download(ctx, b, (uint64_t)n_total, (uint64_t)n_total, conn, st);
+    csr_give(ctx, b);
+    if (rc) return rc;
+    if ((rc = collect_device_errors(ctx, st))) {
+        scrust_csr_free(*conn);
+        *conn = nullptr;
+    }
+    return rc;
+}
+
+}  // extern "C"
+
+namespace {
+
+scrust_batch_plan* plan_create(scrust_context* ctx, const uint64_t* row_offsets, uint32_t n_samples, uint64_t d,
+                               uint32_t k, const scrust_knn_options* opt, const float* x, uint32_t* out_idx,
+                               float* out_dist, bool graphs, scrust_status* st) {
     std::vector<SampleRow> rows;
     int64_t n_total = 0, n_pad = 0;
     if (check_batch(row_offsets, n_samples, d, k, opt, &rows, &n_total, &n_pad, st)) return nullptr;
@@ -338,40 +436,65 @@ scrust_batch_plan* scrust_cuda_batch_plan_create(scrust_context* ctx, const uint
     p->x = x;
     p->out_idx = out_idx;
     p->out_dist = out_dist;
+    p->graphs = graphs;
     std::lock_guard<std::mutex> lock(ctx->mu);
     DeviceGuard device_guard(ctx->device);
     cudaError_t e = cudaMalloc(&p->table, sizeof(SampleRow) * rows.size());
     if (e == cudaSuccess)
         e = cudaMemcpy(p->table, rows.data(), sizeof(SampleRow) * rows.size(), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-        cuda_fail(st, e, "batch plan: table");
+    if (e == cudaSuccess && graphs) {
+        p->csr.rows_cap = (size_t)n_total;
+        p->csr.nnz_cap = 2 * (size_t)n_total * k;
+        e = cudaMalloc(&p->csr.indptr, sizeof(uint32_t) * ((size_t)n_total + 1));
+        if (e == cudaSuccess) e = cudaMalloc(&p->csr.indices, sizeof(uint32_t) * p->csr.nnz_cap);
+        if (e == cudaSuccess) e = cudaMalloc(&p->csr.values, sizeof(float) * p->csr.nnz_cap);
+    }
+    auto release = [&]() {
         cudaFree(p->table);
+        cudaFree(p->csr.indptr);
+        cudaFree(p->csr.indices);
+        cudaFree(p->csr.values);
         delete p;
+    };
+    if (e != cudaSuccess) {
+        cuda_fail(st, e, "batch plan: allocation");
+        release();
         return nullptr;
     }
-    // Autotune the list capacity (candidates kept between compactions) and,
-    // unless the caller fixed them, the operand precision, timing each
-    // candidate on this batch; then capture the winner.
+    CsrBuffers* csr = graphs ? &p->csr : nullptr;
+    // Autotune the candidate over-provisioning (list capacity) and the
+    // register top-k width unless the caller fixed the capacity, and the
+    // operand precision, timing each candidate on this batch; then capture
+    // the winner.
     const bool tune_cap = p->opts.list_capacity == 0;
-    std::vector<scrust_knn_options> cands;
+    struct Cand {
+        scrust_knn_options o;
+        int width;
+    };
+    std::vector<Cand> cands;
     const uint32_t caps[3] = {64, 128, 256};
+    std::vector<int> widths = {0};
+    if (k > 1 && k <= 16) widths.push_back(32);
+    if (k > 1 && k <= 32) widths.push_back(-1);
     for (int c = 0; c < (tune_cap ? 3 : 1); ++c)
-        for (int prec = 0; prec < 2; ++prec) {
-            scrust_knn_options o = p->opts;
-            if (tune_cap) o.list_capacity = caps[c];
-            o.precision = prec;
-            cands.push_back(o);
-        }
+        for (int w : widths)
+            for (int prec = 0; prec < 2; ++prec) {
+                scrust_knn_options o = p->opts;
+                if (tune_cap) o.list_capacity = caps[c];
+                o.precision = prec;
+                cands.push_back(Cand{o, w});
+            }
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);
     float best = 1e30f;
-    scrust_knn_options chosen = cands[0];
+    Cand chosen = cands[0];
     int32_t rc = SCRUST_OK;
-    for (const auto& o : cands) {
+    for (const auto& c : cands) {
         for (int rep = 0; rep < 2 && rc == SCRUST_OK; ++rep) {  // first run sizes the workspace
             cudaEventRecord(t0, ctx->stream);
-            rc = batch_enqueue(ctx, x, p->table, n_samples, n_total, n_pad, (int)d, (int)k, o, out_idx, out_dist, st);
+            rc = batch_enqueue(ctx, x, p->table, n_samples, n_total, n_pad, (int)d, (int)k, c.o, out_idx, out_dist, st,
+                               csr, c.width);
             cudaEventRecord(t1, ctx->stream);
         }
         if (rc) break;
@@ -382,14 +505,15 @@ scrust_batch_plan* scrust_cuda_batch_plan_create(scrust_context* ctx, const uint
         }
         if (ms < best) {
             best = ms;
-            chosen = o;
+            chosen = c;
         }
     }
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     if (rc == SCRUST_OK) {
         // Size the workspace for the chosen options, then capture.
-        rc = batch_enqueue(ctx, x, p->table, n_samples, n_total, n_pad, (int)d, (int)k, chosen, out_idx, out_dist, st);
+        rc = batch_enqueue(ctx, x, p->table, n_samples, n_total, n_pad, (int)d, (int)k, chosen.o, out_idx, out_dist,
+                           st, csr, chosen.width);
         if (rc == SCRUST_OK && (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
             rc = cuda_fail(st, e, "batch plan: synchronise");
     }
@@ -398,8 +522,8 @@ scrust_batch_plan* scrust_cuda_batch_plan_create(scrust_context* ctx, const uint
         ctx->timing = false;
         e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            rc = batch_enqueue(ctx, x, p->table, n_samples, n_total, n_pad, (int)d, (int)k, chosen, out_idx, out_dist,
-                               st);
+            rc = batch_enqueue(ctx, x, p->table, n_samples, n_total, n_pad, (int)d, (int)k, chosen.o, out_idx,
+                               out_dist, st, csr, chosen.width);
             const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &p->graph);
             if (rc == SCRUST_OK && e2 != cudaSuccess) rc = cuda_fail(st, e2, "batch plan: capture");
         } else {
@@ -413,14 +537,53 @@ scrust_batch_plan* scrust_cuda_batch_plan_create(scrust_context* ctx, const uint
         cudaGetLastError();
         if (p->exec) cudaGraphExecDestroy(p->exec);
         if (p->graph) cudaGraphDestroy(p->graph);
-        cudaFree(p->table);
-        delete p;
+        release();
         return nullptr;
     }
-    p->opts = chosen;
+    p->opts = chosen.o;
+    p->topk_width = chosen.width;
     p->tuned_ms = best;
     ok(st);
     return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+scrust_batch_plan* scrust_cuda_batch_plan_create(scrust_context* ctx, const uint64_t* row_offsets, uint32_t n_samples,
+                                                 uint64_t d, uint32_t k, const scrust_knn_options* opt,
+                                                 const float* x, uint32_t* out_idx, float* out_dist,
+                                                 scrust_status* st) {
+    return plan_create(ctx, row_offsets, n_samples, d, k, opt, x, out_idx, out_dist, false, st);
+}
+
+scrust_batch_plan* scrust_cuda_batch_plan_create_graphs(scrust_context* ctx, const uint64_t* row_offsets,
+                                                        uint32_t n_samples, uint64_t d, uint32_t k,
+                                                        const scrust_knn_options* opt, const float* x,
+                                                        uint32_t* out_idx, float* out_dist, scrust_status* st) {
+    if (row_offsets && n_samples && row_offsets[n_samples] * (uint64_t)k * 2 >= 0xffffffffull) {
+        fail(st, SCRUST_SHAPE, "expected fewer than 2^31 graph entries in a batch");
+        return nullptr;
+    }
+    return plan_create(ctx, row_offsets, n_samples, d, k, opt, x, out_idx, out_dist, true, st);
+}
+
+int32_t scrust_cuda_batch_plan_graph(const scrust_batch_plan* p, const uint32_t** indptr, const uint32_t** indices,
+                                     const float** values) {
+    if (!p || !p->graphs) return 0;
+    if (indptr) *indptr = p->csr.indptr;
+    if (indices) *indices = p->csr.indices;
+    if (values) *values = p->csr.values;
+    return 1;
+}
+
+int32_t scrust_cuda_batch_plan_topk_width(const scrust_batch_plan* p) {
+    if (!p) return -1;
+    const int w = p->topk_width;
+    if (w < 0 || p->k > 32) return 0;
+    if (w == 32 || p->k > 16) return 32;
+    return p->k == 1 ? 1 : 16;
 }
 
 int32_t scrust_cuda_batch_plan_launch(scrust_batch_plan* p, scrust_status* st) {
@@ -451,6 +614,9 @@ void scrust_cuda_batch_plan_destroy(scrust_batch_plan* p) {
         if (p->exec) cudaGraphExecDestroy(p->exec);
         if (p->graph) cudaGraphDestroy(p->graph);
         cudaFree(p->table);
+        cudaFree(p->csr.indptr);
+        cudaFree(p->csr.indices);
+        cudaFree(p->csr.values);
     }
     delete p;
 }

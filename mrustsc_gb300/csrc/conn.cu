@@ -259,6 +259,254 @@ __global__ void __launch_bounds__(256) directed_group_kernel(const uint32_t* __r
     }
 }
 
+// directed_group_kernel for graphs whose rows hold distinct ids (every kNN
+// graph this library builds): the same weights and sorted rows, and for the
+// transpose each kept edge takes its place in its target row's bucket with one
+// atomic increment of that row's in-degree (the order inside a bucket is
+// arbitrary; the merge kernels order it by source row, which is unique there).
+template <int G>
+__global__ void __launch_bounds__(256) directed_bucket_kernel(const uint32_t* __restrict__ idx,
+                                                              const float* __restrict__ dist, int64_t n, int k,
+                                                              const float* __restrict__ sigmas,
+                                                              const float* __restrict__ rhos,
+                                                              uint32_t* __restrict__ dcol, float* __restrict__ dw,
+                                                              uint32_t* __restrict__ dcnt,
+                                                              uint32_t* __restrict__ indeg,
+                                                              uint32_t* __restrict__ erank) {
+    const int lane = threadIdx.x & 31;
+    const int g = lane / G, j = lane % G;
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const bool row_ok = i < n;
+    uint32_t nb = 0;
+    float wt = 0.f;
+    bool kept = false;
+    if (row_ok && j < k) {
+        nb = idx[i * k + j];
+        if ((int64_t)nb != i) {
+            const float sigma = sigmas[i], rho = rhos[i];
+            const float offset = __fsub_rn(dist[i * k + j], rho);
+            wt = (offset <= 0.f || sigma == 0.f) ? 1.0f : expf(__fdiv_rn(-offset, sigma));
+            kept = wt != 0.f;
+        }
+    }
+    const unsigned long long key = kept ? ((unsigned long long)nb << 32) | (uint32_t)j : ~0ull;
+    int rank = 0;
+#pragma unroll
+    for (int o = 0; o < G; ++o) rank += __shfl_sync(0xffffffffu, key, g * G + o) < key;
+    const uint32_t group_bits = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (G * g));
+    const int m = __popc(__ballot_sync(0xffffffffu, kept) & group_bits);
+    if (!row_ok) return;
+    if (j == 0) dcnt[i] = (uint32_t)m;
+    if (kept) {
+        const int64_t slot = i * k + rank;
+        dcol[slot] = nb;
+        dw[slot] = wt;
+        erank[slot] = atomicAdd(indeg + nb, 1u);
+    }
+}
+
+// Each kept edge (i -> c, w) into its target row's bucket:
+// tval[tstart[c] + rank] = i << 32 | bits(w).
+__global__ void bucket_scatter_kernel(const uint32_t* __restrict__ dcol, const float* __restrict__ dw,
+                                      const uint32_t* __restrict__ dcnt, const uint32_t* __restrict__ erank,
+                                      const uint32_t* __restrict__ tstart, int64_t n, int k,
+                                      unsigned long long* __restrict__ tval) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n * k) return;
+    const int64_t i = s / k;
+    const int t = (int)(s - i * k);
+    if (t >= (int)dcnt[i]) return;
+    const uint32_t c = dcol[s];
+    tval[(int64_t)tstart[c] + erank[s]] = ((unsigned long long)(uint32_t)i << 32) | __float_as_uint(dw[s]);
+}
+
+// Ascending sort of one bucket in place by one warp (a bitonic network whose
+// merges all run ascending, with positions past `len` read as +infinity, so
+// any length works).  Keys are source << 32 | weight bits, sources unique.
+__device__ void warp_sort_bucket(unsigned long long* v, uint32_t len) {
+    const int lane = threadIdx.x & 31;
+    uint32_t p2 = 1;
+    while (p2 < len) p2 <<= 1;
+    for (uint32_t size = 2; size <= p2; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t t = lane; t < p2 / 2; t += 32) {
+                // pair (a, b), a < b: the first stage of a merge compares
+                // mirror positions, the later ones positions `stride` apart
+                const uint32_t block = t / stride, off = t % stride;
+                uint32_t a, b;
+                if (stride == (size >> 1)) {
+                    const uint32_t base = (t / (size >> 1)) * size;
+                    a = base + (t % (size >> 1));
+                    b = base + size - 1 - (t % (size >> 1));
+                } else {
+                    a = block * 2 * stride + off;
+                    b = a + stride;
+                }
+                if (b < len) {
+                    const unsigned long long x = v[a], y = v[b];
+                    if (y < x) {
+                        v[a] = y;
+                        v[b] = x;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// The fuzzy union of row i, one warp per row, for graphs with distinct ids
+// per row and k <= 32: the row's directed entries (sorted by column, one per
+// lane) and its bucket of incoming edges (sources unique, any order).  Every
+// entry's place in the merged row is its rank among the union's distinct
+// columns: for a bucket of up to 128 edges (four per lane) the ranks come
+// from shuffles, a larger bucket is sorted in place and placed by binary
+// search.  This pass writes each directed entry's place to fpos and its
+// merged value (w + r) - (w * r) over dw, each incoming edge's place to bpos
+// (all ones when it merged into a directed entry), and the row's length;
+// the writing pass then only moves entries.
+constexpr int kBucketPerLane = 4;
+
+__device__ __forceinline__ uint32_t mask_below(int c) { return c >= 32 ? 0xffffffffu : ((1u << c) - 1u); }
+
+__global__ void __launch_bounds__(256) merge_rank_kernel(const uint32_t* __restrict__ dcol, float* __restrict__ dw,
+                                                         const uint32_t* __restrict__ dcnt,
+                                                         unsigned long long* __restrict__ tval,
+                                                         const uint32_t* __restrict__ tstart, int64_t n, int k,
+                                                         uint32_t* __restrict__ fpos, uint32_t* __restrict__ bpos,
+                                                         uint32_t* __restrict__ rowcnt) {
+    const int lane = threadIdx.x & 31;
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;
+    const int nf = (int)dcnt[i];
+    const uint32_t b0 = tstart[i];
+    const int nb = (int)(tstart[i + 1] - b0);
+    const uint32_t fcol = lane < nf ? dcol[i * k + lane] : 0xffffffffu;
+    const float fw = lane < nf ? dw[i * k + lane] : 0.f;
+    int less_b = 0;      // incoming edges with a source below this lane's column
+    bool dup_f = false;  // this lane's column has an incoming edge
+    float rv_f = 0.f;
+    uint32_t dupmask;
+    if (nb <= 32 * kBucketPerLane) {
+        uint32_t bsrc[kBucketPerLane];
+        float bw[kBucketPerLane];
+        int rank[kBucketPerLane], less_f[kBucketPerLane];
+        bool dup_b[kBucketPerLane];
+#pragma unroll
+        for (int q = 0; q < kBucketPerLane; ++q) {
+            const int j = q * 32 + lane;
+            const unsigned long long e = j < nb ? tval[b0 + j] : ~0ull;
+            bsrc[q] = (uint32_t)(e >> 32);
+            bw[q] = __uint_as_float((uint32_t)e);
+            rank[q] = 0;
+            less_f[q] = 0;
+            dup_b[q] = false;
+        }
+#pragma unroll
+        for (int q2 = 0; q2 < kBucketPerLane; ++q2) {
+            if (q2 * 32 >= nb) break;
+            const int lim = min(32, nb - q2 * 32);
+            for (int t = 0; t < lim; ++t) {
+                const uint32_t s_t = __shfl_sync(0xffffffffu, bsrc[q2], t);
+                const float w_t = __shfl_sync(0xffffffffu, bw[q2], t);
+#pragma unroll
+                for (int q = 0; q < kBucketPerLane; ++q) rank[q] += s_t < bsrc[q];
+                less_b += s_t < fcol;
+                if (s_t == fcol) {
+                    dup_f = true;
+                    rv_f = w_t;
+                }
+            }
+        }
+        for (int t = 0; t < nf; ++t) {
+            const uint32_t c_t = __shfl_sync(0xffffffffu, fcol, t);
+#pragma unroll
+            for (int q = 0; q < kBucketPerLane; ++q) {
+                less_f[q] += c_t < bsrc[q];
+                dup_b[q] |= c_t == bsrc[q];
+            }
+        }
+        dupmask = __ballot_sync(0xffffffffu, lane < nf && dup_f);
+#pragma unroll
+        for (int q = 0; q < kBucketPerLane; ++q) {
+            const int j = q * 32 + lane;
+            if (j < nb)
+                bpos[b0 + j] = dup_b[q] ? 0xffffffffu
+                                        : (uint32_t)(rank[q] + less_f[q]) - (uint32_t)__popc(dupmask & mask_below(less_f[q]));
+        }
+    } else {
+        warp_sort_bucket(tval + b0, (uint32_t)nb);
+        if (lane < nf) {  // lower bound of this lane's column among the sorted sources
+            int lo = 0, hi = nb;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if ((uint32_t)(tval[b0 + mid] >> 32) < fcol)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            less_b = lo;
+            if (lo < nb) {
+                const unsigned long long e = tval[b0 + lo];
+                if ((uint32_t)(e >> 32) == fcol) {
+                    dup_f = true;
+                    rv_f = __uint_as_float((uint32_t)e);
+                }
+            }
+        }
+        dupmask = __ballot_sync(0xffffffffu, lane < nf && dup_f);
+        for (int base = 0; base < nb; base += 32) {
+            const int j = base + lane;
+            const uint32_t src = j < nb ? (uint32_t)(tval[b0 + j] >> 32) : 0xffffffffu;
+            int lf = 0;
+            bool db = false;
+            for (int t = 0; t < nf; ++t) {
+                const uint32_t c_t = __shfl_sync(0xffffffffu, fcol, t);
+                lf += c_t < src;
+                db |= c_t == src;
+            }
+            if (j < nb) bpos[b0 + j] = db ? 0xffffffffu : (uint32_t)(j + lf) - (uint32_t)__popc(dupmask & mask_below(lf));
+        }
+    }
+    if (lane < nf) {
+        fpos[i * k + lane] = (uint32_t)(lane + less_b) - (uint32_t)__popc(dupmask & lanemask_lt());
+        const float wv = fw, rv = dup_f ? rv_f : 0.f;
+        dw[i * k + lane] = __fsub_rn(__fadd_rn(wv, rv), __fmul_rn(wv, rv));
+    }
+    if (lane == 0) rowcnt[i] = (uint32_t)(nf + nb) - (uint32_t)__popc(dupmask);
+}
+
+// The writing pass: every entry to its place in the CSR (an incoming edge
+// alone in its column keeps its weight: (0 + r) - (0 * r) = r).
+__global__ void __launch_bounds__(256) merge_place_kernel(const uint32_t* __restrict__ dcol,
+                                                          const float* __restrict__ dw,
+                                                          const uint32_t* __restrict__ dcnt,
+                                                          const unsigned long long* __restrict__ tval,
+                                                          const uint32_t* __restrict__ tstart, int64_t n, int k,
+                                                          const uint32_t* __restrict__ fpos,
+                                                          const uint32_t* __restrict__ bpos,
+                                                          const uint32_t* __restrict__ indptr,
+                                                          uint32_t* __restrict__ out_cols, float* __restrict__ out_vals) {
+    const int lane = threadIdx.x & 31;
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;
+    const int nf = (int)dcnt[i];
+    const uint32_t b0 = tstart[i], b1 = tstart[i + 1];
+    const uint32_t base = indptr[i];
+    if (lane < nf) {
+        const uint32_t p = base + fpos[i * k + lane];
+        out_cols[p] = dcol[i * k + lane];
+        out_vals[p] = dw[i * k + lane];
+    }
+    for (uint32_t j = b0 + lane; j < b1; j += 32) {
+        const uint32_t q = bpos[j];
+        if (q == 0xffffffffu) continue;
+        const unsigned long long e = tval[j];
+        out_cols[base + q] = (uint32_t)(e >> 32);
+        out_vals[base + q] = __uint_as_float((uint32_t)e);
+    }
+}
+
 // Bucket starts of the edges sorted by target row: start[j] = the number of
 // keys below j, for j in [0, n] (keys are at most n; n marks unused slots).
 // Position p writes the starts of the rows in (key[p-1], key[p]]; the last
@@ -612,8 +860,59 @@ int32_t run_query_connectivities(scrust_context* ctx, const uint32_t* idx, const
     return ok(st);
 }
 
+// The fuzzy union of a graph whose rows hold distinct ids, k <= 32: weights
+// with bucket places from one atomic per edge, the in-degree scan, the bucket
+// scatter, then a counting and a writing merge with one warp per row.  The
+// CSR is bit-identical to the radix-sort path's.
+int32_t run_connectivities_distinct(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n, int k,
+                                    CsrBuffers* out, scrust_status* st) {
+    cudaError_t e = cudaSuccess;
+    cudaStream_t s = ctx->stream;
+    const int64_t E = n * (int64_t)k;
+    const size_t scan_elems = scan_scratch_elems(n + 1);
+    char* a = (char*)ws_get(ctx, SLOT_CONN_A, sizeof(float) * 2 * (size_t)n + sizeof(uint32_t) * 3 * (size_t)(n + 1) + 256, &e);
+    uint32_t* dcol = (uint32_t*)ws_get(ctx, SLOT_CONN_B, sizeof(uint32_t) * (size_t)E, &e);
+    float* dw = (float*)ws_get(ctx, SLOT_CONN_C, sizeof(float) * (size_t)E, &e);
+    uint32_t* erank = (uint32_t*)ws_get(ctx, SLOT_CONN_D, sizeof(uint32_t) * (size_t)E, &e);  // then bpos
+    unsigned long long* tval = (unsigned long long*)ws_get(ctx, SLOT_CONN_E, sizeof(unsigned long long) * (size_t)E, &e);
+    uint32_t* fpos = (uint32_t*)ws_get(ctx, SLOT_CONN_F, sizeof(uint32_t) * (size_t)E, &e);
+    uint32_t* scan_scratch = (uint32_t*)ws_get(ctx, SLOT_SCAN, sizeof(uint32_t) * scan_elems, &e);
+    if (!a || !dcol || !dw || !erank || !tval || !fpos || !scan_scratch)
+        return cuda_fail(st, e, "connectivities: workspace");
+    float* sig = (float*)a;
+    float* rho = sig + n;
+    uint32_t* indeg = (uint32_t*)(rho + n);  // n + 1, then the bucket starts in place
+    uint32_t* rowcnt = indeg + (n + 1);      // n + 1
+    uint32_t* dcnt = rowcnt + (n + 1);       // n (+1 spare)
+    if ((e = cudaMemsetAsync(indeg, 0, sizeof(uint32_t) * (size_t)(n + 1), s)) != cudaSuccess)
+        return cuda_fail(st, e, "memset");
+    if ((e = launch_smooth_knn(ctx, dist, n, k, sig, rho, false)) != cudaSuccess) return cuda_fail(st, e, "smooth_knn");
+    if (k <= 16)
+        directed_bucket_kernel<16><<<(unsigned)((n * 16 + 255) / 256), 256, 0, s>>>(idx, dist, n, k, sig, rho, dcol,
+                                                                                   dw, dcnt, indeg, erank);
+    else
+        directed_bucket_kernel<32><<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(idx, dist, n, k, sig, rho, dcol,
+                                                                                   dw, dcnt, indeg, erank);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "directed weights");
+    if ((e = device_exclusive_scan(ctx, indeg, indeg, n + 1, scan_scratch, scan_elems)) != cudaSuccess)
+        return cuda_fail(st, e, "in-degree scan");
+    bucket_scatter_kernel<<<(unsigned)((E + 255) / 256), 256, 0, s>>>(dcol, dw, dcnt, erank, indeg, n, k, tval);
+    const unsigned merge_blocks = (unsigned)((n * 32 + 255) / 256);
+    uint32_t* bpos = erank;  // the ranks are read by the scatter only
+    merge_rank_kernel<<<merge_blocks, 256, 0, s>>>(dcol, dw, dcnt, tval, indeg, n, k, fpos, bpos, rowcnt);
+    if ((e = cudaMemsetAsync(rowcnt + n, 0, sizeof(uint32_t), s)) != cudaSuccess) return cuda_fail(st, e, "memset");
+    if ((e = device_exclusive_scan(ctx, rowcnt, out->indptr, n + 1, scan_scratch, scan_elems)) != cudaSuccess)
+        return cuda_fail(st, e, "row scan");
+    merge_place_kernel<<<merge_blocks, 256, 0, s>>>(dcol, dw, dcnt, tval, indeg, n, k, fpos, bpos, out->indptr,
+                                                    out->indices, out->values);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "merge");
+    ctx->launches += 4;
+    return ok(st);
+}
+
 int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n, int k,
-                           bool validate, CsrBuffers* out, scrust_status* st) {
+                           bool validate, CsrBuffers* out, scrust_status* st, bool distinct_rows) {
+    if (distinct_rows && !validate && k <= 32) return run_connectivities_distinct(ctx, idx, dist, n, k, out, st);
     cudaError_t e = cudaSuccess;
     cudaStream_t s = ctx->stream;
     const int64_t E = n * (int64_t)k;

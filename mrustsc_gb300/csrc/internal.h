@@ -58,6 +58,8 @@ enum Slot : int {
     SLOT_RERANK_BIG,    // rows for the rerank's second sorted pass
     SLOT_QTERMS,        // per-query-row bound terms of a query-versus-reference solve
     SLOT_QSCRATCH,      // scratch operands of a query-versus-reference solve
+    SLOT_BATCH_GIDX,    // a batch's neighbour ids made batch-global for its connectivities
+    SLOT_UMAP,          // the UMAP layout's schedules, moves, transpose and second layout
     SLOT_COUNT
 };
 
@@ -177,6 +179,10 @@ struct KnnPlan {
     int ctot = 0;             // list storage per (row, segment)
     int segments = 1;
     int max_ctas = 0;         // tensor sweep: CTAs at most (0: one per SM)
+    // Tensor sweep, general passes: the per-row top-k kept in registers.
+    // 0 = the narrowest that holds k (16 or 32; lists alone above 32), 16 or
+    // 32 = that width (at least k), -1 = lists alone (warp-cooperative prunes).
+    int topk_width = 0;
 };
 
 // Keys the rerank's warp path holds per row (the union of the row's lists);
@@ -334,8 +340,19 @@ inline int padded_row_floats(int d) { return (d + 3) / 4 * 4; }
 // reference's, and nothing built from them (weights, graphs) changes.
 cudaError_t launch_smooth_knn(scrust_context* ctx, const float* dist, int64_t n, int k,
                               float* sigmas, float* rhos, bool report_sigmas);
+// Device CSR buffers from the context's pool (call with the context lock
+// held), back to the pool, and a download into a new host CSR (pinned slab;
+// synchronises the context stream).
+int32_t csr_take(scrust_context* ctx, uint64_t rows, uint64_t nnz_cap, CsrBuffers* out, scrust_status* st);
+void csr_give(scrust_context* ctx, const CsrBuffers& b);
+int32_t csr_download(scrust_context* ctx, const CsrBuffers& b, uint64_t rows, uint64_t cols, scrust_csr** out,
+                     scrust_status* st);
+
+// The UMAP connectivities CSR of an n x k graph.  `distinct_rows`: every row's
+// ids are distinct (true of every kNN graph this library builds), which
+// allows the bucket transpose; graphs from callers take the stable radix sort.
 int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n,
-                           int k, bool validate, CsrBuffers* out, scrust_status* st);
+                           int k, bool validate, CsrBuffers* out, scrust_status* st, bool distinct_rows = false);
 // Rows of the directed fuzzy set of query rows against a reference (no
 // symmetrisation, no self to drop): sigma/rho per row as smooth_knn, then
 // exp weights, zero weights dropped, columns ascending, as a CSR of q rows.

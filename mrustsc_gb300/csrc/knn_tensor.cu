@@ -1093,14 +1093,22 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.argmin_out = argmin_out;
     if (argmin_out && (plan.k != 1 || resume)) return cudaErrorInvalidValue;
     if (resume && !theta_io) return cudaErrorInvalidValue;
-    auto kern = a.k == 1    ? (argmin_out ? tensor_candidates_kernel<1, 3> : tensor_candidates_kernel<1, 0>)
-                : a.k <= 16 ? (a.thr_only ? tensor_candidates_kernel<16, 1>
-                               : a.collect ? tensor_candidates_kernel<16, 2>
-                                           : tensor_candidates_kernel<16, 0>)
-                : a.k <= 32 ? (a.thr_only ? tensor_candidates_kernel<32, 1>
-                               : a.collect ? tensor_candidates_kernel<32, 2>
-                                           : tensor_candidates_kernel<32, 0>)
-                            : tensor_candidates_kernel<0, 0>;
+    // Register top-k width of a general pass (threshold and collect passes
+    // keep the width that holds k).
+    int width = a.k == 1 ? 1 : a.k <= 16 ? 16 : a.k <= 32 ? 32 : 0;
+    if (!a.thr_only && !a.collect && a.k > 1) {
+        if (plan.topk_width < 0) width = 0;
+        else if (plan.topk_width == 32 && a.k <= 32) width = 32;
+        else if (plan.topk_width != 0 && plan.topk_width != 16 && plan.topk_width != 32) return cudaErrorInvalidValue;
+    }
+    auto kern = width == 1    ? (argmin_out ? tensor_candidates_kernel<1, 3> : tensor_candidates_kernel<1, 0>)
+                : width == 16 ? (a.thr_only ? tensor_candidates_kernel<16, 1>
+                                 : a.collect ? tensor_candidates_kernel<16, 2>
+                                             : tensor_candidates_kernel<16, 0>)
+                : width == 32 ? (a.thr_only ? tensor_candidates_kernel<32, 1>
+                                 : a.collect ? tensor_candidates_kernel<32, 2>
+                                             : tensor_candidates_kernel<32, 0>)
+                              : tensor_candidates_kernel<0, 0>;
     cudaError_t e = set_smem_limit(ctx, (const void*)kern, (int)SMEM_BYTES);
     if (e != cudaSuccess) return e;
     const int grid = std::min(a.items, plan.max_ctas > 0 ? std::min(plan.max_ctas, ctx->sm_count) : ctx->sm_count);

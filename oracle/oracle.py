@@ -14,6 +14,7 @@ Functions mirror the reference files they restate:
   knn_fp64_cross_c   the same for query rows against reference rows
   smooth_knn         crates/scrust-core/src/neighbors.rs:239-298
   connectivities     crates/scrust-core/src/neighbors.rs:208-372
+  umap, fit_ab_params, tau_words   crates/scrust-core/src/umap.rs:64-509 (umap_oracle.c)
 """
 
 from __future__ import annotations
@@ -28,6 +29,7 @@ import numpy as np
 
 _HERE = pathlib.Path(__file__).resolve().parent
 _SRC = _HERE / "neighbors_oracle.c"
+_SOURCES = (_SRC, _HERE / "umap_oracle.c")
 _OUT = _HERE / "_build" / "liboracle.so"
 _LOCK = threading.Lock()
 _LIB = None
@@ -42,11 +44,12 @@ class OracleError(ValueError):
 def build(force: bool = False) -> pathlib.Path:
     """Compile the restatement with gcc (no -march flags: same code on x86 and Arm)."""
     _OUT.parent.mkdir(parents=True, exist_ok=True)
-    if force or not _OUT.exists() or _OUT.stat().st_mtime < _SRC.stat().st_mtime:
+    newest = max(src.stat().st_mtime for src in _SOURCES)
+    if force or not _OUT.exists() or _OUT.stat().st_mtime < newest:
         tmp = _OUT.with_suffix(f".{os.getpid()}.tmp.so")
         cmd = [
             "gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-            str(_SRC), "-o", str(tmp), "-lm",
+            *map(str, _SOURCES), "-o", str(tmp), "-lm",
         ]
         subprocess.run(cmd, check=True)
         os.replace(tmp, _OUT)
@@ -80,6 +83,11 @@ def _lib():
             lib.oracle_unrolled_sum_f32.argtypes = [f32p, i64]
             lib.oracle_unrolled_sum_f32.restype = ctypes.c_float
             lib.oracle_num_threads.restype = ctypes.c_int
+            lib.oracle_tau_words.argtypes = [ctypes.c_uint64, i64, u32p]
+            lib.oracle_fit_ab_params.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.POINTER(ctypes.c_float),
+                                                 ctypes.POINTER(ctypes.c_float)]
+            lib.oracle_umap.argtypes = [u32p, u32p, f32p, i64, i64, i64, i64, ctypes.c_float, ctypes.c_float,
+                                        ctypes.c_float, i64, ctypes.c_uint64, f32p]
             _LIB = lib
     return _LIB
 
@@ -293,3 +301,30 @@ def knn_fp64_cross(queries, reference, k: int):
         idx[b:b + 256] = order
         dist[b:b + 256] = np.sqrt(np.take_along_axis(d2, order, 1))
     return idx, dist
+
+
+def tau_words(seed: int, count: int) -> np.ndarray:
+    """The first words of the reference's TauRng::new(seed) (umap.rs:174-229)."""
+    out = np.zeros(count, np.uint32)
+    _lib().oracle_tau_words(ctypes.c_uint64(seed), count, _p(out, ctypes.c_uint32))
+    return out
+
+
+def fit_ab_params(min_dist: float, spread: float) -> tuple[float, float]:
+    a, b = ctypes.c_float(), ctypes.c_float()
+    _check(_lib().oracle_fit_ab_params(min_dist, spread, ctypes.byref(a), ctypes.byref(b)), "fit_ab_params")
+    return a.value, b.value
+
+
+def umap(indptr, indices, values, n_cols: int, n_components: int = 2, n_epochs: int = 200, min_dist: float = 0.5,
+         spread: float = 1.0, learning_rate: float = 1.0, negative_sample_rate: int = 5, seed: int = 0):
+    """The reference's CPU UMAP layout (umap.rs:64), (n, n_components) f32."""
+    ip = np.ascontiguousarray(indptr, dtype=np.uint32)
+    ix = np.ascontiguousarray(indices, dtype=np.uint32)
+    vl = _f32(values)
+    n = len(ip) - 1
+    out = np.zeros((max(n, 1), max(n_components, 1)), np.float32)
+    _check(_lib().oracle_umap(_p(ip, ctypes.c_uint32), _p(ix, ctypes.c_uint32), _p(vl, ctypes.c_float), n, n_cols,
+                              n_components, n_epochs, min_dist, spread, learning_rate, negative_sample_rate,
+                              ctypes.c_uint64(seed), _p(out, ctypes.c_float)), "umap")
+    return out[:n, :n_components]

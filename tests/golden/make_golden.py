@@ -8,8 +8,11 @@ It reads the scanpy constants the reference pins in
 crates/scrust-core/src/neighbors.rs:498-544 (ten sample cells of
 `reference_embedding(300, 20, 42)` with their scanpy neighbour rows and
 connectivity rows, and the exact nnz / weight sum / square sum of the whole
-matrix) and writes them, unchanged, to `scanpy_reference_embedding_300x20.json`.
-The values are parsed from the source text, not re-typed.
+matrix) and writes them, unchanged, to `scanpy_reference_embedding_300x20.json`;
+and the UMAP constants of crates/scrust-core/src/umap.rs's tests (the 80-cell
+scanpy graph and layout, umap-learn's fitted-curve table) to
+`umap_reference_80_cells.json`.  The values are parsed from the source text,
+not re-typed.
 """
 
 from __future__ import annotations
@@ -68,6 +71,30 @@ def parse(neighbors_rs: str) -> dict:
     }
 
 
+def parse_umap(umap_rs: str) -> dict:
+    """The 80-cell scanpy graph and layout and umap-learn's fitted-curve table
+    that crates/scrust-core/src/umap.rs pins (tests module)."""
+    n_cells = int(re.search(r"N_CELLS:\s*usize\s*=\s*(\d+)", umap_rs).group(1))
+    edges = [[int(h), int(t), _rust_float(w)]
+             for h, t, w in re.findall(r"\((\d+),\s*(\d+),\s*([0-9eE_.+-]+)\)", _block(umap_rs, "EDGES: &["))]
+    layout = [_rust_float(v) for v in re.findall(r"-?[0-9][0-9eE_.+-]*", _block(umap_rs, "EMBEDDING: &["))]
+    table_block = _block(umap_rs, "EXPECTED: &[(f32, f32, f64, f64)]")
+    table = [[_rust_float(v) for v in row]
+             for row in re.findall(r"\(\s*([0-9eE_.+-]+),\s*([0-9eE_.+-]+),\s*([0-9eE_.+-]+),\s*([0-9eE_.+-]+)\)",
+                                   table_block)]
+    assert len(layout) == 2 * n_cells and len(table) == 24 and edges
+    return {
+        "source": "crates/scrust-core/src/umap.rs (tests: reference::EDGES / EMBEDDING, "
+                  "fitted_curve_matches_umap_learn::EXPECTED)",
+        "n_cells": n_cells,
+        "edges_upper": edges,
+        "scanpy_layout": layout,
+        "fit_ab_table": table,
+        "bars": {"fit_ab_relative_tolerance": 1e-4, "near": 15, "wide": 30, "preserved_min_fraction": 0.80,
+                 "epochs": 500, "seed": 0},
+    }
+
+
 def main(argv: list[str]) -> None:
     if len(argv) != 2:
         raise SystemExit("usage: make_golden.py <path of the scrust checkout>")
@@ -75,6 +102,10 @@ def main(argv: list[str]) -> None:
     text = (root / "crates/scrust-core/src/neighbors.rs").read_text()
     out = HERE / "scanpy_reference_embedding_300x20.json"
     out.write_text(json.dumps(parse(text), indent=1) + "\n")
+    print(f"wrote {out}")
+    umap_text = (root / "crates/scrust-core/src/umap.rs").read_text()
+    out = HERE / "umap_reference_80_cells.json"
+    out.write_text(json.dumps(parse_umap(umap_text), indent=1) + "\n")
     print(f"wrote {out}")
 
 

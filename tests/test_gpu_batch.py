@@ -100,3 +100,75 @@ def test_plan_graph_launch_matches_direct_batch(scrust):
                 np.testing.assert_array_equal(gd[a:b], dd)
     finally:
         L.scrust_cuda_batch_plan_destroy(plan)
+
+
+@pytest.mark.parametrize("k", [15, 30])
+def test_batch_graphs_equal_single_sample_graphs(scrust, oracle, k):
+    """Every sample's connectivities from the batch pass equal the restated
+    connectivities of that sample's own kNN graph (CSR structure bit-exact,
+    values within 1e-5), and the kNN rows equal the single-sample solve."""
+    samples = ragged_samples([300, 1000, 257, 3000, 40, 511, 2049], seed=k + 1)
+    samples[3][100:260] = samples[3][100]  # hub rows inside one sample
+    out = scrust.neighbors_graph_batch(samples, k, "auto")
+    for x, (idx, dist, csr) in zip(samples, out):
+        si, sd = scrust.knn(x, k, "auto", form="tensor")
+        np.testing.assert_array_equal(idx, si)
+        np.testing.assert_array_equal(dist, sd)
+        ref = oracle.connectivities(idx, dist)
+        np.testing.assert_array_equal(csr[0], ref[0])
+        np.testing.assert_array_equal(csr[1], ref[1])
+        np.testing.assert_allclose(csr[2], ref[2], rtol=0, atol=1e-5)
+        assert csr[3] == len(x)
+
+
+def test_graph_plan_builds_every_sample_in_one_launch(scrust, oracle):
+    import torch
+
+    L = _lib.lib()
+    ctx = _lib.context(0)
+    samples = ragged_samples([700, 2500, 260, 1200], seed=9)
+    k = 15
+    x = np.concatenate(samples)
+    offsets = np.zeros(len(samples) + 1, np.uint64)
+    offsets[1:] = np.cumsum([len(s) for s in samples])
+    n = int(offsets[-1])
+    xd = torch.from_numpy(x).cuda()
+    idx = torch.empty((n, k), dtype=torch.int32, device="cuda")
+    dst = torch.empty((n, k), dtype=torch.float32, device="cuda")
+    st = _lib.Status()
+    opts = _lib.options(form="tensor")
+    plan = L.scrust_cuda_batch_plan_create_graphs(ctx, _lib.ptr(offsets), len(samples), 50, k, ctypes.byref(opts),
+                                                  xd.data_ptr(), idx.data_ptr(), dst.data_ptr(), ctypes.byref(st))
+    assert plan, st.message.decode()
+    try:
+        assert L.scrust_cuda_batch_plan_topk_width(plan) in (0, 16, 32)
+        idx.fill_(0)
+        _lib.check(L.scrust_cuda_batch_plan_launch(plan, ctypes.byref(st)), st)
+        _lib.check(L.scrust_cuda_synchronize(ctx, ctypes.byref(st)), st)
+        ip, ix, vl = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        assert L.scrust_cuda_batch_plan_graph(plan, ctypes.byref(ip), ctypes.byref(ix), ctypes.byref(vl)) == 1
+
+        class DeviceView:  # the plan's device array, seen by torch without a copy
+            def __init__(self, ptr, count, typestr):
+                self.__cuda_array_interface__ = {"shape": (count,), "typestr": typestr, "data": (ptr, False),
+                                                 "version": 2}
+
+        def grab(ptr, count, typestr):
+            return torch.as_tensor(DeviceView(ptr.value, count, typestr), device="cuda").cpu().numpy()
+
+        indptr = grab(ip, n + 1, "<u4")
+        nnz = int(indptr[-1])
+        cols = grab(ix, nnz, "<u4")
+        vals = grab(vl, nnz, "<f4")
+        gi = idx.cpu().numpy().view(np.uint32)
+        gd = dst.cpu().numpy()
+        from mrustsc_gb300._scrust import split_batch_graph
+
+        for xs, (si, sd, csr) in zip(samples, split_batch_graph(offsets, gi, gd, indptr, cols, vals)):
+            np.testing.assert_array_equal(si, oracle.knn_fp64(xs, k)[0])
+            ref = oracle.connectivities(si, sd)
+            np.testing.assert_array_equal(csr[0], ref[0])
+            np.testing.assert_array_equal(csr[1], ref[1])
+            np.testing.assert_allclose(csr[2], ref[2], rtol=0, atol=1e-5)
+    finally:
+        L.scrust_cuda_batch_plan_destroy(plan)

@@ -190,3 +190,22 @@ def test_pp_neighbors_end_to_end(oracle):
     c = adata.obsp["connectivities"]
     assert np.count_nonzero(c.diagonal()) == 0
     assert adata.uns["neighbors"]["params"] == {"n_neighbors": 15, "method": "umap", "use_rep": "X_pca"}
+
+
+@pytest.mark.parametrize("k", [15, 30])
+def test_graphs_with_hub_rows(scrust, oracle, k):
+    """Rows listed by far more than 32 others (a star: every point's nearest
+    cell is the centre; a block of 400 identical cells, whose lowest ids every
+    copy lists) against the restated connectivities of the same kNN graph."""
+    rng = np.random.default_rng(k)
+    star = rng.normal(size=(3000, 50))
+    star /= np.linalg.norm(star, axis=1, keepdims=True)
+    star = np.vstack([np.zeros((1, 50)), star]).astype(np.float32)
+    block = synthetic.mixture(2000, 20, clusters=5, dup_frac=0.0, seed=4)
+    block[100:500] = block[100]
+    for x in (star, block):
+        for form in ("plain", "tensor"):
+            idx, dist, conn = scrust.neighbors_graph(x, k, form=form)
+            indeg = np.bincount(idx.ravel().astype(np.int64), minlength=len(x))
+            assert indeg.max() > 32
+            assert_same_csr(conn, oracle.connectivities(idx, dist))
