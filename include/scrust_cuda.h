@@ -30,6 +30,14 @@
  *                                    fused into one device pass
  *   scrust_cuda_umap                 scrust_core::umap::umap
  *                                    crates/scrust-core/src/umap.rs:64
+ *   scrust_cuda_pca                  scrust_core::pca::pca
+ *                                    crates/scrust-core/src/pca.rs:74
+ *   scrust_cuda_leiden               scrust_core::cluster::leiden
+ *                                    crates/scrust-core/src/cluster.rs:88
+ *   scrust_cuda_louvain              scrust_core::cluster::louvain
+ *                                    crates/scrust-core/src/cluster.rs:125
+ *   scrust_cuda_modularity           scrust_core::cluster::modularity
+ *                                    crates/scrust-core/src/cluster.rs:148
  * Entry points with no reference counterpart (new semantics, parity against
  * the FP64 oracle only): scrust_cuda_knn_batched (many samples in one launch)
  * and the scrust_serve_* query service (queries against a resident atlas).
@@ -369,6 +377,64 @@ SCRUST_API int32_t scrust_cuda_umap_device(scrust_context* context, const uint32
                                            const float* values, uint64_t n_rows, uint64_t n_cols, uint64_t nnz,
                                            const scrust_umap_params* params, float* out_embedding,
                                            scrust_status* status);
+
+/* ---- PCA, the step before the neighbours path ----
+ *
+ * Replaces scrust_core::pca::pca (crates/scrust-core/src/pca.rs:74): truncated
+ * PCA of a cells x genes CSR matrix by the reference's randomised SVD
+ * (sketch of n_components + 24 columns, 7 or 4 power iterations, the
+ * largest-loading sign fix, scanpy's explained variance and ratios for
+ * zero_center on and off).  Deterministic: the same inputs and seed give the
+ * same bits; the Gaussian sketch is this library's counter-based one, so the
+ * results agree with the reference's subspace, not its bits.  Outputs: the
+ * embedding (n_cells x n_components, obsm["X_pca"]), the components
+ * (n_components x n_genes, varm["PCs"] transposed), the explained variance
+ * and its ratio (n_components each).  Errors mirror pca.rs:81-94:
+ * n_components of 0 or above min(n_cells, n_genes), or fewer than 2 cells ->
+ * INVALID_PARAMETER.  n_components at most 104. */
+SCRUST_API int32_t scrust_cuda_pca(scrust_context* context, const uint32_t* indptr, const uint32_t* indices,
+                                   const float* values, uint64_t n_cells, uint64_t n_genes, uint32_t n_components,
+                                   int32_t zero_center, uint64_t seed, float* out_embedding, float* out_components,
+                                   float* out_variance, float* out_variance_ratio, scrust_status* status);
+/* Device pointers (nnz given): the embedding stays in HBM, ready for
+ * scrust_cuda_neighbors_graph_device.  Synchronises once at the end. */
+SCRUST_API int32_t scrust_cuda_pca_device(scrust_context* context, const uint32_t* indptr, const uint32_t* indices,
+                                          const float* values, uint64_t n_cells, uint64_t n_genes, uint64_t nnz,
+                                          uint32_t n_components, int32_t zero_center, uint64_t seed,
+                                          float* out_embedding, float* out_components, float* out_variance,
+                                          float* out_variance_ratio, scrust_status* status);
+
+/* ---- Community detection on the connectivities, the step after it ----
+ *
+ * Replace scrust_core::cluster::{leiden, louvain, modularity}
+ * (crates/scrust-core/src/cluster.rs:88,125,148): RBConfiguration modularity
+ * with a resolution on the graph (A + A^T) / 2 of a square CSR matrix.
+ * Leiden runs up to n_iterations passes of local moving, refinement into
+ * well-connected subcommunities and aggregation, stopping at a pass that
+ * returns its own input; Louvain one pass without refinement.  Labels are
+ * numbered by descending community size, ties to the smaller id; the
+ * modularity of the labels and the community count are written beside them.
+ * The moves run in parallel rounds, so the partition is this library's own:
+ * deterministic for the same graph and seed, not the reference's label for
+ * label (its moves are sequential from a ChaCha12 stream).  Errors mirror
+ * cluster.rs:95-97,170-180,214-290: resolution not finite and > 0 or
+ * n_iterations of 0 -> INVALID_PARAMETER; an empty or non-square graph ->
+ * SHAPE; weights negative or not finite, or none positive ->
+ * INVALID_PARAMETER.  Host pointers; synchronises. */
+SCRUST_API int32_t scrust_cuda_leiden(scrust_context* context, const uint32_t* indptr, const uint32_t* indices,
+                                      const float* values, uint64_t n_rows, uint64_t n_cols, double resolution,
+                                      uint32_t n_iterations, uint64_t seed, uint32_t* out_labels,
+                                      double* out_modularity, uint64_t* out_n_communities, scrust_status* status);
+SCRUST_API int32_t scrust_cuda_louvain(scrust_context* context, const uint32_t* indptr, const uint32_t* indices,
+                                       const float* values, uint64_t n_rows, uint64_t n_cols, double resolution,
+                                       uint64_t seed, uint32_t* out_labels, double* out_modularity,
+                                       uint64_t* out_n_communities, scrust_status* status);
+/* Modularity of given labels: n_labels must equal n_rows (else SHAPE) and
+ * every label must be below n_rows (else INVALID_PARAMETER). */
+SCRUST_API int32_t scrust_cuda_modularity(scrust_context* context, const uint32_t* indptr, const uint32_t* indices,
+                                          const float* values, uint64_t n_rows, uint64_t n_cols,
+                                          const uint32_t* labels, uint64_t n_labels, double resolution,
+                                          double* out_modularity, scrust_status* status);
 
 /* Phase timing.  When enabled, each kNN / connectivities call records CUDA
  * events on the context stream around its phases; scrust_cuda_phase_times

@@ -158,6 +158,20 @@ _SIGNATURES = {
                                                       _P, _P, ctypes.POINTER(Status)]),
     "scrust_cuda_version": (ctypes.c_char_p, []),
     "scrust_umap_params_default": (None, [ctypes.POINTER(UmapParams)]),
+    "scrust_cuda_pca": (ctypes.c_int32, [_P, _P, _P, _P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                          ctypes.c_int32, ctypes.c_uint64, _P, _P, _P, _P, ctypes.POINTER(Status)]),
+    "scrust_cuda_pca_device": (ctypes.c_int32, [_P, _P, _P, _P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                                 ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64, _P, _P, _P, _P,
+                                                 ctypes.POINTER(Status)]),
+    "scrust_cuda_leiden": (ctypes.c_int32, [_P, _P, _P, _P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double,
+                                             ctypes.c_uint32, ctypes.c_uint64, _P, ctypes.POINTER(ctypes.c_double),
+                                             ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(Status)]),
+    "scrust_cuda_louvain": (ctypes.c_int32, [_P, _P, _P, _P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double,
+                                              ctypes.c_uint64, _P, ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(Status)]),
+    "scrust_cuda_modularity": (ctypes.c_int32, [_P, _P, _P, _P, ctypes.c_uint64, ctypes.c_uint64, _P,
+                                                 ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                                                 ctypes.POINTER(Status)]),
     "scrust_cuda_umap": (ctypes.c_int32, [_P, _P, _P, _P, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(UmapParams),
                                            _P, ctypes.POINTER(Status)]),
     "scrust_cuda_umap_device": (ctypes.c_int32, [_P, _P, _P, _P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,

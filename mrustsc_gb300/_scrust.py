@@ -20,6 +20,7 @@ call raises ``RuntimeError`` rather than falling back.  ``"metal"`` raises
 from __future__ import annotations
 
 import ctypes
+import math
 
 import numpy as np
 
@@ -277,3 +278,102 @@ def umap(indptr, indices, values, n_cols, n_components, n_epochs, min_dist, spre
                             ctypes.byref(st))
     _lib.check(rc, st)
     return out
+
+
+def pca(indptr, indices, values, n_cols, n_components, zero_center, seed, device):
+    """Truncated PCA of a cells x genes CSR matrix: a dict of `embedding`
+    (n, k), `components` (k, n_genes), `explained_variance` and
+    `explained_variance_ratio` (k,), as the reference's binding returns
+    (crates/scrust-py/src/preprocess.rs:154-185).  Deterministic on the GPU."""
+    ip = _array1(indptr, np.uint32, "indptr")
+    ix = _array1(indices, np.uint32, "indices")
+    vl = _array1(values, np.float32, "values")
+    for name, v in (("n_cols", n_cols), ("n_components", n_components), ("seed", seed)):
+        if int(v) < 0:
+            raise OverflowError(f"can't convert negative int to unsigned ({name})")
+    dev = _device_index(device)
+    n = len(ip) - 1
+    if n < 0 or len(ix) != int(ip[-1]) or len(vl) != len(ix):
+        raise _lib.ScrustValueError(_lib.SHAPE, "expected indptr of n + 1 entries ending at len(indices) == len(values)")
+    g, k = int(n_cols), int(n_components)
+    L = _lib.lib()
+    st = _lib.Status()
+    emb = np.empty((n, k), np.float32)
+    comps = np.empty((k, g), np.float32)
+    var = np.empty(k, np.float32)
+    ratio = np.empty(k, np.float32)
+    valid = 0 < k <= min(n, g) and n >= 2
+    ctx = _lib.context(dev) if valid else None
+    rc = L.scrust_cuda_pca(ctx, _lib.ptr(ip), _lib.ptr(ix) if ix.size else None, _lib.ptr(vl) if vl.size else None,
+                           n, g, k, 1 if zero_center else 0, int(seed), _lib.ptr(emb) if emb.size else None,
+                           _lib.ptr(comps) if comps.size else None, _lib.ptr(var) if var.size else None,
+                           _lib.ptr(ratio) if ratio.size else None, ctypes.byref(st))
+    _lib.check(rc, st)
+    return {"embedding": emb, "components": comps, "explained_variance": var, "explained_variance_ratio": ratio}
+
+
+def _graph_args(indptr, indices, values, n_cols):
+    ip = _array1(indptr, np.uint32, "indptr")
+    ix = _array1(indices, np.uint32, "indices")
+    vl = _array1(values, np.float32, "values")
+    if int(n_cols) < 0:
+        raise OverflowError("can't convert negative int to unsigned (n_cols)")
+    n = len(ip) - 1
+    if n < 0 or len(ix) != int(ip[-1]) or len(vl) != len(ix):
+        raise _lib.ScrustValueError(_lib.SHAPE, "expected indptr of n + 1 entries ending at len(indices) == len(values)")
+    return ip, ix, vl, n, int(n_cols)
+
+
+def _cluster(entry, indptr, indices, values, n_cols, resolution, extra, device):
+    ip, ix, vl, n, nc = _graph_args(indptr, indices, values, n_cols)
+    dev = _device_index(device)
+    L = _lib.lib()
+    st = _lib.Status()
+    labels = np.empty(max(n, 0), np.uint32)
+    q = ctypes.c_double(0.0)
+    count = ctypes.c_uint64(0)
+    # Argument errors come before a device is required, as in the reference.
+    valid = n > 0 and nc == n and math.isfinite(float(resolution)) and float(resolution) > 0
+    ctx = _lib.context(dev) if valid else None
+    rc = getattr(L, entry)(ctx, _lib.ptr(ip), _lib.ptr(ix) if ix.size else None, _lib.ptr(vl) if vl.size else None,
+                           max(n, 0), nc, float(resolution), *extra, _lib.ptr(labels) if labels.size else None,
+                           ctypes.byref(q), ctypes.byref(count), ctypes.byref(st))
+    _lib.check(rc, st)
+    return labels, float(q.value), int(count.value)
+
+
+def leiden(indptr, indices, values, n_cols, resolution, n_iterations, seed, device):
+    """Leiden communities of a square CSR graph: (labels u32, modularity,
+    n_communities), labels numbered by descending community size.  The
+    reference's signature (crates/scrust-py/src/cluster.rs:30-49); the moves
+    run in parallel rounds on the GPU, deterministic for a seed."""
+    for name, v in (("n_iterations", n_iterations), ("seed", seed)):
+        if int(v) < 0:
+            raise OverflowError(f"can't convert negative int to unsigned ({name})")
+    return _cluster("scrust_cuda_leiden", indptr, indices, values, n_cols, resolution,
+                    (int(n_iterations), int(seed)), device)
+
+
+def louvain(indptr, indices, values, n_cols, resolution, seed, device):
+    """Louvain communities (crates/scrust-py/src/cluster.rs:51-69), as leiden."""
+    if int(seed) < 0:
+        raise OverflowError("can't convert negative int to unsigned (seed)")
+    return _cluster("scrust_cuda_louvain", indptr, indices, values, n_cols, resolution, (int(seed),), device)
+
+
+def modularity(indptr, indices, values, n_cols, labels, resolution):
+    """Modularity of `labels` on the graph (crates/scrust-py/src/cluster.rs:71-86),
+    computed on the GPU."""
+    ip, ix, vl, n, nc = _graph_args(indptr, indices, values, n_cols)
+    lab = _array1(labels, np.uint32, "labels")
+    L = _lib.lib()
+    st = _lib.Status()
+    q = ctypes.c_double(0.0)
+    valid = n > 0 and nc == n and len(lab) == n and math.isfinite(float(resolution)) and float(resolution) > 0
+    ctx = _lib.context(0) if valid else None
+    rc = L.scrust_cuda_modularity(ctx, _lib.ptr(ip), _lib.ptr(ix) if ix.size else None,
+                                  _lib.ptr(vl) if vl.size else None, max(n, 0), nc,
+                                  _lib.ptr(lab) if lab.size else None, len(lab), float(resolution), ctypes.byref(q),
+                                  ctypes.byref(st))
+    _lib.check(rc, st)
+    return float(q.value)

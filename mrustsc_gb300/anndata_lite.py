@@ -1,6 +1,8 @@
-"""A minimal AnnData stand-in with the slots ``pp.neighbors`` reads and
-writes (``X``, ``obsm``, ``obsp``, ``uns``, ``n_obs``), for environments
-without the ``anndata`` package.  Any object with those attributes works."""
+"""A minimal AnnData stand-in with the slots ``pp.pca``, ``pp.neighbors``,
+``tl.umap``, ``tl.leiden`` and ``tl.louvain`` read and write (``X``, ``obs``,
+``obsm``, ``obsp``, ``varm``, ``uns``, ``n_obs``), for environments without
+the ``anndata`` package.  Any object
+with those attributes works."""
 
 from __future__ import annotations
 
@@ -10,8 +12,10 @@ import numpy as np
 class AnnData:
     def __init__(self, X=None, *, obsm: dict | None = None, n_obs: int | None = None):
         self.X = X
+        self.obs: dict = {}
         self.obsm = dict(obsm or {})
         self.obsp: dict = {}
+        self.varm: dict = {}
         self.uns: dict = {}
         if n_obs is None:
             n_obs = X.shape[0] if X is not None else next(iter(self.obsm.values())).shape[0]

@@ -12,6 +12,9 @@ Routing follows the reference's own device semantics
 * ``connectivities(indices, distances)`` takes no device in the reference;
   it goes to the reference's module when the process-wide
   ``scrust.settings.device`` is ``"cpu"`` and to this backend otherwise.
+* ``umap``, ``pca``, ``leiden`` and ``louvain`` take a device as their last
+  argument and route as ``knn`` does; ``modularity`` takes none and routes
+  as ``connectivities`` does.
 * Every other attribute is the reference module's.
 
 This is routing between the reference's implementation and this one, chosen
@@ -56,6 +59,26 @@ class Core:
         if self._device_setting() == "cpu":
             return self._real.connectivities(indices, distances)
         return self._backend.connectivities(indices, distances)
+
+    def _by_device(self, name: str, args: tuple) -> Any:
+        target = self._real if args[-1] == "cpu" else self._backend
+        return getattr(target, name)(*args)
+
+    def umap(self, *args):
+        return self._by_device("umap", args)
+
+    def pca(self, *args):
+        return self._by_device("pca", args)
+
+    def leiden(self, *args):
+        return self._by_device("leiden", args)
+
+    def louvain(self, *args):
+        return self._by_device("louvain", args)
+
+    def modularity(self, *args):
+        target = self._real if self._device_setting() == "cpu" else self._backend
+        return target.modularity(*args)
 
     def gpu_available(self) -> bool:
         return bool(self._backend.gpu_available())

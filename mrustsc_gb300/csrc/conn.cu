@@ -369,6 +369,60 @@ constexpr int kBucketPerLane = 4;
 
 __device__ __forceinline__ uint32_t mask_below(int c) { return c >= 32 ? 0xffffffffu : ((1u << c) - 1u); }
 
+// Ranks for a bucket of at most 32 * Q incoming edges, Q per lane.
+template <int Q>
+__device__ __forceinline__ uint32_t rank_small_bucket(const unsigned long long* __restrict__ tval, uint32_t b0, int nb,
+                                                      int nf, uint32_t fcol, uint32_t* __restrict__ bpos,
+                                                      int* less_b, bool* dup_f, float* rv_f) {
+    const int lane = threadIdx.x & 31;
+    uint32_t bsrc[Q];
+    float bw[Q];
+    int rank[Q], less_f[Q];
+    bool dup_b[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int j = q * 32 + lane;
+        const unsigned long long e = j < nb ? tval[b0 + j] : ~0ull;
+        bsrc[q] = (uint32_t)(e >> 32);
+        bw[q] = __uint_as_float((uint32_t)e);
+        rank[q] = 0;
+        less_f[q] = 0;
+        dup_b[q] = false;
+    }
+#pragma unroll
+    for (int q2 = 0; q2 < Q; ++q2) {
+        const int lim = min(32, nb - q2 * 32);
+        for (int t = 0; t < lim; ++t) {
+            const uint32_t s_t = __shfl_sync(0xffffffffu, bsrc[q2], t);
+            const float w_t = __shfl_sync(0xffffffffu, bw[q2], t);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) rank[q] += s_t < bsrc[q];
+            *less_b += s_t < fcol;
+            if (s_t == fcol) {
+                *dup_f = true;
+                *rv_f = w_t;
+            }
+        }
+    }
+    for (int t = 0; t < nf; ++t) {
+        const uint32_t c_t = __shfl_sync(0xffffffffu, fcol, t);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            less_f[q] += c_t < bsrc[q];
+            dup_b[q] |= c_t == bsrc[q];
+        }
+    }
+    const uint32_t dupmask = __ballot_sync(0xffffffffu, lane < nf && *dup_f);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int j = q * 32 + lane;
+        if (j < nb)
+            bpos[b0 + j] = dup_b[q] ? 0xffffffffu
+                                    : (uint32_t)(rank[q] + less_f[q]) - (uint32_t)__popc(dupmask & mask_below(less_f[q]));
+    }
+    return dupmask;
+}
+
 __global__ void __launch_bounds__(256) merge_rank_kernel(const uint32_t* __restrict__ dcol, float* __restrict__ dw,
                                                          const uint32_t* __restrict__ dcnt,
                                                          unsigned long long* __restrict__ tval,
@@ -387,53 +441,12 @@ __global__ void __launch_bounds__(256) merge_rank_kernel(const uint32_t* __restr
     bool dup_f = false;  // this lane's column has an incoming edge
     float rv_f = 0.f;
     uint32_t dupmask;
-    if (nb <= 32 * kBucketPerLane) {
-        uint32_t bsrc[kBucketPerLane];
-        float bw[kBucketPerLane];
-        int rank[kBucketPerLane], less_f[kBucketPerLane];
-        bool dup_b[kBucketPerLane];
-#pragma unroll
-        for (int q = 0; q < kBucketPerLane; ++q) {
-            const int j = q * 32 + lane;
-            const unsigned long long e = j < nb ? tval[b0 + j] : ~0ull;
-            bsrc[q] = (uint32_t)(e >> 32);
-            bw[q] = __uint_as_float((uint32_t)e);
-            rank[q] = 0;
-            less_f[q] = 0;
-            dup_b[q] = false;
-        }
-#pragma unroll
-        for (int q2 = 0; q2 < kBucketPerLane; ++q2) {
-            if (q2 * 32 >= nb) break;
-            const int lim = min(32, nb - q2 * 32);
-            for (int t = 0; t < lim; ++t) {
-                const uint32_t s_t = __shfl_sync(0xffffffffu, bsrc[q2], t);
-                const float w_t = __shfl_sync(0xffffffffu, bw[q2], t);
-#pragma unroll
-                for (int q = 0; q < kBucketPerLane; ++q) rank[q] += s_t < bsrc[q];
-                less_b += s_t < fcol;
-                if (s_t == fcol) {
-                    dup_f = true;
-                    rv_f = w_t;
-                }
-            }
-        }
-        for (int t = 0; t < nf; ++t) {
-            const uint32_t c_t = __shfl_sync(0xffffffffu, fcol, t);
-#pragma unroll
-            for (int q = 0; q < kBucketPerLane; ++q) {
-                less_f[q] += c_t < bsrc[q];
-                dup_b[q] |= c_t == bsrc[q];
-            }
-        }
-        dupmask = __ballot_sync(0xffffffffu, lane < nf && dup_f);
-#pragma unroll
-        for (int q = 0; q < kBucketPerLane; ++q) {
-            const int j = q * 32 + lane;
-            if (j < nb)
-                bpos[b0 + j] = dup_b[q] ? 0xffffffffu
-                                        : (uint32_t)(rank[q] + less_f[q]) - (uint32_t)__popc(dupmask & mask_below(less_f[q]));
-        }
+    if (nb <= 32) {
+        dupmask = rank_small_bucket<1>(tval, b0, nb, nf, fcol, bpos, &less_b, &dup_f, &rv_f);
+    } else if (nb <= 64) {
+        dupmask = rank_small_bucket<2>(tval, b0, nb, nf, fcol, bpos, &less_b, &dup_f, &rv_f);
+    } else if (nb <= 32 * kBucketPerLane) {
+        dupmask = rank_small_bucket<kBucketPerLane>(tval, b0, nb, nf, fcol, bpos, &less_b, &dup_f, &rv_f);
     } else {
         warp_sort_bucket(tval + b0, (uint32_t)nb);
         if (lane < nf) {  // lower bound of this lane's column among the sorted sources

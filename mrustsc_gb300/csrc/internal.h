@@ -60,6 +60,7 @@ enum Slot : int {
     SLOT_QSCRATCH,      // scratch operands of a query-versus-reference solve
     SLOT_BATCH_GIDX,    // a batch's neighbour ids made batch-global for its connectivities
     SLOT_UMAP,          // the UMAP layout's schedules, moves, transpose and second layout
+    SLOT_PCA,           // PCA: sketch, bases, CSC copy, Grams, small factors
     SLOT_COUNT
 };
 

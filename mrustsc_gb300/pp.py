@@ -41,3 +41,22 @@ def neighbors(adata, *, n_neighbors: int = 15, use_rep: str = "X_pca", device: s
         "distances_key": "distances",
         "params": params,
     }
+
+
+def pca(adata, *, n_comps: int = 50, zero_center: bool = True, random_state: int = 0, device: str = "auto") -> None:
+    """Principal component analysis by randomised SVD (python/scrust/pp/_basics.py:166-183)."""
+    import scipy.sparse as sp
+
+    from ._shared import _INDEX_DTYPE
+
+    x = adata.X if isinstance(adata.X, sp.csr_matrix) else sp.csr_matrix(adata.X)
+    result = _extension().pca(x.indptr.astype(_INDEX_DTYPE, copy=False), x.indices.astype(_INDEX_DTYPE, copy=False),
+                              x.data.astype(_VALUE_DTYPE, copy=False), x.shape[1], n_comps, zero_center, random_state,
+                              device)
+    adata.obsm["X_pca"] = np.asarray(result["embedding"], dtype=_VALUE_DTYPE)
+    adata.varm["PCs"] = np.asarray(result["components"], dtype=_VALUE_DTYPE).T.copy()
+    adata.uns["pca"] = {
+        "variance_ratio": np.asarray(result["explained_variance_ratio"], dtype=_VALUE_DTYPE),
+        "variance": np.asarray(result["explained_variance"], dtype=_VALUE_DTYPE),
+        "params": {"zero_center": zero_center, "n_comps": n_comps, "random_state": random_state},
+    }

@@ -15,6 +15,7 @@ Functions mirror the reference files they restate:
   smooth_knn         crates/scrust-core/src/neighbors.rs:239-298
   connectivities     crates/scrust-core/src/neighbors.rs:208-372
   umap, fit_ab_params, tau_words   crates/scrust-core/src/umap.rs:64-509 (umap_oracle.c)
+  leiden, louvain, modularity      crates/scrust-core/src/cluster.rs:88-850 (cluster_oracle.c)
 """
 
 from __future__ import annotations
@@ -29,7 +30,7 @@ import numpy as np
 
 _HERE = pathlib.Path(__file__).resolve().parent
 _SRC = _HERE / "neighbors_oracle.c"
-_SOURCES = (_SRC, _HERE / "umap_oracle.c")
+_SOURCES = (_SRC, _HERE / "umap_oracle.c", _HERE / "cluster_oracle.c")
 _OUT = _HERE / "_build" / "liboracle.so"
 _LOCK = threading.Lock()
 _LIB = None
@@ -84,6 +85,11 @@ def _lib():
             lib.oracle_unrolled_sum_f32.restype = ctypes.c_float
             lib.oracle_num_threads.restype = ctypes.c_int
             lib.oracle_tau_words.argtypes = [ctypes.c_uint64, i64, u32p]
+            lib.oracle_leiden.argtypes = [u32p, u32p, f32p, i64, i64, ctypes.c_double, i64, ctypes.c_uint64, u32p,
+                                          f64p, i64p]
+            lib.oracle_louvain.argtypes = [u32p, u32p, f32p, i64, i64, ctypes.c_double, ctypes.c_uint64, u32p, f64p,
+                                           i64p]
+            lib.oracle_modularity.argtypes = [u32p, u32p, f32p, i64, i64, u32p, i64, ctypes.c_double, f64p]
             lib.oracle_fit_ab_params.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.POINTER(ctypes.c_float),
                                                  ctypes.POINTER(ctypes.c_float)]
             lib.oracle_umap.argtypes = [u32p, u32p, f32p, i64, i64, i64, i64, ctypes.c_float, ctypes.c_float,
@@ -328,3 +334,45 @@ def umap(indptr, indices, values, n_cols: int, n_components: int = 2, n_epochs: 
                               n_components, n_epochs, min_dist, spread, learning_rate, negative_sample_rate,
                               ctypes.c_uint64(seed), _p(out, ctypes.c_float)), "umap")
     return out[:n, :n_components]
+
+
+def _csr32(indptr, indices, values):
+    return (np.ascontiguousarray(indptr, dtype=np.uint32), np.ascontiguousarray(indices, dtype=np.uint32),
+            _f32(values))
+
+
+def leiden(indptr, indices, values, n_cols: int, resolution: float = 1.0, n_iterations: int = 2, seed: int = 0):
+    """(labels u32, modularity, n_communities) of the restated Leiden (cluster.rs:88)."""
+    ip, ix, vl = _csr32(indptr, indices, values)
+    n = len(ip) - 1
+    labels = np.zeros(max(n, 1), np.uint32)
+    q = ctypes.c_double()
+    nc = np.zeros(1, np.int64)
+    _check(_lib().oracle_leiden(_p(ip, ctypes.c_uint32), _p(ix, ctypes.c_uint32), _p(vl, ctypes.c_float), n, n_cols,
+                                resolution, n_iterations, ctypes.c_uint64(seed), _p(labels, ctypes.c_uint32),
+                                ctypes.byref(q), _p(nc, ctypes.c_int64)), "leiden")
+    return labels[:n], q.value, int(nc[0])
+
+
+def louvain(indptr, indices, values, n_cols: int, resolution: float = 1.0, seed: int = 0):
+    """(labels u32, modularity, n_communities) of the restated Louvain (cluster.rs:125)."""
+    ip, ix, vl = _csr32(indptr, indices, values)
+    n = len(ip) - 1
+    labels = np.zeros(max(n, 1), np.uint32)
+    q = ctypes.c_double()
+    nc = np.zeros(1, np.int64)
+    _check(_lib().oracle_louvain(_p(ip, ctypes.c_uint32), _p(ix, ctypes.c_uint32), _p(vl, ctypes.c_float), n, n_cols,
+                                 resolution, ctypes.c_uint64(seed), _p(labels, ctypes.c_uint32), ctypes.byref(q),
+                                 _p(nc, ctypes.c_int64)), "louvain")
+    return labels[:n], q.value, int(nc[0])
+
+
+def modularity(indptr, indices, values, n_cols: int, labels, resolution: float = 1.0) -> float:
+    """Q of a labelling (cluster.rs:148)."""
+    ip, ix, vl = _csr32(indptr, indices, values)
+    lb = np.ascontiguousarray(labels, dtype=np.uint32)
+    q = ctypes.c_double()
+    _check(_lib().oracle_modularity(_p(ip, ctypes.c_uint32), _p(ix, ctypes.c_uint32), _p(vl, ctypes.c_float),
+                                    len(ip) - 1, n_cols, _p(lb, ctypes.c_uint32), len(lb), resolution,
+                                    ctypes.byref(q)), "modularity")
+    return q.value

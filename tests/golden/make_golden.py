@@ -11,8 +11,9 @@ connectivity rows, and the exact nnz / weight sum / square sum of the whole
 matrix) and writes them, unchanged, to `scanpy_reference_embedding_300x20.json`;
 and the UMAP constants of crates/scrust-core/src/umap.rs's tests (the 80-cell
 scanpy graph and layout, umap-learn's fitted-curve table) to
-`umap_reference_80_cells.json`.  The values are parsed from the source text,
-not re-typed.
+`umap_reference_80_cells.json`; and scanpy's PCA of the 300 x 200 fixture of
+crates/scrust-core/src/pca.rs's tests to `pca_scanpy_300x200.json`.  The
+values are parsed from the source text, not re-typed.
 """
 
 from __future__ import annotations
@@ -95,6 +96,30 @@ def parse_umap(umap_rs: str) -> dict:
     }
 
 
+def parse_pca(pca_rs: str) -> dict:
+    """scanpy's arpack PCA of the 300 x 200 LCG fixture that
+    crates/scrust-core/src/pca.rs pins (tests module)."""
+    ratio = [_rust_float(v) for v in re.findall(r"-?[0-9][0-9eE_.+-]*",
+                                                  _block(pca_rs, "SCANPY_VARIANCE_RATIO: [f32; 3]"))]
+    variance = [_rust_float(v) for v in re.findall(r"-?[0-9][0-9eE_.+-]*",
+                                                     _block(pca_rs, "SCANPY_VARIANCE: [f32; 3]"))]
+    start = pca_rs.index("SCANPY_EMBEDDING")
+    eq = pca_rs.index("=", start)
+    end = pca_rs.index("];", eq)
+    rows = re.findall(r"\[([^\[\]]+)\]", pca_rs[eq + 1:end + 1])
+    embedding = [[_rust_float(v) for v in re.findall(r"-?[0-9][0-9eE_.+-]*", row)] for row in rows]
+    assert len(ratio) == 3 and len(variance) == 3 and len(embedding) == 3 and all(len(r) == 300 for r in embedding)
+    return {
+        "source": "crates/scrust-core/src/pca.rs (tests: SCANPY_VARIANCE_RATIO, SCANPY_VARIANCE, SCANPY_EMBEDDING; "
+                  "scanpy 1.12.2 sc.pp.pca(n_comps=10, svd_solver='arpack'))",
+        "fixture": {"generator": "lcg", "seed": 42, "n_cells": 300, "n_genes": 200},
+        "scanpy_variance_ratio": ratio,
+        "scanpy_variance": variance,
+        "scanpy_embedding": embedding,
+        "bars": {"correlation_min": 0.99, "variance_relative_tolerance": 1e-3, "n_comps": 10},
+    }
+
+
 def main(argv: list[str]) -> None:
     if len(argv) != 2:
         raise SystemExit("usage: make_golden.py <path of the scrust checkout>")
@@ -106,6 +131,10 @@ def main(argv: list[str]) -> None:
     umap_text = (root / "crates/scrust-core/src/umap.rs").read_text()
     out = HERE / "umap_reference_80_cells.json"
     out.write_text(json.dumps(parse_umap(umap_text), indent=1) + "\n")
+    print(f"wrote {out}")
+    pca_text = (root / "crates/scrust-core/src/pca.rs").read_text()
+    out = HERE / "pca_scanpy_300x200.json"
+    out.write_text(json.dumps(parse_pca(pca_text), indent=1) + "\n")
     print(f"wrote {out}")
 
 

@@ -128,8 +128,41 @@ def test_core_routes_cpu_to_the_reference_module():
     core.connectivities(np.zeros((6, 2), np.uint32), np.ones((6, 2), np.float32))
     assert [c[0] for c in real.calls] == ["knn", "connectivities"] and ours.calls == []
     # every other attribute is the reference module's
-    real.pca = lambda *a: "pca"
-    assert core.pca() == "pca"
+    real.morans_i = lambda *a: "morans_i"
+    assert core.morans_i() == "morans_i"
+
+
+class Tagged:
+    """Answers every call with (its own tag, the call's name, the args)."""
+
+    def __init__(self, tag):
+        self.tag = tag
+
+    def __getattr__(self, name):
+        return lambda *args: (self.tag, name, args)
+
+
+@pytest.mark.parametrize("name,args", [
+    ("umap", ("ip", "ix", "vl", 5, 2, 10, 0.5, 1.0, 1.0, 5, 0)),
+    ("pca", ("ip", "ix", "vl", 5, 2, True, 0)),
+    ("leiden", ("ip", "ix", "vl", 5, 1.0, 2, 0)),
+    ("louvain", ("ip", "ix", "vl", 5, 1.0, 0)),
+])
+def test_core_routes_the_other_stages_by_their_device(name, args):
+    from mrustsc_gb300.core import Core
+
+    core = Core(Tagged("reference"), device_setting=lambda: "auto", backend=Tagged("gb300"))
+    assert getattr(core, name)(*args, "cpu") == ("reference", name, args + ("cpu",))
+    for device in ("auto", "gpu", "cuda:0"):
+        assert getattr(core, name)(*args, device) == ("gb300", name, args + (device,))
+
+
+def test_core_routes_modularity_by_the_settings_device():
+    from mrustsc_gb300.core import Core
+
+    args = ("ip", "ix", "vl", 5, "labels", 1.0)
+    assert Core(Tagged("reference"), lambda: "cpu", Tagged("gb300")).modularity(*args)[0] == "reference"
+    assert Core(Tagged("reference"), lambda: "auto", Tagged("gb300")).modularity(*args)[0] == "gb300"
 
 
 def test_unmodified_neighbors_surface_through_the_core_on_cpu(monkeypatch):
@@ -144,3 +177,68 @@ def test_unmodified_neighbors_surface_through_the_core_on_cpu(monkeypatch):
     pp.neighbors(adata, n_neighbors=4, device="cpu")
     assert real.args_of("knn")[1:] == (3, "cpu") and ours.calls == []
     assert adata.obsp["distances"].shape == (N_OBS, N_OBS)
+
+
+class ClusterCore(FakeCore):
+    def leiden(self, indptr, indices, values, n_cols, resolution, n_iterations, seed, device):
+        self.calls.append(("leiden", (n_cols, resolution, n_iterations, seed, device), {}))
+        return np.array([1, 0, 0, 1, 2, 0, 1], np.uint32), 0.25, 3
+
+    def louvain(self, indptr, indices, values, n_cols, resolution, seed, device):
+        self.calls.append(("louvain", (n_cols, resolution, seed, device), {}))
+        return np.array([0, 0, 1, 1, 0, 1, 0], np.uint32), 0.5, 2
+
+
+@pytest.fixture
+def cluster_core(monkeypatch):
+    fake = ClusterCore()
+    import mrustsc_gb300.tl as tl
+    monkeypatch.setattr(tl, "_extension", lambda: fake)
+    return fake
+
+
+def _graph_adata():
+    adata = _adata()
+    adata.obsp["connectivities"] = sp.csr_matrix(np.ones((N_OBS, N_OBS), np.float32) - np.eye(N_OBS, dtype=np.float32))
+    return adata
+
+
+def _labels_of(column):
+    return [str(x) for x in np.asarray(column)]
+
+
+def test_leiden_writes_obs_and_uns_as_scanpy(cluster_core):
+    """python/scrust/tl/_cluster.py:51-79: obs[key] labels as strings,
+    uns[key] = {params, modularity}; the arguments reach the core unchanged."""
+    from mrustsc_gb300 import tl
+
+    adata = _graph_adata()
+    assert tl.leiden(adata, 0.7, n_iterations=3, random_state=4) is None
+    assert cluster_core.args_of("leiden") == (N_OBS, 0.7, 3, 4, "auto")
+    assert _labels_of(adata.obs["leiden"]) == ["1", "0", "0", "1", "2", "0", "1"]
+    assert adata.uns["leiden"] == {"params": {"resolution": 0.7, "random_state": 4, "n_iterations": 3},
+                                   "modularity": 0.25}
+
+
+def test_louvain_writes_under_its_key(cluster_core):
+    from mrustsc_gb300 import tl
+
+    adata = _graph_adata()
+    tl.louvain(adata, key_added="groups", random_state=2, device="cuda")
+    assert cluster_core.args_of("louvain") == (N_OBS, 1.0, 2, "cuda")
+    assert _labels_of(adata.obs["groups"]) == ["0", "0", "1", "1", "0", "1", "0"]
+    assert adata.uns["groups"] == {"params": {"resolution": 1.0, "random_state": 2}, "modularity": 0.5}
+
+
+def test_clustering_reads_the_graph_neighbors_key_names(cluster_core):
+    """uns[neighbors_key]["connectivities_key"] picks the obsp entry
+    (python/scrust/tl/_cluster.py:18-28); no graph at all raises KeyError."""
+    from mrustsc_gb300 import tl
+
+    adata = _adata()
+    adata.obsp["alt"] = sp.csr_matrix(np.ones((N_OBS, N_OBS), np.float32))
+    adata.uns["nbrs"] = {"connectivities_key": "alt"}
+    tl.leiden(adata, neighbors_key="nbrs")
+    assert "leiden" in adata.obs
+    with pytest.raises(KeyError):
+        tl.leiden(_adata())
