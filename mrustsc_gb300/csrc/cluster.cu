@@ -662,6 +662,8 @@ int64_t Clusterer::compact(const uint32_t* labels, int64_t n, int64_t width, uin
 
 int32_t Clusterer::build(const uint32_t* indptr, const uint32_t* indices, const float* values, int64_t n,
                          int64_t nnz) {
+    if (nnz == 0)
+        return fail(st_, SCRUST_INVALID_PARAMETER, "the graph needs at least one edge of positive weight");
     int* bad = alloc<int>(1);
     uint32_t* erow = alloc<uint32_t>(nnz);
     const int64_t m = 2 * nnz;

@@ -40,6 +40,10 @@ def louvain(scrust, g, resolution=1.0, seed=0):
     return scrust.louvain(*g, resolution, seed, "auto")
 
 
+def u32(labels):
+    return np.asarray(labels, np.uint32)
+
+
 def knn_graph(scrust, n, clusters, seed, d=20, k=15):
     rng = np.random.default_rng(seed)
     centres = rng.uniform(-4.0, 4.0, size=(clusters, d)).astype(np.float32)
@@ -55,11 +59,11 @@ def test_modularity_matches_hand_computed_values(scrust, oracle):
              ([0, 1, 2, 3, 4, 5], 1.0, -sum((k / 14.0) ** 2 for k in (2, 2, 3, 3, 2, 2))),
              ([0, 0, 0, 1, 1, 1], 2.0, 6 / 7 - 1.0)]
     for labels, res, want in cases:
-        got = scrust.modularity(*g, labels, res)
+        got = scrust.modularity(*g, u32(labels), res)
         assert abs(got - want) < EXACT_TOL
         assert abs(got - oracle.modularity(*g, labels, resolution=res)) < EXACT_TOL
     # (A + A^T) / 2: the one-sided barbell at weight 2 is the barbell
-    assert abs(scrust.modularity(*cc.half_barbell(), [0, 0, 0, 1, 1, 1], 1.0) - (6 / 7 - 0.5)) < EXACT_TOL
+    assert abs(scrust.modularity(*cc.half_barbell(), u32([0, 0, 0, 1, 1, 1]), 1.0) - (6 / 7 - 0.5)) < EXACT_TOL
 
 
 @pytest.mark.parametrize("algorithm", ["leiden", "louvain"])
@@ -125,10 +129,12 @@ def test_rejects_degenerate_input(scrust):
     rectangular = (np.array([0, 1], np.uint32), np.array([2], np.uint32), np.array([1.0], np.float32), 4)
     with pytest.raises(ValueError):
         leiden(scrust, rectangular)
-    with pytest.raises(ValueError):
-        scrust.modularity(*g, [0, 0], 1.0)
-    with pytest.raises(ValueError):
-        scrust.modularity(*cc.barbell(), [0, 1, 2, 3, 4, 2**32 - 1], 1.0)
+    with pytest.raises(ValueError, match="labels, one per node"):
+        scrust.modularity(*g, u32([0, 0]), 1.0)
+    with pytest.raises(ValueError, match="below the node count"):
+        scrust.modularity(*cc.barbell(), u32([0, 1, 2, 3, 4, 2**32 - 1]), 1.0)
+    with pytest.raises(ValueError, match="1-D numpy array of uint32"):
+        scrust.modularity(*cc.barbell(), [0, 0, 0, 1, 1, 1], 1.0)
 
 
 @pytest.mark.parametrize("n,clusters,seed", [(3000, 12, 1), (20000, 40, 2)])
