@@ -333,7 +333,7 @@ def run_ours(args):
     clocks.start()
     launches0 = L.scrust_cuda_launch_count(ctx)
     phases = []
-    buf = (ctypes.c_float * 6)()
+    buf = (ctypes.c_float * 8)()
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
     total_ms = 0.0
@@ -343,7 +343,7 @@ def run_ours(args):
         end.record(stream)
         end.synchronize()
         total_ms += start.elapsed_time(end)
-        got = L.scrust_cuda_phase_times(ctx, buf, 6)
+        got = L.scrust_cuda_phase_times(ctx, buf, 8)
         phases.append([buf[i] for i in range(got)])
     torch.cuda.synchronize()
     launches = int(L.scrust_cuda_launch_count(ctx) - launches0)
@@ -365,7 +365,7 @@ def run_ours(args):
     nnz = int(L.scrust_csr_nnz(out))
     L.scrust_csr_free(out)
 
-    ph = np.array(phases) if phases and len(phases[0]) == 6 else np.zeros((1, 6))
+    ph = np.array(phases) if phases and len(phases[0]) == 8 else np.zeros((1, 8))
     ph_mean = ph.mean(0)
     cand_ms = float(ph_mean[1])
     pk, pk_kind = peaks()
@@ -378,12 +378,27 @@ def run_ours(args):
         # pair, 2 * 256 * 256 * d algorithmic flops; the pairs it computes are
         # counted by the kernel's own counters in one extra, untimed step.
         sweep_ms = cand_ms - float(ph_mean[5]) if ph_mean[4] > 0 else cand_ms
-        cnt = (ctypes.c_uint64 * 16)()
-        L.scrust_cuda_kernel_stats(ctx, 1, cnt, 16)
+        cnt = (ctypes.c_uint64 * 80)()
+        L.scrust_cuda_kernel_stats(ctx, 1, cnt, 80)
         step()
         _lib.check(L.scrust_cuda_synchronize(ctx, ctypes.byref(st)), st)
-        L.scrust_cuda_kernel_stats(ctx, 0, cnt, 16)
+        L.scrust_cuda_kernel_stats(ctx, 0, cnt, 80)
         tiles = int(cnt[8])
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        if ph_mean[4] > 0:
+            # The four launches of an ordered solve, with their own counters.
+            collect2_ms = cand_ms - float(ph_mean[4] + ph_mean[5] + ph_mean[6] + ph_mean[7])
+            pass_ms = [float(ph_mean[4]), float(ph_mean[6]), float(ph_mean[7]), collect2_ms]
+            names = ["threshold, priority tiles", "threshold, kept tiles", "collect, priority tiles",
+                     "collect, kept tiles"]
+            sweep_passes = []
+            for i, name in enumerate(names):
+                c = [int(cnt[16 * (i + 1) + j]) for j in range(16)]
+                t = c[8]
+                sweep_passes.append({"pass": name, "ms": pass_ms[i], "tiles": t,
+                                     "us_per_tile_per_sm": pass_ms[i] * 1e3 * sms / t if t else None,
+                                     "appends": c[0], "topk_chunks_entered": c[12], "topk_bulk_merges": c[13],
+                                     "topk_insert_rounds": c[14], "topk_entrants": c[15]})
         blocks = (n + 255) // 256
         flops = tiles * 2.0 * 256 * 256 * d
         achieved = flops / (sweep_ms / 1e3) / 1e12
@@ -395,6 +410,8 @@ def run_ours(args):
                 "kernel_ms": sweep_ms, "units": "(256-row block, 256-column tile) pairs computed",
                 "units_per_step": tiles, "flops_per_unit": 2 * 256 * 256 * d,
                 "brute_force_units": blocks * blocks, "peak_source": f"bf16 burst, {pk_kind}"}
+        if ph_mean[4] > 0:
+            roof["passes"] = sweep_passes
     else:
         flops = 2.0 * n * n * d
         sm_count = torch.cuda.get_device_properties(local).multi_processor_count
@@ -419,7 +436,9 @@ def run_ours(args):
             "phases_ms": {"prep": float(ph_mean[0]), "candidates": float(ph_mean[1]),
                           "rerank": float(ph_mean[2]), "connectivities": float(ph_mean[3]),
                           "candidates_first_pass": float(ph_mean[4]),
-                          "candidates_tile_lists": float(ph_mean[5])},
+                          "candidates_tile_lists": float(ph_mean[5]),
+                          "candidates_second_pass": float(ph_mean[6]),
+                          "candidates_first_collect": float(ph_mean[7])},
             "phases_gbs": phases_gbs, "phases_gbs_peak": f"{hbm} GB/s, {pk_kind} copy bandwidth",
             "graph_nnz": nnz, "gpu_launches": launches, "roofline": roof, "clocks": clk}
 

@@ -439,9 +439,10 @@ SCRUST_API int32_t scrust_cuda_modularity(scrust_context* context, const uint32_
 /* Phase timing.  When enabled, each kNN / connectivities call records CUDA
  * events on the context stream around its phases; scrust_cuda_phase_times
  * writes the last call's milliseconds (after a synchronise) in the order
- * prep, candidates, rerank, connectivities, then two parts of candidates in
- * an ordered tensor-form solve (its first sweep pass and the building of the
- * second pass's tile lists; 0 otherwise), and returns how many it wrote. */
+ * prep, candidates, rerank, connectivities, then four parts of candidates in
+ * an ordered tensor-form solve (its first sweep pass, the building of the
+ * second pass's tile lists, the second pass, and the first collect pass when
+ * k <= 32; 0 otherwise), and returns how many it wrote. */
 SCRUST_API void scrust_cuda_set_timing(scrust_context* context, int32_t enable);
 SCRUST_API int32_t scrust_cuda_phase_times(scrust_context* context, float* ms, int32_t max_phases);
 
@@ -452,7 +453,11 @@ SCRUST_API int32_t scrust_cuda_phase_times(scrust_context* context, float* ms, i
  * 2 overflow rows, 3 epilogue wait cycles, 5/6 MMA wait cycles (B tiles,
  * accumulators), 7 producer wait cycles, 8 tiles, 9 prune cycles, and for the
  * register top-k 12 chunks with an entrant, 13 bulk merges, 14 insertion
- * rounds, 15 entrants; 4, 10 and 11 are unused. */
+ * rounds, 15 entrants; 4, 10 and 11 are unused.  Words 0-15 hold every sweep
+ * launch together; with max_words up to 80, words 16-31, 32-47 and 48-63 hold
+ * the first, second and third sweep launch of each solve on their own and
+ * 64-79 every later launch (an ordered solve with k <= 32 runs the two
+ * threshold passes, then the two collect passes). */
 SCRUST_API int32_t scrust_cuda_kernel_stats(scrust_context* context, int32_t enable, uint64_t* out,
                                             int32_t max_words);
 

@@ -104,11 +104,19 @@ bool encode_2d(scrust_context* ctx, CUtensorMap* map, CUtensorMapDataType dtype,
 
 size_t plain_smem_bytes(int dp);
 
+// The counter block of the next sweep launch, or null when statistics are off.
+unsigned long long* sweep_stats(scrust_context* ctx) {
+    if (!ctx->d_stats) return nullptr;
+    const int slot = std::min(ctx->stats_launch, kStatSlots - 1);
+    ctx->stats_launch++;
+    return ctx->d_stats + kStatWords * slot;
+}
+
 void mark(scrust_context* ctx, Phase p) {
     if (!ctx->timing) return;
     if (!ctx->ev[p] && cudaEventCreate(&ctx->ev[p]) != cudaSuccess) return;
     if (p == PH_START)
-        for (int i = 0; i < 7; i++) ctx->ev_recorded[i] = false;
+        for (int i = 0; i < PH_COUNT; i++) ctx->ev_recorded[i] = false;
     if (cudaEventRecord(ctx->ev[p], ctx->stream) == cudaSuccess) ctx->ev_recorded[p] = true;
 }
 
@@ -279,6 +287,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
     const float* xwork = x;
     float* xcentred = nullptr;
     double* norm64 = nullptr;
+    ctx->stats_launch = 0;
     mark(ctx, PH_START);
     if (cosine) {
         float* xn = (float*)ws_get(ctx, SLOT_XWORK, sizeof(float) * (size_t)n * d, &e);
@@ -380,7 +389,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
             const int mode = split ? kPassThresholds : kPassFull;
             rerank_ids_only = split;
             if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                              &first, false, order.theta, nullptr, ctx->d_stats, nullptr, mode)) !=
+                                              &first, false, order.theta, nullptr, sweep_stats(ctx), nullptr, mode)) !=
                 cudaSuccess)
                 return cuda_fail(st, e, "knn_candidates_tc");
             mark(ctx, PH_PASS1);
@@ -388,16 +397,19 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
             if ((rc = build_second_pass(ctx, A16, bf16, n, d, order, bA, bdelta, &second, st))) return rc;
             mark(ctx, PH_LISTS);
             if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                              &second, true, order.theta, nullptr, ctx->d_stats, nullptr, mode)) !=
+                                              &second, true, order.theta, nullptr, sweep_stats(ctx), nullptr, mode)) !=
                 cudaSuccess)
                 return cuda_fail(st, e, "knn_candidates_tc");
+            mark(ctx, PH_PASS2);
             ctx->launches += 2;
             if (split) {
                 if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                                  &first, false, order.theta, nullptr, ctx->d_stats, nullptr,
-                                                  kPassCollect)) != cudaSuccess ||
-                    (e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                                  &second, true, order.theta, nullptr, ctx->d_stats, nullptr,
+                                                  &first, false, order.theta, nullptr, sweep_stats(ctx), nullptr,
+                                                  kPassCollect)) != cudaSuccess)
+                    return cuda_fail(st, e, "knn_candidates_tc");
+                mark(ctx, PH_COLLECT1);
+                if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
+                                                  &second, true, order.theta, nullptr, sweep_stats(ctx), nullptr,
                                                   kPassCollect)) != cudaSuccess)
                     return cuda_fail(st, e, "knn_candidates_tc");
                 ctx->launches += 2;
@@ -417,7 +429,7 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
                     return cuda_fail(st, e, "memset");
             }
             if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                              &shared, false, theta, nullptr, ctx->d_stats)) != cudaSuccess)
+                                              &shared, false, theta, nullptr, sweep_stats(ctx))) != cudaSuccess)
                 return cuda_fail(st, e, "knn_candidates_tc");
             ctx->launches += 1;
         }
@@ -1001,10 +1013,11 @@ int32_t scrust_cuda_phase_times(scrust_context* ctx, float* ms, int32_t max_phas
         }
         ms[written++] = t;
     }
-    // Inside the candidates phase of an ordered solve: the first sweep pass
-    // and the building of the second pass's tile lists.
-    const int sub[2][2] = {{PH_PREP, PH_PASS1}, {PH_PASS1, PH_LISTS}};
-    for (int i = 0; i < 2 && written < max_phases; ++i) {
+    // Inside the candidates phase of an ordered solve: the first sweep pass,
+    // the building of the second pass's tile lists, the second pass, and the
+    // first collect pass (k <= 32).
+    const int sub[4][2] = {{PH_PREP, PH_PASS1}, {PH_PASS1, PH_LISTS}, {PH_LISTS, PH_PASS2}, {PH_PASS2, PH_COLLECT1}};
+    for (int i = 0; i < 4 && written < max_phases; ++i) {
         float t = 0.f;
         if (!(ctx->ev_recorded[sub[i][0]] && ctx->ev_recorded[sub[i][1]] &&
               cudaEventElapsedTime(&t, ctx->ev[sub[i][0]], ctx->ev[sub[i][1]]) == cudaSuccess)) {
@@ -1022,23 +1035,27 @@ int32_t scrust_cuda_kernel_stats(scrust_context* ctx, int32_t enable, uint64_t* 
     if (!ctx) return 0;
     std::lock_guard<std::mutex> lock(ctx->mu);
     DeviceGuard device_guard(ctx->device);
+    constexpr size_t bytes = sizeof(unsigned long long) * kStatWords * kStatSlots;
     if (enable && !ctx->d_stats) {
-        if (cudaMalloc(&ctx->d_stats, 16 * sizeof(unsigned long long)) != cudaSuccess) {
+        if (cudaMalloc(&ctx->d_stats, bytes) != cudaSuccess) {
             cudaGetLastError();
             ctx->d_stats = nullptr;
             return 0;
         }
-        cudaMemsetAsync(ctx->d_stats, 0, 16 * sizeof(unsigned long long), ctx->stream);
+        cudaMemsetAsync(ctx->d_stats, 0, bytes, ctx->stream);
     }
     int written = 0;
     if (ctx->d_stats && out && max_words > 0) {
-        unsigned long long h[16] = {0};
-        if (cudaMemcpyAsync(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess &&
+        // Words 0-15: every launch together; then 16 words per slot.
+        unsigned long long h[kStatWords * (kStatSlots + 1)] = {0};
+        if (cudaMemcpyAsync(h + kStatWords, ctx->d_stats, bytes, cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess &&
             cudaStreamSynchronize(ctx->stream) == cudaSuccess) {
-            written = max_words < 16 ? max_words : 16;
+            for (int s = 1; s <= kStatSlots; s++)
+                for (int i = 0; i < kStatWords; i++) h[i] += h[kStatWords * s + i];
+            written = std::min(max_words, kStatWords * (kStatSlots + 1));
             for (int i = 0; i < written; i++) out[i] = h[i];
         }
-        cudaMemsetAsync(ctx->d_stats, 0, 16 * sizeof(unsigned long long), ctx->stream);
+        cudaMemsetAsync(ctx->d_stats, 0, bytes, ctx->stream);
     }
     if (!enable && ctx->d_stats) {
         cudaStreamSynchronize(ctx->stream);

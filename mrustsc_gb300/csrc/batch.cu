@@ -220,7 +220,7 @@ int32_t batch_enqueue(scrust_context* ctx, const float* x, const void* table, ui
     tl.order = order;
     mark(ctx, PH_PREP);
     if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16, &tl, false,
-                                      theta, nullptr, ctx->d_stats)) != cudaSuccess)
+                                      theta, nullptr, sweep_stats(ctx))) != cudaSuccess)
         return cuda_fail(st, e, "batch: knn_candidates_tc");
     ctx->launches += 1;
     mark(ctx, PH_CAND);

@@ -116,10 +116,13 @@ struct scrust_context {
     std::vector<scrust::CsrBuffers> csr_pool;
     PFN_cuTensorMapEncodeTiled_v12000 encode_tiled = nullptr;
     uint64_t launches = 0;              // kernels enqueued so far
-    unsigned long long* d_stats = nullptr;  // kernel counters when statistics are on (16 words)
+    // Kernel counters when statistics are on: 16 words per sweep launch of a
+    // solve, for its first three launches and all later ones together.
+    unsigned long long* d_stats = nullptr;
+    int stats_launch = 0;               // sweep launches of the current solve so far
     bool timing = false;
-    cudaEvent_t ev[7] = {};             // phase boundaries: prep | candidates | rerank | connectivities,
-    bool ev_recorded[7] = {};           // and inside candidates: first sweep pass | second-pass tile lists
+    cudaEvent_t ev[9] = {};             // phase boundaries: prep | candidates | rerank | connectivities, and
+    bool ev_recorded[9] = {};           // inside candidates: sweep pass 1 | tile lists | pass 2 | collect 1
     std::vector<std::pair<const void*, int>> smem_limits;  // dynamic shared memory limits already set
     std::vector<const void*> carveouts;                      // kernels whose shared-memory carveout is set
 };
@@ -145,8 +148,13 @@ struct scrust_csr {
 namespace scrust {
 
 // Phase boundary events (no-ops unless timing is enabled).
-enum Phase { PH_START = 0, PH_PREP = 1, PH_CAND = 2, PH_RERANK = 3, PH_CONN = 4, PH_PASS1 = 5, PH_LISTS = 6 };
+enum Phase {
+    PH_START = 0, PH_PREP = 1, PH_CAND = 2, PH_RERANK = 3, PH_CONN = 4, PH_PASS1 = 5, PH_LISTS = 6, PH_PASS2 = 7,
+    PH_COLLECT1 = 8, PH_COUNT = 9
+};
+static_assert(sizeof(scrust_context::ev) / sizeof(cudaEvent_t) == PH_COUNT, "one event per phase boundary");
 void mark(scrust_context* ctx, Phase p);
+unsigned long long* sweep_stats(scrust_context* ctx);
 
 // Maps the device error block to a status, then clears it (synchronises).
 int32_t collect_device_errors(scrust_context* ctx, scrust_status* st);
@@ -299,6 +307,9 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
 // thresholds only (register top-k, theta_io written, lists untouched), then
 // collection at the fixed thresholds (appends only).
 constexpr int kPassFull = 0, kPassThresholds = 1, kPassCollect = 2;
+// Kernel counters: words per block, and blocks (the first three sweep
+// launches of a solve, then all later ones).
+constexpr int kStatWords = 16, kStatSlots = 4;
 
 // Per-row bound of the candidate lists, as the rerank re-applies it: the
 // plain form's additive margin, or the tensor form's (A, delta, eps2).
