@@ -256,13 +256,18 @@ struct TopK {
         v[0] = fminf(v[0], x);
     }
     __device__ __forceinline__ float kth() const { return v[K - 1]; }
-    // Merges 32 ascending values in (f32 bit patterns): the K smallest of
-    // both, ascending (the elementwise minimum against the reversed run is
-    // bitonic; a bitonic clean-up sorts it).
-    __device__ __forceinline__ void merge_sorted(const uint32_t (&x)[32]) {
-        static_assert(K <= 32, "merge_sorted holds at most 32 values");
+    // Merges N ascending values in: the K smallest of both, ascending (the
+    // N values padded to K with +inf, against the reversed run, then the
+    // bitonic clean-up).
+    template <int N>
+    __device__ __forceinline__ void merge_few(const float (&g)[N]) {
+        static_assert(K >= N, "merge_few needs at least N slots");
 #pragma unroll
-        for (int i = 0; i < K; i++) v[i] = fminf(v[i], __uint_as_float(x[K - 1 - i]));
+        for (int t = 0; t < N; t++) v[K - N + t] = fminf(v[K - N + t], g[N - 1 - t]);
+        clean_up();
+    }
+    // Bitonic clean-up of v into ascending order.
+    __device__ __forceinline__ void clean_up() {
 #pragma unroll
         for (int stride = K >> 1; stride > 0; stride >>= 1)
 #pragma unroll
@@ -275,7 +280,84 @@ struct TopK {
                 }
             }
     }
+    // Merges 32 ascending values in (f32 bit patterns): the K smallest of
+    // both, ascending (the elementwise minimum against the reversed run is
+    // bitonic; a bitonic clean-up sorts it).
+    __device__ __forceinline__ void merge_sorted(const uint32_t (&x)[32]) {
+        static_assert(K <= 32, "merge_sorted holds at most 32 values");
+#pragma unroll
+        for (int i = 0; i < K; i++) v[i] = fminf(v[i], __uint_as_float(x[K - 1 - i]));
+        clean_up();
+    }
 };
+
+#define SCRUST_CAS(i, j)                                            \
+    {                                                               \
+        const float lo_ = fminf(g[i], g[j]), hi_ = fmaxf(g[i], g[j]); \
+        g[i] = lo_;                                                 \
+        g[j] = hi_;                                                 \
+    }
+// Ascending sort of eight values in registers (a 19-comparator network).
+__device__ __forceinline__ void sort8(float (&g)[8]) {
+    SCRUST_CAS(0, 1) SCRUST_CAS(2, 3) SCRUST_CAS(4, 5) SCRUST_CAS(6, 7)
+    SCRUST_CAS(0, 2) SCRUST_CAS(1, 3) SCRUST_CAS(4, 6) SCRUST_CAS(5, 7)
+    SCRUST_CAS(1, 2) SCRUST_CAS(5, 6) SCRUST_CAS(0, 4) SCRUST_CAS(3, 7)
+    SCRUST_CAS(1, 5) SCRUST_CAS(2, 6) SCRUST_CAS(1, 4) SCRUST_CAS(3, 6)
+    SCRUST_CAS(2, 4) SCRUST_CAS(3, 5) SCRUST_CAS(3, 4)
+}
+// Ascending sort of four values (five comparators).
+__device__ __forceinline__ void sort4(float (&g)[4]) {
+    SCRUST_CAS(0, 1) SCRUST_CAS(2, 3) SCRUST_CAS(0, 2) SCRUST_CAS(1, 3) SCRUST_CAS(1, 2)
+}
+#undef SCRUST_CAS
+
+// Columns past the reference rows and the row itself become +inf, so that
+// no group minimum is taken over them (they occur in at most two chunks of
+// a work item: the warp branches once).
+__device__ __forceinline__ void mask_chunk(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a) {
+    const uint32_t valid = chunk_valid(colbase, a.nr, a.self != 0, row + a.self_offset);
+    if (__any_sync(0xffffffffu, valid != 0xffffffffu)) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) v[j] = ((valid >> j) & 1u) ? v[j] : 0x7f800000u;
+    }
+}
+
+// The minima of a chunk's four 8-column groups.
+__device__ __forceinline__ void quarter_mins(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a,
+                                             float (&g)[4]) {
+    mask_chunk(v, colbase, row, a);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int b = 8 * q;
+        g[q] = min3f(min3f(f_of(v[b]), f_of(v[b + 1]), f_of(v[b + 2])),
+                     min3f(f_of(v[b + 3]), f_of(v[b + 4]), f_of(v[b + 5])), fminf(f_of(v[b + 6]), f_of(v[b + 7])));
+    }
+}
+
+// The minima of a chunk's eight 4-column groups.
+__device__ __forceinline__ void eighth_mins(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a,
+                                            float (&g)[8]) {
+    mask_chunk(v, colbase, row, a);
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        g[q] = fminf(min3f(f_of(v[4 * q]), f_of(v[4 * q + 1]), f_of(v[4 * q + 2])), f_of(v[4 * q + 3]));
+}
+
+// The minima of a chunk's two 16-column halves.
+__device__ __forceinline__ void half_mins(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a,
+                                          float& lo, float& hi) {
+    mask_chunk(v, colbase, row, a);
+    float m[12];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int b = 16 * h;
+#pragma unroll
+        for (int i = 0; i < 5; i++) m[6 * h + i] = min3f(f_of(v[b + 3 * i]), f_of(v[b + 3 * i + 1]), f_of(v[b + 3 * i + 2]));
+        m[6 * h + 5] = f_of(v[b + 15]);
+    }
+    lo = fminf(min3f(m[0], m[1], m[2]), min3f(m[3], m[4], m[5]));
+    hi = fminf(min3f(m[6], m[7], m[8]), min3f(m[9], m[10], m[11]));
+}
 
 // Ascending bitonic sort of 32 f32 values held as bit patterns in
 // registers, in place (fully unrolled, static indices).
@@ -702,6 +784,104 @@ __global__ void __launch_bounds__(THREADS, 1)
                                     cnt++;
                                 }
                             }
+                        }
+                    } else if constexpr (TOPK == 16 && PASS == 1) {
+                        // Threshold pass: each group of columns offers only
+                        // its minimum.  The top-K then holds values of
+                        // distinct columns, so its K-th is still an upper
+                        // bound of the row's k-th smallest (slightly above it
+                        // when two of the nearest share a group), and a tile
+                        // costs a sort of its group minima and a merge instead
+                        // of an insertion per entrant.  Groups of 8 on an
+                        // item's first tile (16 minima per lane: the K-th is
+                        // finite after one tile), of 16 after it.
+                        const float kth0 = top.kth();
+                        uint32_t vb[32];
+                        if (it == 0) {
+#pragma unroll 1
+                            for (int c = 0; c < 4; ++c) {
+                                float q[4];
+                                tmem_ld32(tbase + 32 * c, va);
+                                tmem_ld_wait(va);
+                                quarter_mins(va, col0 + 32 * c, row, a, q);
+                                cm[c] = fminf(fminf(q[0], q[1]), fminf(q[2], q[3]));
+                                if (__any_sync(0xffffffffu, cm[c] < fminf(top.kth(), th))) {
+                                    sort4(q);
+                                    top.merge_few(q);
+                                }
+                            }
+                            th = fminf(th, bnd.theta_f32(top.kth()));
+                        } else {
+                            float g[8];
+                            tmem_ld32(tbase, va);
+                            tmem_ld_wait(va);
+                            tmem_ld32(tbase + 32, vb);
+                            half_mins(va, col0, row, a, g[0], g[1]);
+                            tmem_ld_wait(vb);
+                            tmem_ld32(tbase + 64, va);
+                            half_mins(vb, col0 + 32, row, a, g[2], g[3]);
+                            tmem_ld_wait(va);
+                            tmem_ld32(tbase + 96, vb);
+                            half_mins(va, col0 + 64, row, a, g[4], g[5]);
+                            tmem_ld_wait(vb);
+                            half_mins(vb, col0 + 96, row, a, g[6], g[7]);
+#pragma unroll
+                            for (int c = 0; c < 4; ++c) cm[c] = fminf(g[2 * c], g[2 * c + 1]);
+                            const float lim = fminf(top.kth(), th);
+                            const float tmin = fminf(fminf(cm[0], cm[1]), fminf(cm[2], cm[3]));
+                            if (__any_sync(0xffffffffu, tmin < lim)) {
+                                if (a.stats) {
+                                    uint32_t in = 0;
+#pragma unroll
+                                    for (int t = 0; t < 8; t++) in += g[t] < lim ? 1u : 0u;
+                                    const uint32_t all = __reduce_add_sync(0xffffffffu, in);
+                                    if (lane == 0) {
+                                        atomicAdd(a.stats + TS_TOPK_ENTER, 1ull);
+                                        atomicAdd(a.stats + TS_TOPK_BULK, 1ull);
+                                        atomicAdd(a.stats + TS_TOPK_ENTRANTS, (unsigned long long)all);
+                                    }
+                                }
+                                sort8(g);
+                                top.merge_few(g);
+                            }
+                            if (top.kth() < kth0) th = fminf(th, bnd.theta_f32(top.kth()));
+                        }
+                    } else if constexpr (TOPK == 32 && PASS == 1) {
+                        // The same for a top-32: groups of 4 on an item's
+                        // first tile (32 minima per lane), of 16 after it; one
+                        // chunk in flight (a top-32 leaves no registers for
+                        // two).
+                        const float kth0 = top.kth();
+                        if (it == 0) {
+#pragma unroll 1
+                            for (int c = 0; c < 4; ++c) {
+                                float q[8];
+                                tmem_ld32(tbase + 32 * c, va);
+                                tmem_ld_wait(va);
+                                eighth_mins(va, col0 + 32 * c, row, a, q);
+                                cm[c] = fminf(fminf(fminf(q[0], q[1]), fminf(q[2], q[3])),
+                                              fminf(fminf(q[4], q[5]), fminf(q[6], q[7])));
+                                if (__any_sync(0xffffffffu, cm[c] < fminf(top.kth(), th))) {
+                                    sort8(q);
+                                    top.merge_few(q);
+                                }
+                            }
+                            th = fminf(th, bnd.theta_f32(top.kth()));
+                        } else {
+                            float g[8];
+#pragma unroll
+                            for (int c = 0; c < 4; ++c) {
+                                tmem_ld32(tbase + 32 * c, va);
+                                tmem_ld_wait(va);
+                                half_mins(va, col0 + 32 * c, row, a, g[2 * c], g[2 * c + 1]);
+                                cm[c] = fminf(g[2 * c], g[2 * c + 1]);
+                            }
+                            const float tmin = fminf(fminf(cm[0], cm[1]), fminf(cm[2], cm[3]));
+                            if (__any_sync(0xffffffffu, tmin < fminf(top.kth(), th))) {
+                                sort8(g);
+                                top.merge_few(g);
+                            }
+                            if (top.kth() < kth0) th = fminf(th, bnd.theta_f32(top.kth()));
                         }
                     } else if constexpr (TOPK <= 16) {
                         const float kth0 = top.kth();
