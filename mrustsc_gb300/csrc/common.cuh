@@ -104,6 +104,36 @@ __device__ __forceinline__ float dist2_f32_v4(const float4* __restrict__ a, cons
     return __fadd_rn(__fadd_rn(s0, s1), __fadd_rn(s2, s3));
 }
 
+// 32 bytes from global memory in one load (32-byte aligned; read-only path).
+__device__ __forceinline__ void ldg_v8(const float* p, float (&r)[8]) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]), "=f"(r[6]), "=f"(r[7])
+        : "l"(p));
+}
+
+// dist2_f32 on rows padded with zeros to d8 32-byte words (32-byte aligned):
+// the same accumulators in the same order (the padding adds exact zeros), so
+// the same value; a lane's loads then use whole 32-byte sectors.
+__device__ __forceinline__ float dist2_f32_v8(const float* __restrict__ a, const float* __restrict__ b, int d8) {
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll 1
+    for (int t = 0; t < d8; ++t) {
+        float x[8], y[8];
+        ldg_v8(a + 8 * t, x);
+        ldg_v8(b + 8 * t, y);
+#pragma unroll
+        for (int h = 0; h < 8; h += 4) {
+            const float d0 = __fsub_rn(x[h], y[h]), d1 = __fsub_rn(x[h + 1], y[h + 1]),
+                        d2 = __fsub_rn(x[h + 2], y[h + 2]), d3 = __fsub_rn(x[h + 3], y[h + 3]);
+            s0 = __fmaf_rn(d0, d0, s0);
+            s1 = __fmaf_rn(d1, d1, s1);
+            s2 = __fmaf_rn(d2, d2, s2);
+            s3 = __fmaf_rn(d3, d3, s3);
+        }
+    }
+    return __fadd_rn(__fadd_rn(s0, s1), __fadd_rn(s2, s3));
+}
+
 // Relative error bound of dist2_f32 with a 1.5x safety factor.
 __host__ __device__ __forceinline__ float dist2_f32_gamma(int d) {
     return (float)(1.5 * ((double)((d + 3) / 4) + 5.0) * kUnit32);

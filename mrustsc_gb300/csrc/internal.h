@@ -340,10 +340,11 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
 size_t work_order_scratch(int items);
 cudaError_t sort_by_work(scrust_context* ctx, const uint32_t* counts, int items, char* scratch, uint32_t* order);
 // order.cu: rows of x in list order, xs[s] = x[perm[s]] (zeros where perm
-// holds 0xffffffff), `stride` floats apart with zeros after the d-th.
+// holds 0xffffffff), `stride` floats apart with zeros after the d-th.  The
+// rerank reads such rows in 32-byte words: a multiple of 8 floats.
 cudaError_t launch_gather_rows(const float* x, const uint32_t* perm, int64_t n, int d, int stride, float* xs,
                                cudaStream_t s);
-inline int padded_row_floats(int d) { return (d + 3) / 4 * 4; }
+inline int padded_row_floats(int d) { return (d + 7) / 8 * 8; }
 
 // conn.cu
 // Per-row sigma and rho.  `report_sigmas`: also compute the global mean that

@@ -32,7 +32,8 @@
 //
 // The kernel is compiled once per (top-k size, pass kind).  PASS 1 only
 // tightens thresholds with a register top-k, PASS 2 only collects ids below
-// fixed thresholds, PASS 3 keeps each row's nearest column (no lists), and
+// fixed thresholds, PASS 3 keeps each row's nearest column to within 32 ulp
+// of the smallest value (no lists; an ordering needs no more), and
 // PASS 0 takes the kind from its arguments.  A specialised pass carries none
 // of the others' code, which matters because the epilogue is held to 96
 // registers (18 warps on an SM) and its ALU pipe is the bottleneck.
@@ -93,7 +94,9 @@ struct TensorArgs {
                                 // (float_key; 0xffffffff = none), shared across column segments; or null
     const uint32_t* row_map;    // per query row its input row, 0xffffffff for padding; null: all rows real
     // k = 1 without lists: per (row, part) the smallest MMA value and its
-    // column, packed as float_key << 32 | column; null otherwise.
+    // column, packed as float_key << 32 | column; null otherwise.  (The
+    // nearest-column pass carries the column in the value's low five bits, so
+    // its choice is exact up to values within 32 ulp of each other.)
     unsigned long long* argmin_out;
     int final_cap;              // lists longer than this are pruned once more when an item ends
     int resume;                 // lists and thresholds continue from an earlier pass
@@ -331,6 +334,28 @@ __device__ __forceinline__ void quarter_mins(uint32_t (&v)[32], int64_t colbase,
         const int b = 8 * q;
         g[q] = min3f(min3f(f_of(v[b]), f_of(v[b + 1]), f_of(v[b + 2])),
                      min3f(f_of(v[b + 3]), f_of(v[b + 4]), f_of(v[b + 5])), fminf(f_of(v[b + 6]), f_of(v[b + 7])));
+    }
+}
+
+// Nearest-column pass: every value of the chunk carries its column in the low
+// five bits of its f32 pattern (an error of under 32 ulp, which an
+// approximately nearest column tolerates), so one minimum tree yields both
+// the smallest value and its column, with no vote or branch per chunk.
+// Columns past the reference rows (and the row itself) get a large finite
+// value.
+__device__ __forceinline__ void argmin_chunk(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a,
+                                             float& best_v, uint32_t& best_c) {
+    const uint32_t valid = chunk_valid(colbase, a.nr, a.self != 0, row + a.self_offset);
+    if (__any_sync(0xffffffffu, valid != 0xffffffffu)) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) v[j] = ((valid >> j) & 1u) ? v[j] : 0x7f7fffe0u;
+    }
+#pragma unroll
+    for (int j = 0; j < 32; j++) v[j] = (v[j] & ~31u) | (uint32_t)j;
+    const float m = min32(v);
+    if (m < best_v) {
+        best_v = m;
+        best_c = (uint32_t)colbase + (__float_as_uint(m) & 31u);
     }
 }
 
@@ -785,6 +810,20 @@ __global__ void __launch_bounds__(THREADS, 1)
                                 }
                             }
                         }
+                    } else if constexpr (PASS == 3) {
+                        uint32_t vb[32];
+                        tmem_ld32(tbase, va);
+                        tmem_ld_wait(va);
+                        tmem_ld32(tbase + 32, vb);
+                        argmin_chunk(va, col0, row, a, top.v[0], best);
+                        tmem_ld_wait(vb);
+                        tmem_ld32(tbase + 64, va);
+                        argmin_chunk(vb, col0 + 32, row, a, top.v[0], best);
+                        tmem_ld_wait(va);
+                        tmem_ld32(tbase + 96, vb);
+                        argmin_chunk(va, col0 + 64, row, a, top.v[0], best);
+                        tmem_ld_wait(vb);
+                        argmin_chunk(vb, col0 + 96, row, a, top.v[0], best);
                     } else if constexpr (TOPK == 16 && PASS == 1) {
                         // Threshold pass: each group of columns offers only
                         // its minimum.  The top-K then holds values of

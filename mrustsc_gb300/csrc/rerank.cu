@@ -43,7 +43,7 @@ struct RerankArgs {
     const float* xr_list;  // reference rows indexed by list entry (xs for a self solve)
     int ids_only;          // the lists hold ids only (collected below their thresholds): keep every entry
     int xs_stride;         // floats per row of xs and xr_list
-    int xs_v4;             // rows padded with zeros to a multiple of 4 floats, 16-byte aligned
+    int xs_v8;             // rows padded with zeros to a multiple of 8 floats, 32-byte aligned
     const uint32_t* row_lo;  // per input row: first row of its solve (a batch of solves), or null
     const uint32_t* row_hi;  // per input row: end of its solve
     const float* theta;    // per list: its threshold when the candidate pass ended, or null
@@ -297,9 +297,7 @@ __device__ int sorted_row(const RerankArgs& a, int64_t slot, unsigned long long*
                 const int pos = m + __popc(ballot & lanemask_lt());
                 if (pos < CAP) {
                     const float* xr = a.xr_list + (int64_t)id * a.xs_stride;
-                    const float r = a.xs_v4 ? dist2_f32_v4(reinterpret_cast<const float4*>(xq),
-                                                           reinterpret_cast<const float4*>(xr), a.xs_stride / 4)
-                                            : dist2_f32(xq, xr, a.d);
+                    const float r = a.xs_v8 ? dist2_f32_v8(xq, xr, a.xs_stride / 8) : dist2_f32(xq, xr, a.d);
                     keys[pos] = ((unsigned long long)float_key(r) << 32) | (uint32_t)input_row(a, id);
                 }
             }
@@ -451,9 +449,7 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
         }
         if (keep) {
             const float* xr = a.xr_list + (int64_t)id * a.xs_stride;
-            const float d2 = a.xs_v4 ? dist2_f32_v4(reinterpret_cast<const float4*>(xq),
-                                                    reinterpret_cast<const float4*>(xr), a.xs_stride / 4)
-                                     : dist2_f32(xq, xr, a.d);
+            const float d2 = a.xs_v8 ? dist2_f32_v8(xq, xr, a.xs_stride / 8) : dist2_f32(xq, xr, a.d);
             key[r] = ((unsigned long long)float_key(d2) << 32) | (uint32_t)input_row(a, id);
         }
         m += __popc(__ballot_sync(0xffffffffu, keep));
@@ -746,7 +742,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.xr_list = xr_list ? xr_list : xs;
     a.xs_stride = xs_stride > 0 ? xs_stride : plan.d;
     a.ids_only = ids_only ? 1 : 0;
-    a.xs_v4 = !xr_list && xs && a.xs_stride % 4 == 0 && ((uintptr_t)xs & 15) == 0;
+    a.xs_v8 = !xr_list && xs && a.xs_stride % 8 == 0 && ((uintptr_t)xs & 31) == 0;
     a.theta = theta;
     a.row_lo = row_lo;
     a.row_hi = row_hi;
