@@ -356,99 +356,146 @@ __device__ void warp_sort_bucket(unsigned long long* v, uint32_t len) {
 }
 
 // The fuzzy union of row i, one warp per row, for graphs with distinct ids
-// per row and k <= 32: the row's directed entries (sorted by column, one per
-// lane) and its bucket of incoming edges (sources unique, any order).  Every
-// entry's place in the merged row is its rank among the union's distinct
-// columns: for a bucket of up to 128 edges (four per lane) the ranks come
-// from shuffles, a larger bucket is sorted in place and placed by binary
-// search.  This pass writes each directed entry's place to fpos and its
-// merged value (w + r) - (w * r) over dw, each incoming edge's place to bpos
-// (all ones when it merged into a directed entry), and the row's length;
-// the writing pass then only moves entries.
-constexpr int kBucketPerLane = 4;
-
+// per row, k <= 32 and n < 2^31.  The row's directed entries (nf, sorted by
+// column) and its bucket of incoming edges (nb, sources unique, any order)
+// are keyed column << 1 | direction and sorted together across the warp
+// (32 or 64 positions, position lane + 32 r in register r), so an edge
+// present in both directions becomes a directed entry followed by its
+// incoming twin: the pair merges into (w + r) - (w * r), every other entry
+// keeps its weight.  The merged row goes, compacted, to the row's scratch run
+// at i * k + start[i] (room for k + nb entries) and its length to rowcnt[i];
+// merge_place_kernel then copies the runs into the CSR.  Rows with more than
+// 64 entries in all sort their bucket in place and place every entry by
+// binary search.
 __device__ __forceinline__ uint32_t mask_below(int c) { return c >= 32 ? 0xffffffffu : ((1u << c) - 1u); }
 
-// Ranks for a bucket of at most 32 * Q incoming edges, Q per lane.
-template <int Q>
-__device__ __forceinline__ uint32_t rank_small_bucket(const unsigned long long* __restrict__ tval, uint32_t b0, int nb,
-                                                      int nf, uint32_t fcol, uint32_t* __restrict__ bpos,
-                                                      int* less_b, bool* dup_f, float* rv_f) {
+template <int P>
+__device__ __forceinline__ int union_sorted_row(const uint32_t* __restrict__ dcol, const float* __restrict__ dw,
+                                                const unsigned long long* __restrict__ tval, int64_t i, int k,
+                                                int nf, uint32_t b0, int nb, uint32_t* __restrict__ scol,
+                                                float* __restrict__ sval) {
+    constexpr int R = P / 32;
     const int lane = threadIdx.x & 31;
-    uint32_t bsrc[Q];
-    float bw[Q];
-    int rank[Q], less_f[Q];
-    bool dup_b[Q];
+    uint32_t key[R];
+    float w[R];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        const int j = q * 32 + lane;
-        const unsigned long long e = j < nb ? tval[b0 + j] : ~0ull;
-        bsrc[q] = (uint32_t)(e >> 32);
-        bw[q] = __uint_as_float((uint32_t)e);
-        rank[q] = 0;
-        less_f[q] = 0;
-        dup_b[q] = false;
+    for (int r = 0; r < R; ++r) {
+        const int p = lane + 32 * r;
+        key[r] = 0xffffffffu;
+        w[r] = 0.f;
+        if (p < nf) {
+            key[r] = dcol[i * k + p] << 1;
+            w[r] = dw[i * k + p];
+        } else if (p < nf + nb) {
+            const unsigned long long e = tval[b0 + (p - nf)];
+            key[r] = ((uint32_t)(e >> 32) << 1) | 1u;
+            w[r] = __uint_as_float((uint32_t)e);
+        }
     }
+    // Ascending bitonic sort over the P positions (keys of valid entries are
+    // unique; the padding keys are equal and carry nothing).
 #pragma unroll
-    for (int q2 = 0; q2 < Q; ++q2) {
-        const int lim = min(32, nb - q2 * 32);
-        for (int t = 0; t < lim; ++t) {
-            const uint32_t s_t = __shfl_sync(0xffffffffu, bsrc[q2], t);
-            const float w_t = __shfl_sync(0xffffffffu, bw[q2], t);
+    for (int size = 2; size <= P; size <<= 1) {
 #pragma unroll
-            for (int q = 0; q < Q; ++q) rank[q] += s_t < bsrc[q];
-            *less_b += s_t < fcol;
-            if (s_t == fcol) {
-                *dup_f = true;
-                *rv_f = w_t;
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride == 32) {
+                if (key[R - 1] < key[0]) {
+                    const uint32_t tk = key[0];
+                    const float tw = w[0];
+                    key[0] = key[R - 1];
+                    w[0] = w[R - 1];
+                    key[R - 1] = tk;
+                    w[R - 1] = tw;
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int p = lane + 32 * r;
+                    const uint32_t ok = __shfl_xor_sync(0xffffffffu, key[r], stride);
+                    const float ow = __shfl_xor_sync(0xffffffffu, w[r], stride);
+                    const bool take_min = ((p & stride) == 0) == ((p & size) == 0);
+                    if (ok != key[r] && (ok < key[r]) == take_min) {
+                        key[r] = ok;
+                        w[r] = ow;
+                    }
+                }
             }
         }
     }
-    for (int t = 0; t < nf; ++t) {
-        const uint32_t c_t = __shfl_sync(0xffffffffu, fcol, t);
+    // Neighbouring positions: p - 1 and p + 1.
+    uint32_t prev[R], next[R];
+    float nextw[R];
 #pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            less_f[q] += c_t < bsrc[q];
-            dup_b[q] |= c_t == bsrc[q];
+    for (int r = 0; r < R; ++r) {
+        const uint32_t up = __shfl_up_sync(0xffffffffu, key[r], 1);
+        const uint32_t dn = __shfl_down_sync(0xffffffffu, key[r], 1);
+        const float dnw = __shfl_down_sync(0xffffffffu, w[r], 1);
+        const uint32_t wrap_up = r > 0 ? __shfl_sync(0xffffffffu, key[r > 0 ? r - 1 : 0], 31) : 0xffffffffu;
+        const uint32_t wrap_dn = r + 1 < R ? __shfl_sync(0xffffffffu, key[r + 1 < R ? r + 1 : r], 0) : 0xffffffffu;
+        const float wrap_dnw = r + 1 < R ? __shfl_sync(0xffffffffu, w[r + 1 < R ? r + 1 : r], 0) : 0.f;
+        prev[r] = lane == 0 ? wrap_up : up;
+        next[r] = lane == 31 ? wrap_dn : dn;
+        nextw[r] = lane == 31 ? wrap_dnw : dnw;
+    }
+    bool keep[R];
+    uint32_t ball[R];
+    int total = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        // An incoming edge right after its directed twin merged into it.
+        keep[r] = key[r] != 0xffffffffu && !((key[r] & 1u) && prev[r] == (key[r] ^ 1u));
+        ball[r] = __ballot_sync(0xffffffffu, keep[r]);
+        total += __popc(ball[r]);
+    }
+    int before = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (keep[r]) {
+            const int pos = before + __popc(ball[r] & lanemask_lt());
+            float v = w[r];
+            if (!(key[r] & 1u) && next[r] == (key[r] | 1u)) {
+                const float rv = nextw[r];
+                v = __fsub_rn(__fadd_rn(w[r], rv), __fmul_rn(w[r], rv));
+            }
+            scol[pos] = key[r] >> 1;
+            sval[pos] = v;
         }
+        before += __popc(ball[r]);
     }
-    const uint32_t dupmask = __ballot_sync(0xffffffffu, lane < nf && *dup_f);
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        const int j = q * 32 + lane;
-        if (j < nb)
-            bpos[b0 + j] = dup_b[q] ? 0xffffffffu
-                                    : (uint32_t)(rank[q] + less_f[q]) - (uint32_t)__popc(dupmask & mask_below(less_f[q]));
-    }
-    return dupmask;
+    return total;
 }
 
-__global__ void __launch_bounds__(256) merge_rank_kernel(const uint32_t* __restrict__ dcol, float* __restrict__ dw,
-                                                         const uint32_t* __restrict__ dcnt,
-                                                         unsigned long long* __restrict__ tval,
-                                                         const uint32_t* __restrict__ tstart, int64_t n, int k,
-                                                         uint32_t* __restrict__ fpos, uint32_t* __restrict__ bpos,
-                                                         uint32_t* __restrict__ rowcnt) {
+__global__ void __launch_bounds__(256) merge_union_kernel(const uint32_t* __restrict__ dcol,
+                                                          const float* __restrict__ dw,
+                                                          const uint32_t* __restrict__ dcnt,
+                                                          unsigned long long* __restrict__ tval,
+                                                          const uint32_t* __restrict__ tstart, int64_t n, int k,
+                                                          uint32_t* __restrict__ scol, float* __restrict__ sval,
+                                                          uint32_t* __restrict__ rowcnt) {
     const int lane = threadIdx.x & 31;
     const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= n) return;
     const int nf = (int)dcnt[i];
     const uint32_t b0 = tstart[i];
     const int nb = (int)(tstart[i + 1] - b0);
-    const uint32_t fcol = lane < nf ? dcol[i * k + lane] : 0xffffffffu;
-    const float fw = lane < nf ? dw[i * k + lane] : 0.f;
-    int less_b = 0;      // incoming edges with a source below this lane's column
-    bool dup_f = false;  // this lane's column has an incoming edge
-    float rv_f = 0.f;
-    uint32_t dupmask;
-    if (nb <= 32) {
-        dupmask = rank_small_bucket<1>(tval, b0, nb, nf, fcol, bpos, &less_b, &dup_f, &rv_f);
-    } else if (nb <= 64) {
-        dupmask = rank_small_bucket<2>(tval, b0, nb, nf, fcol, bpos, &less_b, &dup_f, &rv_f);
-    } else if (nb <= 32 * kBucketPerLane) {
-        dupmask = rank_small_bucket<kBucketPerLane>(tval, b0, nb, nf, fcol, bpos, &less_b, &dup_f, &rv_f);
+    const int64_t run = i * k + b0;
+    uint32_t* rc = scol + run;
+    float* rv = sval + run;
+    int total;
+    if (nf + nb <= 32) {
+        total = union_sorted_row<32>(dcol, dw, tval, i, k, nf, b0, nb, rc, rv);
+    } else if (nf + nb <= 64) {
+        total = union_sorted_row<64>(dcol, dw, tval, i, k, nf, b0, nb, rc, rv);
     } else {
+        // Many incoming edges: the bucket sorted in place, every directed
+        // entry placed by binary search among the sources and every incoming
+        // edge by counting the directed columns below it.
         warp_sort_bucket(tval + b0, (uint32_t)nb);
+        const uint32_t fcol = lane < nf ? dcol[i * k + lane] : 0xffffffffu;
+        const float fw = lane < nf ? dw[i * k + lane] : 0.f;
+        int less_b = 0;
+        bool dup_f = false;
+        float rv_f = 0.f;
         if (lane < nf) {  // lower bound of this lane's column among the sorted sources
             int lo = 0, hi = nb;
             while (lo < hi) {
@@ -467,10 +514,11 @@ __global__ void __launch_bounds__(256) merge_rank_kernel(const uint32_t* __restr
                 }
             }
         }
-        dupmask = __ballot_sync(0xffffffffu, lane < nf && dup_f);
+        const uint32_t dupmask = __ballot_sync(0xffffffffu, lane < nf && dup_f);
         for (int base = 0; base < nb; base += 32) {
             const int j = base + lane;
-            const uint32_t src = j < nb ? (uint32_t)(tval[b0 + j] >> 32) : 0xffffffffu;
+            const unsigned long long e = j < nb ? tval[b0 + j] : ~0ull;
+            const uint32_t src = (uint32_t)(e >> 32);
             int lf = 0;
             bool db = false;
             for (int t = 0; t < nf; ++t) {
@@ -478,45 +526,37 @@ __global__ void __launch_bounds__(256) merge_rank_kernel(const uint32_t* __restr
                 lf += c_t < src;
                 db |= c_t == src;
             }
-            if (j < nb) bpos[b0 + j] = db ? 0xffffffffu : (uint32_t)(j + lf) - (uint32_t)__popc(dupmask & mask_below(lf));
+            if (j < nb && !db) {
+                const uint32_t q = (uint32_t)(j + lf) - (uint32_t)__popc(dupmask & mask_below(lf));
+                rc[q] = src;
+                rv[q] = __uint_as_float((uint32_t)e);
+            }
         }
+        if (lane < nf) {
+            const uint32_t q = (uint32_t)(lane + less_b) - (uint32_t)__popc(dupmask & lanemask_lt());
+            const float r2 = dup_f ? rv_f : 0.f;
+            rc[q] = fcol;
+            rv[q] = __fsub_rn(__fadd_rn(fw, r2), __fmul_rn(fw, r2));
+        }
+        total = nf + nb - __popc(dupmask);
     }
-    if (lane < nf) {
-        fpos[i * k + lane] = (uint32_t)(lane + less_b) - (uint32_t)__popc(dupmask & lanemask_lt());
-        const float wv = fw, rv = dup_f ? rv_f : 0.f;
-        dw[i * k + lane] = __fsub_rn(__fadd_rn(wv, rv), __fmul_rn(wv, rv));
-    }
-    if (lane == 0) rowcnt[i] = (uint32_t)(nf + nb) - (uint32_t)__popc(dupmask);
+    if (lane == 0) rowcnt[i] = (uint32_t)total;
 }
 
-// The writing pass: every entry to its place in the CSR (an incoming edge
-// alone in its column keeps its weight: (0 + r) - (0 * r) = r).
-__global__ void __launch_bounds__(256) merge_place_kernel(const uint32_t* __restrict__ dcol,
-                                                          const float* __restrict__ dw,
-                                                          const uint32_t* __restrict__ dcnt,
-                                                          const unsigned long long* __restrict__ tval,
+// The writing pass: every merged run into its place in the CSR.
+__global__ void __launch_bounds__(256) merge_place_kernel(const uint32_t* __restrict__ scol,
+                                                          const float* __restrict__ sval,
                                                           const uint32_t* __restrict__ tstart, int64_t n, int k,
-                                                          const uint32_t* __restrict__ fpos,
-                                                          const uint32_t* __restrict__ bpos,
                                                           const uint32_t* __restrict__ indptr,
                                                           uint32_t* __restrict__ out_cols, float* __restrict__ out_vals) {
     const int lane = threadIdx.x & 31;
     const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= n) return;
-    const int nf = (int)dcnt[i];
-    const uint32_t b0 = tstart[i], b1 = tstart[i + 1];
-    const uint32_t base = indptr[i];
-    if (lane < nf) {
-        const uint32_t p = base + fpos[i * k + lane];
-        out_cols[p] = dcol[i * k + lane];
-        out_vals[p] = dw[i * k + lane];
-    }
-    for (uint32_t j = b0 + lane; j < b1; j += 32) {
-        const uint32_t q = bpos[j];
-        if (q == 0xffffffffu) continue;
-        const unsigned long long e = tval[j];
-        out_cols[base + q] = (uint32_t)(e >> 32);
-        out_vals[base + q] = __uint_as_float((uint32_t)e);
+    const int64_t run = i * k + tstart[i];
+    const uint32_t base = indptr[i], len = indptr[i + 1] - base;
+    for (uint32_t j = lane; j < len; j += 32) {
+        out_cols[base + j] = scol[run + j];
+        out_vals[base + j] = sval[run + j];
     }
 }
 
@@ -886,11 +926,13 @@ int32_t run_connectivities_distinct(scrust_context* ctx, const uint32_t* idx, co
     char* a = (char*)ws_get(ctx, SLOT_CONN_A, sizeof(float) * 2 * (size_t)n + sizeof(uint32_t) * 3 * (size_t)(n + 1) + 256, &e);
     uint32_t* dcol = (uint32_t*)ws_get(ctx, SLOT_CONN_B, sizeof(uint32_t) * (size_t)E, &e);
     float* dw = (float*)ws_get(ctx, SLOT_CONN_C, sizeof(float) * (size_t)E, &e);
-    uint32_t* erank = (uint32_t*)ws_get(ctx, SLOT_CONN_D, sizeof(uint32_t) * (size_t)E, &e);  // then bpos
+    uint32_t* erank = (uint32_t*)ws_get(ctx, SLOT_CONN_D, sizeof(uint32_t) * (size_t)E, &e);
     unsigned long long* tval = (unsigned long long*)ws_get(ctx, SLOT_CONN_E, sizeof(unsigned long long) * (size_t)E, &e);
-    uint32_t* fpos = (uint32_t*)ws_get(ctx, SLOT_CONN_F, sizeof(uint32_t) * (size_t)E, &e);
+    // Merged runs: row i's at i * k + start[i], k + in-degree entries each.
+    uint32_t* scol = (uint32_t*)ws_get(ctx, SLOT_CONN_H, 2 * sizeof(uint32_t) * 2 * (size_t)E, &e);
+    float* sval = scol ? (float*)(scol + 2 * (size_t)E) : nullptr;
     uint32_t* scan_scratch = (uint32_t*)ws_get(ctx, SLOT_SCAN, sizeof(uint32_t) * scan_elems, &e);
-    if (!a || !dcol || !dw || !erank || !tval || !fpos || !scan_scratch)
+    if (!a || !dcol || !dw || !erank || !tval || !scol || !scan_scratch)
         return cuda_fail(st, e, "connectivities: workspace");
     float* sig = (float*)a;
     float* rho = sig + n;
@@ -911,13 +953,11 @@ int32_t run_connectivities_distinct(scrust_context* ctx, const uint32_t* idx, co
         return cuda_fail(st, e, "in-degree scan");
     bucket_scatter_kernel<<<(unsigned)((E + 255) / 256), 256, 0, s>>>(dcol, dw, dcnt, erank, indeg, n, k, tval);
     const unsigned merge_blocks = (unsigned)((n * 32 + 255) / 256);
-    uint32_t* bpos = erank;  // the ranks are read by the scatter only
-    merge_rank_kernel<<<merge_blocks, 256, 0, s>>>(dcol, dw, dcnt, tval, indeg, n, k, fpos, bpos, rowcnt);
+    merge_union_kernel<<<merge_blocks, 256, 0, s>>>(dcol, dw, dcnt, tval, indeg, n, k, scol, sval, rowcnt);
     if ((e = cudaMemsetAsync(rowcnt + n, 0, sizeof(uint32_t), s)) != cudaSuccess) return cuda_fail(st, e, "memset");
     if ((e = device_exclusive_scan(ctx, rowcnt, out->indptr, n + 1, scan_scratch, scan_elems)) != cudaSuccess)
         return cuda_fail(st, e, "row scan");
-    merge_place_kernel<<<merge_blocks, 256, 0, s>>>(dcol, dw, dcnt, tval, indeg, n, k, fpos, bpos, out->indptr,
-                                                    out->indices, out->values);
+    merge_place_kernel<<<merge_blocks, 256, 0, s>>>(scol, sval, indeg, n, k, out->indptr, out->indices, out->values);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "merge");
     ctx->launches += 4;
     return ok(st);
@@ -925,7 +965,8 @@ int32_t run_connectivities_distinct(scrust_context* ctx, const uint32_t* idx, co
 
 int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n, int k,
                            bool validate, CsrBuffers* out, scrust_status* st, bool distinct_rows) {
-    if (distinct_rows && !validate && k <= 32) return run_connectivities_distinct(ctx, idx, dist, n, k, out, st);
+    if (distinct_rows && !validate && k <= 32 && n < ((int64_t)1 << 31))
+        return run_connectivities_distinct(ctx, idx, dist, n, k, out, st);
     cudaError_t e = cudaSuccess;
     cudaStream_t s = ctx->stream;
     const int64_t E = n * (int64_t)k;

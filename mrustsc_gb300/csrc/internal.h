@@ -45,6 +45,7 @@ enum Slot : int {
     SLOT_CONN_E,
     SLOT_CONN_F,
     SLOT_CONN_G,
+    SLOT_CONN_H,        // merged rows of the fuzzy union before they are placed
     SLOT_SCAN,
     SLOT_MISC,
     SLOT_WORKQ,
