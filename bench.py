@@ -386,11 +386,12 @@ def run_ours(args):
         tiles = int(cnt[8])
         sms = torch.cuda.get_device_properties(local).multi_processor_count
         if ph_mean[4] > 0:
-            # The four launches of an ordered solve, with their own counters.
-            collect2_ms = cand_ms - float(ph_mean[4] + ph_mean[5] + ph_mean[6] + ph_mean[7])
-            pass_ms = [float(ph_mean[4]), float(ph_mean[6]), float(ph_mean[7]), collect2_ms]
-            names = ["threshold, priority tiles", "threshold, kept tiles", "collect, priority tiles",
-                     "collect, kept tiles"]
+            # The launches of an ordered solve (k <= 32), with their own
+            # counters: the threshold pass over the priority tiles, then one
+            # collect pass over the priority tiles and the tiles the tile
+            # balls keep.
+            pass_ms = [float(ph_mean[4]), float(ph_mean[7])]
+            names = ["threshold, priority tiles", "collect, priority and kept tiles"]
             sweep_passes = []
             for i, name in enumerate(names):
                 c = [int(cnt[16 * (i + 1) + j]) for j in range(16)]
@@ -437,8 +438,7 @@ def run_ours(args):
                           "rerank": float(ph_mean[2]), "connectivities": float(ph_mean[3]),
                           "candidates_first_pass": float(ph_mean[4]),
                           "candidates_tile_lists": float(ph_mean[5]),
-                          "candidates_second_pass": float(ph_mean[6]),
-                          "candidates_first_collect": float(ph_mean[7])},
+                          "candidates_collect": float(ph_mean[7])},
             "phases_gbs": phases_gbs, "phases_gbs_peak": f"{hbm} GB/s, {pk_kind} copy bandwidth",
             "graph_nnz": nnz, "gpu_launches": launches, "roofline": roof, "clocks": clk}
 

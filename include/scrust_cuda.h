@@ -441,8 +441,9 @@ SCRUST_API int32_t scrust_cuda_modularity(scrust_context* context, const uint32_
  * writes the last call's milliseconds (after a synchronise) in the order
  * prep, candidates, rerank, connectivities, then four parts of candidates in
  * an ordered tensor-form solve (its first sweep pass, the building of the
- * second pass's tile lists, the second pass, and the first collect pass when
- * k <= 32; 0 otherwise), and returns how many it wrote. */
+ * second tile lists, the second sweep pass when k > 32, and the collect pass
+ * over both tile lists when k <= 32; 0 where absent), and returns how many it
+ * wrote. */
 SCRUST_API void scrust_cuda_set_timing(scrust_context* context, int32_t enable);
 SCRUST_API int32_t scrust_cuda_phase_times(scrust_context* context, float* ms, int32_t max_phases);
 
@@ -456,8 +457,9 @@ SCRUST_API int32_t scrust_cuda_phase_times(scrust_context* context, float* ms, i
  * rounds, 15 entrants; 4, 10 and 11 are unused.  Words 0-15 hold every sweep
  * launch together; with max_words up to 80, words 16-31, 32-47 and 48-63 hold
  * the first, second and third sweep launch of each solve on their own and
- * 64-79 every later launch (an ordered solve with k <= 32 runs the two
- * threshold passes, then the two collect passes). */
+ * 64-79 every later launch (an ordered solve with k <= 32 runs a threshold
+ * pass over its priority tiles, then one collect pass over those and the tiles
+ * the tile balls keep). */
 SCRUST_API int32_t scrust_cuda_kernel_stats(scrust_context* context, int32_t enable, uint64_t* out,
                                             int32_t max_words);
 

@@ -375,16 +375,20 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
         plan.segments = lists.segments;
         mark(ctx, PH_PREP);
         if (order_rows) {
-            // Two passes: the priority tiles, then the tiles the tile balls
-            // cannot rule out.
+            // The priority tiles first; then the tiles the tile balls cannot
+            // rule out.
             TileLists first;
             first.tiles = order.prio;
             first.count = order.prio_cnt;
             first.stride = kPrioMax;
             first.order = order.prio_order;
-            // k <= 32: both passes only tighten the thresholds; two collect
-            // passes over the same tiles then append just the columns below
-            // the final thresholds.  Larger k: the passes keep lists.
+            // k <= 32: the first pass only tightens the thresholds, and one
+            // collect pass over both tile lists appends just the ids of the
+            // columns below them.  The thresholds after the priority tiles
+            // already bound every row (a threshold pass over the other tiles
+            // would lower them by a fraction of a percent of the candidates),
+            // so the other tiles are only collected.  Larger k: two passes
+            // that keep lists.
             const bool split = k <= 32;
             const int mode = split ? kPassThresholds : kPassFull;
             rerank_ids_only = split;
@@ -392,27 +396,30 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
                                               &first, false, order.theta, nullptr, sweep_stats(ctx), nullptr, mode)) !=
                 cudaSuccess)
                 return cuda_fail(st, e, "knn_candidates_tc");
+            ctx->launches += 1;
             mark(ctx, PH_PASS1);
             TileLists second;
             if ((rc = build_second_pass(ctx, A16, bf16, n, d, order, bA, bdelta, &second, st))) return rc;
             mark(ctx, PH_LISTS);
-            if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                              &second, true, order.theta, nullptr, sweep_stats(ctx), nullptr, mode)) !=
-                cudaSuccess)
-                return cuda_fail(st, e, "knn_candidates_tc");
-            mark(ctx, PH_PASS2);
-            ctx->launches += 2;
             if (split) {
+                mark(ctx, PH_PASS2);
+                TileLists both = first;
+                both.tiles2 = second.tiles;
+                both.count2 = second.count;
+                both.stride2 = second.stride;
                 if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
-                                                  &first, false, order.theta, nullptr, sweep_stats(ctx), nullptr,
+                                                  &both, false, order.theta, nullptr, sweep_stats(ctx), nullptr,
                                                   kPassCollect)) != cudaSuccess)
                     return cuda_fail(st, e, "knn_candidates_tc");
                 mark(ctx, PH_COLLECT1);
+                ctx->launches += 1;
+            } else {
                 if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
                                                   &second, true, order.theta, nullptr, sweep_stats(ctx), nullptr,
-                                                  kPassCollect)) != cudaSuccess)
+                                                  mode)) != cudaSuccess)
                     return cuda_fail(st, e, "knn_candidates_tc");
-                ctx->launches += 2;
+                mark(ctx, PH_PASS2);
+                ctx->launches += 1;
             }
         } else {
             // Every list keeps its threshold, so the rerank needs no selection.

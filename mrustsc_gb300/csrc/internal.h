@@ -285,6 +285,11 @@ struct TileLists {
     const uint32_t* count = nullptr;   // per row block
     int stride = 0;
     const uint32_t* order = nullptr;   // row blocks by decreasing count, or null
+    // A second explicit list per row block, visited after the first
+    // (`stride2` entries apart, `count2` per row block), or null.
+    const uint32_t* tiles2 = nullptr;
+    const uint32_t* count2 = nullptr;
+    int stride2 = 0;
     // Without explicit tiles: per row block the column tile range [x, y) it
     // sweeps (a batch of independent solves laid out block-diagonally), or null.
     const uint2* range = nullptr;

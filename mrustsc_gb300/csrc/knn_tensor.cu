@@ -88,6 +88,9 @@ struct TensorArgs {
     const uint32_t* tl_off;     // per-item offsets into tl, or null: item * tl_stride
     const uint32_t* tl_cnt;
     int tl_stride;
+    const uint32_t* tl2;        // a second explicit list per item, visited after the first, or null
+    const uint32_t* tl2_cnt;
+    int tl2_stride;
     const uint32_t* item_order; // items by decreasing work, dealt out in a snake, or null: round robin
     const uint2* item_range;    // per item its column tiles [x, y) (one column segment), or null
     uint32_t* row_theta;        // per query row the smallest threshold any of its lists reached
@@ -150,17 +153,24 @@ __device__ __forceinline__ int sweep_tile(int i, int home, int ct0, int ct1) {
 // the epilogue all derive the same count and sequence from it.
 struct TileOrder {
     const uint32_t* list;
-    int count, home, ct0, ct1;
+    const uint32_t* list2;
+    int count, count1, home, ct0, ct1;
 
     __device__ __forceinline__ TileOrder(const TensorArgs& a, int w, int qt, int ct0_, int ct1_)
-        : list(nullptr), count(ct1_ - ct0_), home(qt * ROWS / TBN), ct0(ct0_), ct1(ct1_) {
+        : list(nullptr), list2(nullptr), count(ct1_ - ct0_), count1(0), home(qt * ROWS / TBN), ct0(ct0_),
+          ct1(ct1_) {
         if (a.tl) {
             list = a.tl + (a.tl_off ? (int64_t)a.tl_off[w] : (int64_t)w * a.tl_stride);
-            count = (int)min(a.tl_cnt[w], (uint32_t)(ct1_ - ct0_));
+            count = count1 = (int)min(a.tl_cnt[w], (uint32_t)(ct1_ - ct0_));
+            if (a.tl2) {
+                list2 = a.tl2 + (int64_t)w * a.tl2_stride;
+                count += (int)min(a.tl2_cnt[w], (uint32_t)(ct1_ - ct0_ - count1));
+            }
         }
     }
     __device__ __forceinline__ int next(int it) const {
-        return list ? (int)list[it] : sweep_tile(it, home, ct0, ct1);
+        if (!list) return sweep_tile(it, home, ct0, ct1);
+        return it < count1 ? (int)list[it] : (int)list2[it - count1];
     }
 };
 
@@ -1288,6 +1298,9 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.tl_off = nullptr;
     a.tl_cnt = nullptr;
     a.tl_stride = 0;
+    a.tl2 = nullptr;
+    a.tl2_cnt = nullptr;
+    a.tl2_stride = 0;
     a.item_order = nullptr;
     a.item_range = tiles ? tiles->range : nullptr;
     a.row_map = tiles ? tiles->row_map : nullptr;
@@ -1302,6 +1315,12 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
         a.tl_cnt = tiles->count;
         a.tl_stride = tiles->stride;
         a.item_order = tiles->order;
+        if (tiles->tiles2) {
+            if (tiles->offset || !tiles->count2) return cudaErrorInvalidValue;
+            a.tl2 = tiles->tiles2;
+            a.tl2_cnt = tiles->count2;
+            a.tl2_stride = tiles->stride2;
+        }
     }
     a.resume = resume ? 1 : 0;
     a.theta_io = theta_io;
