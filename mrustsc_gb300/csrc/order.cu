@@ -133,72 +133,77 @@ __global__ void __launch_bounds__(128) anchor_top_kernel(const float* __restrict
 // anchor to its nearest unvisited neighbouring anchor, or, when all of them
 // have been visited, to the lowest unvisited anchor.  Consecutive cells are
 // then mostly neighbours, so a 256-row block rarely mixes far-apart cells.
-// One warp; the first kChainNb neighbours of every anchor (16-bit ids) and
-// the visited bitmap live in shared memory.  rank[a] is anchor a's place.
+// The block stages the first kChainNb neighbours of every anchor (16-bit
+// ids) in shared memory, many loads in flight; then one thread walks, since
+// every step depends on the one before: its neighbour ids and their visited
+// bits are independent shared loads issued together, and no warp vote stands
+// between steps.  rank[a] is anchor a's place.
 constexpr int kChainNb = 12;
-__global__ void __launch_bounds__(32) anchor_chain_kernel(const uint32_t* __restrict__ nb, int m,
-                                                          uint32_t* __restrict__ rank) {
+constexpr int kChainThreads = 1024;
+__global__ void __launch_bounds__(kChainThreads) anchor_chain_kernel(const uint32_t* __restrict__ nb, int m,
+                                                                     uint32_t* __restrict__ rank) {
     extern __shared__ uint32_t ch_smem[];
-    uint32_t* visited = ch_smem;                                      // (m + 31) / 32 words
-    uint16_t* nbs = reinterpret_cast<uint16_t*>(ch_smem + (m + 31) / 32);  // m * kChainNb
-    const int lane = threadIdx.x;
+    uint32_t* visited = ch_smem;                                           // (m + 31) / 32 words
+    uint16_t* nbs = reinterpret_cast<uint16_t*>(ch_smem + ((m + 31) / 32 + 1) / 2 * 2);  // m * kChainNb, 8-byte aligned
     const int words = (m + 31) / 32;
-    for (int i = lane; i < words; i += 32) visited[i] = 0u;
-    for (int i = lane; i < m * kChainNb; i += 32) {
-        const uint32_t c = nb[(int64_t)(i / kChainNb) * kAnchorNeighbours + i % kChainNb];
-        nbs[i] = c < (uint32_t)m ? (uint16_t)c : (uint16_t)0xffffu;
+    for (int i = threadIdx.x; i < words; i += blockDim.x) visited[i] = 0u;
+    for (int a = threadIdx.x; a < m; a += blockDim.x) {
+        const uint4* src = reinterpret_cast<const uint4*>(nb + (int64_t)a * kAnchorNeighbours);
+        uint32_t c[kChainNb];
+#pragma unroll
+        for (int q = 0; q < kChainNb / 4; ++q) {
+            const uint4 w = src[q];
+            c[4 * q] = w.x;
+            c[4 * q + 1] = w.y;
+            c[4 * q + 2] = w.z;
+            c[4 * q + 3] = w.w;
+        }
+#pragma unroll
+        for (int j = 0; j < kChainNb; ++j)
+            nbs[(int64_t)a * kChainNb + j] = c[j] < (uint32_t)m ? (uint16_t)c[j] : (uint16_t)0xffffu;
     }
-    __syncwarp();
-    int cur = 0, scan = 0;
-    if (lane == 0) {
-        visited[0] = 1u;
-        rank[0] = 0;
-    }
-    __syncwarp();
-    int pos = 1;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    visited[0] = 1u;
+    rank[0] = 0;
+    int cur = 0, scan = 0, pos = 1;
     for (; pos < m; ++pos) {
-        bool cand = false;
-        uint32_t c = 0xffffu;
-        if (lane < kChainNb) {
-            c = nbs[cur * kChainNb + lane];
-            cand = c < (uint32_t)m && !((visited[c >> 5] >> (c & 31)) & 1u);
+        // The 12 neighbour ids of cur as three 8-byte words.
+        const uint2* row = reinterpret_cast<const uint2*>(nbs + (size_t)cur * kChainNb);
+        uint32_t c[kChainNb];
+#pragma unroll
+        for (int q = 0; q < kChainNb / 4; ++q) {
+            const uint2 w = row[q];
+            c[4 * q] = w.x & 0xffffu;
+            c[4 * q + 1] = w.x >> 16;
+            c[4 * q + 2] = w.y & 0xffffu;
+            c[4 * q + 3] = w.y >> 16;
         }
-        const uint32_t bal = __ballot_sync(0xffffffffu, cand);
-        int next;
-        if (bal) {
-            next = (int)__shfl_sync(0xffffffffu, c, __ffs(bal) - 1);
-        } else {
-            next = -1;
-            while (next < 0) {  // some anchor is unvisited since pos < m
-                const int wd = scan + lane;
-                const uint32_t free = wd < words ? ~visited[wd] : 0u;
-                const uint32_t fb = __ballot_sync(0xffffffffu, free != 0u);
-                if (fb) {
-                    const int wl = __ffs(fb) - 1;
-                    const uint32_t fw = __shfl_sync(0xffffffffu, free, wl);
-                    next = (scan + wl) * 32 + __ffs(fw) - 1;
-                    scan += wl;
-                } else {
-                    scan += 32;
-                    if (scan >= words) break;
-                }
-            }
-            if (next < 0 || next >= m) break;  // cannot happen: the bitmap holds an unvisited anchor
+        uint32_t word[kChainNb];
+#pragma unroll
+        for (int j = 0; j < kChainNb; ++j) word[j] = c[j] < (uint32_t)m ? visited[c[j] >> 5] : ~0u;
+        int next = -1;
+#pragma unroll
+        for (int j = kChainNb - 1; j >= 0; --j)
+            if (c[j] < (uint32_t)m && !((word[j] >> (c[j] & 31u)) & 1u)) next = (int)c[j];
+        if (next < 0) {
+            // The lowest unvisited anchor (words below `scan` are full).
+            while (scan < words && visited[scan] == ~0u) ++scan;
+            if (scan >= words) break;  // cannot happen: an unvisited anchor exists while pos < m
+            const uint32_t free = ~visited[scan];
+            next = scan * 32 + __ffs(free) - 1;
+            if (next >= m) break;      // cannot happen: an unvisited anchor below m comes first
         }
-        if (lane == 0) {
-            visited[next >> 5] |= 1u << (next & 31);
-            rank[next] = (uint32_t)pos;
-        }
-        __syncwarp();
+        visited[next >> 5] |= 1u << (next & 31);
+        rank[next] = (uint32_t)pos;
         cur = next;
     }
     // Every anchor gets a rank whatever happened above.
-    if (lane == 0 && pos < m)
-        for (int a = 0; a < m; ++a)
-            if (!((visited[a >> 5] >> (a & 31)) & 1u)) {
-                visited[a >> 5] |= 1u << (a & 31);
-                rank[a] = (uint32_t)pos++;
-            }
+    for (int a = 0; a < m && pos < m; ++a)
+        if (!((visited[a >> 5] >> (a & 31)) & 1u)) {
+            visited[a >> 5] |= 1u << (a & 31);
+            rank[a] = (uint32_t)pos++;
+        }
 }
 
 // Anchor neighbourhoods renamed into walk order: row rank[a] of out holds
@@ -755,6 +760,30 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     // Anchors, and both operand sets in the input order.
     anchors_kernel<<<(unsigned)m, 64, 0, s>>>(x, d, n, m, src, anc);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchors");
+    // Anchor neighbourhoods and the walk that orders the cells.
+    {
+        float* adist = (float*)(base + o_adist);
+        const dim3 grid((unsigned)((m + 63) / 64), (unsigned)((m + 63) / 64));
+        anchor_dist_kernel<<<grid, 256, 0, s>>>(anc, (int)m, d, adist);
+        anchor_top_kernel<<<(unsigned)((m + 3) / 4), 128, 0, s>>>(adist, (int)m, anchor_nb);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor neighbours");
+        ctx->launches += 2;
+    }
+    // The walk (one block on one SM) runs on the copy stream beside the
+    // operands and the rows x anchors pass below, which leaves it that SM; the
+    // main stream waits for it before the cells are formed.
+    const size_t chain_smem = 4 * (size_t)(((m + 31) / 32 + 1) / 2 * 2) + 2 * (size_t)m * kChainNb;
+    if ((e = set_smem_limit(ctx, (const void*)anchor_chain_kernel, (int)chain_smem)) != cudaSuccess ||
+        (e = cudaEventRecord(ctx->copy_ev, s)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev, 0)) != cudaSuccess)
+        return cuda_fail(st, e, "ordering: anchor walk");
+    anchor_chain_kernel<<<1, kChainThreads, chain_smem, ctx->copy_stream>>>(anchor_nb, (int)m, rank);
+    relabel_neighbours_kernel<<<(unsigned)((m * kAnchorNeighbours + 255) / 256), 256, 0, ctx->copy_stream>>>(
+        anchor_nb, rank, (int)m, cell_nb);
+    if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaEventRecord(ctx->copy_ev, ctx->copy_stream)) != cudaSuccess)
+        return cuda_fail(st, e, "ordering: anchor walk");
+    ctx->launches += 2;
+
     void* A0 = base + o_A0;
     void* B0 = base + o_B0;
     float* bA0 = (float*)(base + o_bA0);
@@ -766,30 +795,6 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
                                     arb + m_pad, max_bits + 1, max_bits + 2, s)) != cudaSuccess)
         return cuda_fail(st, e, "ordering: operands");
     ctx->launches += 4;
-
-    // Anchor neighbourhoods and the walk that orders the cells.
-    {
-        float* adist = (float*)(base + o_adist);
-        const dim3 grid((unsigned)((m + 63) / 64), (unsigned)((m + 63) / 64));
-        anchor_dist_kernel<<<grid, 256, 0, s>>>(anc, (int)m, d, adist);
-        anchor_top_kernel<<<(unsigned)((m + 3) / 4), 128, 0, s>>>(adist, (int)m, anchor_nb);
-        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor neighbours");
-        ctx->launches += 2;
-    }
-    // The walk (one warp on one SM) runs on the copy stream beside the rows x
-    // anchors pass below, which leaves it that SM; the main stream waits for
-    // it before the cells are formed.
-    const size_t chain_smem = 4 * (size_t)((m + 31) / 32) + 2 * (size_t)m * kChainNb;
-    if ((e = set_smem_limit(ctx, (const void*)anchor_chain_kernel, (int)chain_smem)) != cudaSuccess ||
-        (e = cudaEventRecord(ctx->copy_ev, s)) != cudaSuccess ||
-        (e = cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev, 0)) != cudaSuccess)
-        return cuda_fail(st, e, "ordering: anchor walk");
-    anchor_chain_kernel<<<1, 32, chain_smem, ctx->copy_stream>>>(anchor_nb, (int)m, rank);
-    relabel_neighbours_kernel<<<(unsigned)((m * kAnchorNeighbours + 255) / 256), 256, 0, ctx->copy_stream>>>(
-        anchor_nb, rank, (int)m, cell_nb);
-    if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaEventRecord(ctx->copy_ev, ctx->copy_stream)) != cudaSuccess)
-        return cuda_fail(st, e, "ordering: anchor walk");
-    ctx->launches += 2;
 
     // Rows x anchors with k = 1 on the tensor cores, keeping only each row's
     // nearest anchor.
