@@ -351,14 +351,14 @@ __device__ __forceinline__ void quarter_mins(uint32_t (&v)[32], int64_t colbase,
 // five bits of its f32 pattern (an error of under 32 ulp, which an
 // approximately nearest column tolerates), so one minimum tree yields both
 // the smallest value and its column, with no vote or branch per chunk.
-// Columns past the reference rows (and the row itself) get a large finite
-// value.
+// Columns past the reference rows (and the row itself) become +inf before
+// the column goes in (+inf or NaN after it, which the minimum never takes).
 __device__ __forceinline__ void argmin_chunk(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a,
                                              float& best_v, uint32_t& best_c) {
     const uint32_t valid = chunk_valid(colbase, a.nr, a.self != 0, row + a.self_offset);
     if (__any_sync(0xffffffffu, valid != 0xffffffffu)) {
 #pragma unroll
-        for (int j = 0; j < 32; j++) v[j] = ((valid >> j) & 1u) ? v[j] : 0x7f7fffe0u;
+        for (int j = 0; j < 32; j++) v[j] = ((valid >> j) & 1u) ? v[j] : 0x7f800000u;
     }
 #pragma unroll
     for (int j = 0; j < 32; j++) v[j] = (v[j] & ~31u) | (uint32_t)j;

@@ -760,23 +760,22 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     // Anchors, and both operand sets in the input order.
     anchors_kernel<<<(unsigned)m, 64, 0, s>>>(x, d, n, m, src, anc);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchors");
-    // Anchor neighbourhoods and the walk that orders the cells.
-    {
-        float* adist = (float*)(base + o_adist);
-        const dim3 grid((unsigned)((m + 63) / 64), (unsigned)((m + 63) / 64));
-        anchor_dist_kernel<<<grid, 256, 0, s>>>(anc, (int)m, d, adist);
-        anchor_top_kernel<<<(unsigned)((m + 3) / 4), 128, 0, s>>>(adist, (int)m, anchor_nb);
-        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor neighbours");
-        ctx->launches += 2;
-    }
-    // The walk (one block on one SM) runs on the copy stream beside the
-    // operands and the rows x anchors pass below, which leaves it that SM; the
-    // main stream waits for it before the cells are formed.
+    // The anchor neighbourhoods and the walk that orders the cells run on the
+    // copy stream beside the operands and the rows x anchors pass below; the
+    // main stream waits for them before the cells are formed.
     const size_t chain_smem = 4 * (size_t)(((m + 31) / 32 + 1) / 2 * 2) + 2 * (size_t)m * kChainNb;
     if ((e = set_smem_limit(ctx, (const void*)anchor_chain_kernel, (int)chain_smem)) != cudaSuccess ||
         (e = cudaEventRecord(ctx->copy_ev, s)) != cudaSuccess ||
         (e = cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev, 0)) != cudaSuccess)
         return cuda_fail(st, e, "ordering: anchor walk");
+    {
+        float* adist = (float*)(base + o_adist);
+        const dim3 grid((unsigned)((m + 63) / 64), (unsigned)((m + 63) / 64));
+        anchor_dist_kernel<<<grid, 256, 0, ctx->copy_stream>>>(anc, (int)m, d, adist);
+        anchor_top_kernel<<<(unsigned)((m + 3) / 4), 128, 0, ctx->copy_stream>>>(adist, (int)m, anchor_nb);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: anchor neighbours");
+        ctx->launches += 2;
+    }
     anchor_chain_kernel<<<1, kChainThreads, chain_smem, ctx->copy_stream>>>(anchor_nb, (int)m, rank);
     relabel_neighbours_kernel<<<(unsigned)((m * kAnchorNeighbours + 255) / 256), 256, 0, ctx->copy_stream>>>(
         anchor_nb, rank, (int)m, cell_nb);
