@@ -151,6 +151,9 @@ __device__ __forceinline__ int sweep_tile(int i, int home, int ct0, int ct1) {
 // The column tiles of one work item in visiting order: its explicit list,
 // or the outward sweep over [ct0, ct1).  The producer, the MMA issuer and
 // the epilogue all derive the same count and sequence from it.
+// TWO: the pass may carry a second list (collect passes only), compiled out
+// of the others, whose registers are scarce.
+template <bool TWO>
 struct TileOrder {
     const uint32_t* list;
     const uint32_t* list2;
@@ -162,7 +165,7 @@ struct TileOrder {
         if (a.tl) {
             list = a.tl + (a.tl_off ? (int64_t)a.tl_off[w] : (int64_t)w * a.tl_stride);
             count = count1 = (int)min(a.tl_cnt[w], (uint32_t)(ct1_ - ct0_));
-            if (a.tl2) {
+            if (TWO && a.tl2) {
                 list2 = a.tl2 + (int64_t)w * a.tl2_stride;
                 count += (int)min(a.tl2_cnt[w], (uint32_t)(ct1_ - ct0_ - count1));
             }
@@ -170,6 +173,7 @@ struct TileOrder {
     }
     __device__ __forceinline__ int next(int it) const {
         if (!list) return sweep_tile(it, home, ct0, ct1);
+        if (!TWO) return (int)list[it];
         return it < count1 ? (int)list[it] : (int)list2[it - count1];
     }
 };
@@ -634,7 +638,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const int qt = w / csegs, seg = w % csegs;
                 const int ct0 = a.item_range ? (int)a.item_range[w].x : seg * a.tiles_per_seg;
                 const int ct1 = a.item_range ? (int)a.item_range[w].y : min(a.col_tiles, ct0 + a.tiles_per_seg);
-                const TileOrder order(a, w, qt, ct0, ct1);
+                const TileOrder<PASS == 2 || PASS == 0> order(a, w, qt, ct0, ct1);
                 if (order.count == 0) continue;
                 const uint32_t ab = ac & 1, au = ac >> 1;
                 if (!mbar_wait_bounded(&aempty[ab], (au & 1) ^ 1, a.err)) {
@@ -677,7 +681,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const int qt = w / csegs, seg = w % csegs;
                 const int ct0 = a.item_range ? (int)a.item_range[w].x : seg * a.tiles_per_seg;
                 const int ct1 = a.item_range ? (int)a.item_range[w].y : min(a.col_tiles, ct0 + a.tiles_per_seg);
-                const TileOrder order(a, w, qt, ct0, ct1);
+                const TileOrder<PASS == 2 || PASS == 0> order(a, w, qt, ct0, ct1);
                 if (order.count == 0) continue;
                 const uint32_t ab = ac & 1, au = ac >> 1;
                 if (!mbar_wait_bounded(&afull[ab], au & 1, a.err)) {
@@ -748,7 +752,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int qt = w / col_segs, seg = w % col_segs;
             const int ct0 = a.item_range ? (int)a.item_range[w].x : seg * a.tiles_per_seg;
             const int ct1 = a.item_range ? (int)a.item_range[w].y : min(a.col_tiles, ct0 + a.tiles_per_seg);
-            const TileOrder order(a, w, qt, ct0, ct1);
+            const TileOrder<PASS == 2 || PASS == 0> order(a, w, qt, ct0, ct1);
             if (order.count == 0) continue;
             const int64_t row = (int64_t)qt * ROWS + h * TBM + r_local;
             const bool valid = row < a.nq && (!a.row_map || a.row_map[row] != 0xffffffffu);
@@ -1330,6 +1334,7 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
         return cudaErrorInvalidValue;
     a.argmin_out = argmin_out;
     if (argmin_out && (plan.k != 1 || resume)) return cudaErrorInvalidValue;
+    if (a.tl2 && !a.collect) return cudaErrorInvalidValue;  // a second list is read by collect passes only
     if (resume && !theta_io) return cudaErrorInvalidValue;
     // Register top-k width of a general pass (threshold and collect passes
     // keep the width that holds k).
