@@ -463,6 +463,15 @@ SCRUST_API int32_t scrust_cuda_phase_times(scrust_context* context, float* ms, i
 SCRUST_API int32_t scrust_cuda_kernel_stats(scrust_context* context, int32_t enable, uint64_t* out,
                                             int32_t max_words);
 
+/* Self-test of the bounded device waits (no counterpart in the reference:
+ * the Metal backend has no device-side waits).  Runs one kernel that waits
+ * on an mbarrier nothing arrives on, with the wall-clock limit every sweep
+ * kernel's waits use replaced by limit_ns (at most 100 ms, else
+ * INVALID_PARAMETER).  Returns SCRUST_TIMEOUT when the wait ran out and was
+ * reported, as a sweep kernel's would be; the context stays usable. */
+SCRUST_API int32_t scrust_cuda_selftest_bounded_wait(scrust_context* context, uint64_t limit_ns,
+                                                     scrust_status* status);
+
 /* Number of kernels this context has launched since it was created. */
 SCRUST_API uint64_t scrust_cuda_launch_count(const scrust_context* context);
 

@@ -125,6 +125,7 @@ _SIGNATURES = {
     "scrust_cuda_set_timing": (None, [_P, ctypes.c_int32]),
     "scrust_cuda_phase_times": (ctypes.c_int32, [_P, ctypes.POINTER(ctypes.c_float), ctypes.c_int32]),
     "scrust_cuda_launch_count": (ctypes.c_uint64, [_P]),
+    "scrust_cuda_selftest_bounded_wait": (ctypes.c_int32, [_P, ctypes.c_uint64, ctypes.POINTER(Status)]),
     "scrust_cuda_kernel_stats": (ctypes.c_int32, [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64),
                                                    ctypes.c_int32]),
     "scrust_cuda_knn_batch": (ctypes.c_int32, [_P, _P, _P, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32,

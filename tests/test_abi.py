@@ -112,3 +112,8 @@ def test_python_layer_maps_errors_like_the_reference(L):
         _scrust.connectivities(np.zeros((2, 1), np.int64), np.zeros((2, 1), np.float32))
     with pytest.raises(ValueError):
         _scrust.connectivities(np.zeros((2, 1), np.uint32), np.zeros((2, 2), np.float32))
+
+
+def test_bounded_wait_self_test_needs_a_context(L):
+    st = L.Status()
+    assert L.lib().scrust_cuda_selftest_bounded_wait(None, 1_000_000, ctypes.byref(st)) == L.NO_GPU
