@@ -59,6 +59,7 @@ enum Slot : int {
     SLOT_RERANK_BIG,    // rows for the rerank's second sorted pass
     SLOT_QTERMS,        // per-query-row bound terms of a query-versus-reference solve
     SLOT_QSCRATCH,      // scratch operands of a query-versus-reference solve
+    SLOT_XORDER,        // routing, priority tiles and pruning of a query solve against an ordered atlas
     SLOT_BATCH_GIDX,    // a batch's neighbour ids made batch-global for its connectivities
     SLOT_UMAP,          // the UMAP layout's schedules, moves, transpose and second layout
     SLOT_PCA,           // PCA: sketch, bases, CSC copy, Grams, small factors
@@ -227,6 +228,16 @@ struct RowOrder {
     const uint32_t* prio_cnt = nullptr;  // [items], at least 1
     float* theta = nullptr;              // [n_pad * 2] list thresholds between the sweep passes
     const uint32_t* cell_of_pos = nullptr;  // [n] cell of each sorted position
+    // The anchors behind the cells (a reference set ordered once keeps them
+    // to route queries): their count, B operands in anchor order
+    // (anchors_pad rows), walk places, the cells' first list positions in walk
+    // order (anchors + 1) and each cell's neighbouring cells (anchors x
+    // kAnchorNeighbours walk places).
+    int64_t anchors = 0, anchors_pad = 0;
+    const void* anchor_B16 = nullptr;
+    const uint32_t* anchor_rank = nullptr;
+    const uint32_t* cell_start = nullptr;
+    const uint32_t* cell_nb = nullptr;
 };
 // Builds the ordering and leaves the tensor operands A16/B16 and their row
 // terms bA/beps (n_pad rows each) in list order; bdelta/beps2 serve as
@@ -235,6 +246,38 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
                         uint32_t* max_bits, bool cosine, bool bf16, void* A16, void* B16, float* bA, float* beps,
                         float* bdelta, float* beps2, RowOrder* out, scrust_status* st);
 struct TileLists;
+// A reference set ordered once for query solves (the served atlas), device
+// memory it owns: the B operands and rows in list order, the permutation, the
+// anchors that route queries to cells, and the cell-segment balls of its
+// column tiles.
+struct AtlasOrder {
+    int64_t m = 0, m_pad = 0, anchors = 0, anchors_pad = 0, segs = 0;
+    int d = 0;
+    bool bf16 = false;
+    void* B16 = nullptr;             // m_pad rows of the B operand, list order
+    uint32_t* perm = nullptr;        // list position -> atlas row
+    float* rows = nullptr;           // atlas rows in list order, padded_row_floats(d) floats each
+    void* anchor_B16 = nullptr;      // anchors_pad rows, anchor order
+    uint32_t* anchor_rank = nullptr; // anchor -> walk place
+    uint32_t* cell_start = nullptr;  // anchors + 1, by walk place
+    uint32_t* cell_nb = nullptr;     // anchors x kAnchorNeighbours walk places
+    float* seg_centre_t = nullptr;   // [64][segs] segment centres (zero past d)
+    float* seg_radius = nullptr;     // [segs]
+    uint32_t* seg_tile = nullptr;    // [segs] column tile of each segment
+};
+// Orders `atlas` (device rows) once: means and the maxima in `words` as the
+// served atlas has them (max centred norm; the quantisation maxima are
+// raised).  Synchronises the context's stream.
+int32_t atlas_order_build(scrust_context* ctx, const float* atlas, int64_t m, int d, const double* means,
+                          uint32_t* words, bool bf16, AtlasOrder* out, scrust_status* st);
+void atlas_order_free(AtlasOrder* o);
+// k <= 32 nearest atlas rows of each query row (input order outputs), exact:
+// queries routed to their nearest anchor's cell and sorted by it, a threshold
+// pass over priority tiles, another over the tiles the balls keep, a collect
+// pass over both, the sorted rerank.  `words` are the atlas's.
+int32_t cross_ordered_enqueue(scrust_context* ctx, const AtlasOrder& at, const float* atlas_rows, const double* means,
+                              const uint32_t* words, const float* dq, int64_t q, int k, uint32_t* d_idx,
+                              float* d_dist, scrust_status* st);
 // After the priority pass: the column tiles each row block still has to
 // visit, from tile bounding balls and the rows' thresholds (order.cu).
 int32_t build_second_pass(scrust_context* ctx, const void* A16, bool bf16, int64_t n, int d, const RowOrder& order,
@@ -340,7 +383,8 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
                           const uint32_t* perm, const float* xs, const float* theta, uint32_t* out_idx,
                           float* out_dist, const uint32_t* row_lo = nullptr, const uint32_t* row_hi = nullptr,
-                          const float* xr_list = nullptr, int xs_stride = 0, bool ids_only = false);
+                          const float* xr_list = nullptr, int xs_stride = 0, bool ids_only = false,
+                          const uint32_t* qperm = nullptr);
 // order.cu: row blocks sorted by decreasing count (stable) into `order`;
 // `scratch` holds work_order_scratch(items) bytes.
 size_t work_order_scratch(int items);

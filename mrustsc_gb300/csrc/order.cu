@@ -243,13 +243,13 @@ __global__ void unpack_perm_kernel(const uint32_t* __restrict__ skeys, const uns
 
 // One warp per 256-row work item: the column tiles holding the item's own
 // cells, then those holding the cells of their nearest anchors, nearest
-// anchors first; distinct, at most kPrioMax.  The item's own tile always
-// comes first, so no list is empty.
+// anchors first; distinct, at most kPrioMax.  In a self solve the item's own
+// tile always comes first, so no list is empty.
 constexpr int kHomeMax = 8;
 __global__ void prio_tiles_kernel(const uint32_t* __restrict__ cell_of_pos, int64_t n,
                                   const uint32_t* __restrict__ cell_start, int m,
                                   const uint32_t* __restrict__ anchor_nb, int ka, int items, int col_tiles,
-                                  uint32_t* __restrict__ prio, uint32_t* __restrict__ prio_cnt) {
+                                  uint32_t* __restrict__ prio, uint32_t* __restrict__ prio_cnt, int self_tile = 1) {
     __shared__ uint32_t outs[4][kPrioMax];
     __shared__ uint32_t homes[4][kHomeMax];
     __shared__ int nhome[4];
@@ -283,7 +283,7 @@ __global__ void prio_tiles_kernel(const uint32_t* __restrict__ cell_of_pos, int6
         cnt++;
         __syncwarp();
     };
-    add((uint32_t)item);
+    if (self_tile) add((uint32_t)item);  // a self solve's own tile (query solves have none)
     const int kk = min(ka, kAnchorNeighbours);
     for (int j = -1; j < kk && cnt < kPrioMax; ++j) {
         for (int hh = 0; hh < nh && cnt < kPrioMax; ++hh) {
@@ -549,16 +549,17 @@ __global__ void __launch_bounds__(256) segment_pairs_kernel(const float* __restr
 __global__ void __launch_bounds__(256) tile_lists_kernel(const uint32_t* __restrict__ bitmap, int words, int tiles,
                                                          const uint32_t* __restrict__ prio,
                                                          const uint32_t* __restrict__ prio_cnt,
-                                                         uint32_t* __restrict__ counts, uint32_t* __restrict__ entries) {
+                                                         uint32_t* __restrict__ counts, uint32_t* __restrict__ entries,
+                                                         int prio_stride = kPrioMax) {
     extern __shared__ uint32_t in_prio[];  // words
     __shared__ int wsum[8];
     const int I = blockIdx.x;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int pc = (int)min(prio_cnt[I], (uint32_t)kPrioMax);
+    const int pc = (int)min(prio_cnt[I], (uint32_t)min(prio_stride, (int)blockDim.x));
     for (int i = threadIdx.x; i < words; i += blockDim.x) in_prio[i] = 0u;
     __syncthreads();
     if (threadIdx.x < pc) {
-        const uint32_t t = prio[(int64_t)I * kPrioMax + threadIdx.x];
+        const uint32_t t = prio[(int64_t)I * prio_stride + threadIdx.x];
         if (t < (uint32_t)tiles) atomicOr(&in_prio[t >> 5], 1u << (t & 31));
     }
     __syncthreads();
@@ -642,6 +643,103 @@ __global__ void narrow_kernel(const unsigned long long* __restrict__ vals, int i
 
 // One thread per 4-float group of an output row (stride is a multiple of 4
 // for the padded layout; otherwise one float per thread).
+// Segment centres transposed to [64][segs], so that threads reading one
+// dimension of consecutive segments read consecutive words.
+__global__ void transpose_centres_kernel(const float* __restrict__ fc, int64_t segs, float* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= segs * 64) return;
+    out[(i % 64) * segs + i / 64] = fc[i];
+}
+
+// Query blocks against atlas tiles: for every (query segment, atlas segment)
+// pair, the atlas tile may hold a candidate of the query block while
+// tile_needed holds (the same test as a self solve's, with the query
+// segment's reach).  One block per query segment at a time, its centre in
+// shared memory; threads over the atlas segments.
+__global__ void __launch_bounds__(256) cross_segment_pairs_kernel(
+    const float* __restrict__ qc, const float* __restrict__ qr, const float* __restrict__ qu,
+    const uint32_t* __restrict__ qo, const uint32_t* __restrict__ q_count, const float* __restrict__ act,
+    const float* __restrict__ ar, const uint32_t* __restrict__ ao, int64_t asegs, int d, int words,
+    uint32_t* __restrict__ bitmap) {
+    __shared__ float c[64];
+    const uint32_t sq = *q_count;
+    for (uint32_t a = blockIdx.x; a < sq; a += gridDim.x) {
+        __syncthreads();
+        if (threadIdx.x < 64) c[threadIdx.x] = qc[(int64_t)a * 64 + threadIdx.x];
+        __syncthreads();
+        const float ra = qr[a], ua = qu[a];
+        const uint32_t item = qo[a];
+        for (int64_t b = threadIdx.x; b < asegs; b += blockDim.x) {
+            float acc = 0.f;
+            for (int t = 0; t < d; ++t) {
+                const float df = c[t] - act[(int64_t)t * asegs + b];
+                acc = fmaf(df, df, acc);
+            }
+            if (tile_needed(acc, ra, ar[b], ua)) {
+                const uint32_t tb = ao[b];
+                atomicOr(bitmap + (int64_t)item * words + (tb >> 5), 1u << (tb & 31));
+            }
+        }
+    }
+}
+
+// Priority tiles of a block of routed queries.  A block of 256 queries sorted
+// by cell may span many cells (queries are few per cell), so every cell of
+// its rows counts: the tiles holding those cells, lowest first, then the
+// tiles of their eight nearest neighbouring cells, at most kQueryPrio in all.
+// One block of 256 threads per query block; two tile bitmaps in shared memory.
+constexpr int kQueryPrio = 256;
+constexpr int kQueryPrioNb = 8;
+__global__ void __launch_bounds__(256) query_prio_kernel(const uint32_t* __restrict__ cell_of_pos, int64_t n,
+                                                         const uint32_t* __restrict__ cell_start, int m,
+                                                         const uint32_t* __restrict__ cell_nb, int col_tiles,
+                                                         uint32_t* __restrict__ prio, uint32_t* __restrict__ prio_cnt) {
+    extern __shared__ uint32_t qp_bm[];
+    const int words = (col_tiles + 31) / 32;
+    uint32_t* home = qp_bm;
+    uint32_t* near = qp_bm + words;
+    const int I = blockIdx.x;
+    for (int i = threadIdx.x; i < 2 * words; i += blockDim.x) qp_bm[i] = 0u;
+    __syncthreads();
+    const int64_t p = (int64_t)I * 256 + threadIdx.x;
+    auto mark = [&](uint32_t* bm, uint32_t c) {
+        if (c >= (uint32_t)m) return;
+        const uint32_t a = cell_start[c], b = cell_start[c + 1];
+        if (b <= a) return;
+        for (uint32_t t = a / 256; t <= (b - 1) / 256 && t < (uint32_t)col_tiles; ++t)
+            atomicOr(&bm[t >> 5], 1u << (t & 31));
+    };
+    if (p < n) {
+        const uint32_t c = cell_of_pos[p];
+        // Rows of one cell come together: the first of each run marks for all.
+        if (p == (int64_t)I * 256 || cell_of_pos[p - 1] != c) {
+            mark(home, c);
+            if (c < (uint32_t)m)
+                for (int j = 0; j < kQueryPrioNb; ++j) mark(near, cell_nb[(int64_t)c * kAnchorNeighbours + j]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t* out = prio + (int64_t)I * kQueryPrio;
+        int cnt = 0;
+        for (int w = 0; w < words && cnt < kQueryPrio; ++w) {
+            uint32_t bits = home[w];
+            while (bits && cnt < kQueryPrio) {
+                out[cnt++] = (uint32_t)(w * 32 + __ffs(bits) - 1);
+                bits &= bits - 1;
+            }
+        }
+        for (int w = 0; w < words && cnt < kQueryPrio; ++w) {
+            uint32_t bits = near[w] & ~home[w];
+            while (bits && cnt < kQueryPrio) {
+                out[cnt++] = (uint32_t)(w * 32 + __ffs(bits) - 1);
+                bits &= bits - 1;
+            }
+        }
+        prio_cnt[I] = (uint32_t)cnt;
+    }
+}
+
 __global__ void gather_rows_kernel(const float* __restrict__ x, const uint32_t* __restrict__ perm, int64_t n, int d,
                                    int stride, float* __restrict__ xs) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -855,6 +953,12 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     out->prio_order = (const uint32_t*)(base + o_po);
     out->theta = (float*)(base + o_theta);
     out->cell_of_pos = cell_of_pos;
+    out->anchors = m;
+    out->anchors_pad = m_pad;
+    out->anchor_B16 = base + o_aB;
+    out->anchor_rank = rank;
+    out->cell_start = cell_start;
+    out->cell_nb = cell_nb;
     return SCRUST_OK;
 }
 
@@ -930,6 +1034,356 @@ int32_t build_second_pass(scrust_context* ctx, const void* A16, bool bf16, int64
     out->stride = tiles;
     out->order = (const uint32_t*)(base + o_wo);
     return SCRUST_OK;
+}
+
+// ---- query solves against an ordered atlas -------------------------------------
+
+namespace {
+
+void launch_tile_balls(bool bf16, const void* ops, int64_t n, int d, int tiles, const uint32_t* cell_of_pos,
+                       const float* theta, const float* bA, const float* bdelta, const TileBalls& b, cudaStream_t s) {
+    if (bf16)
+        tile_balls_kernel<__nv_bfloat16><<<tiles, 256, 0, s>>>((const __nv_bfloat16*)ops, n, d, tiles, cell_of_pos,
+                                                               theta, bA, bdelta, b);
+    else
+        tile_balls_kernel<__half><<<tiles, 256, 0, s>>>((const __half*)ops, n, d, tiles, cell_of_pos, theta, bA,
+                                                        bdelta, b);
+}
+
+// The per-tile ball arrays of `tiles` tiles, laid out from byte `at` of
+// `base`; returns the end of the layout.
+size_t carve_balls(char* base, size_t at, int tiles, int d, TileBalls* b) {
+    auto take = [&](size_t bytes) {
+        const size_t a = at;
+        at = align_up(at + bytes);
+        return base + a;
+    };
+    b->centre = (float*)take(4 * (size_t)d * tiles);
+    b->radius = (float*)take(4 * (size_t)tiles);
+    b->reach = (float*)take(4 * (size_t)tiles);
+    b->seg_centre = (float*)take(4 * (size_t)kSegMax * d * tiles);
+    b->seg_radius = (float*)take(4 * (size_t)kSegMax * tiles);
+    b->seg_reach = (float*)take(4 * (size_t)kSegMax * tiles);
+    b->nseg = (uint32_t*)take(4 * ((size_t)tiles + 1));
+    return at;
+}
+
+}  // namespace
+
+void atlas_order_free(AtlasOrder* o) {
+    if (!o) return;
+    void* ptrs[] = {o->B16, o->perm, o->rows, o->anchor_B16, o->anchor_rank, o->cell_start,
+                    o->cell_nb, o->seg_centre_t, o->seg_radius, o->seg_tile};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    *o = AtlasOrder{};
+}
+
+int32_t atlas_order_build(scrust_context* ctx, const float* atlas, int64_t m, int d, const double* means,
+                          uint32_t* words, bool bf16, AtlasOrder* out, scrust_status* st) {
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaSuccess;
+    AtlasOrder o;
+    o.m = m;
+    o.m_pad = (m + 255) / 256 * 256;
+    o.d = d;
+    o.bf16 = bf16;
+    const int tiles = (int)(o.m_pad / 256);
+    const int P = padded_row_floats(d);
+    // Scratch of the build: operands and row terms in list order, the tile
+    // balls and their flattened segments.
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = off;
+        off = align_up(off + bytes);
+        return at;
+    };
+    const int64_t smax = (int64_t)tiles * kSegMax;
+    const size_t scan_elems = scan_scratch_elems((int64_t)tiles + 1);
+    const size_t o_A = take(128 * (size_t)o.m_pad), o_t = take(4 * 4 * (size_t)o.m_pad),
+                 o_th = take(4 * 2 * (size_t)o.m_pad), o_so = take(4 * ((size_t)tiles + 1)),
+                 o_fc = take(4 * 64 * (size_t)smax), o_fr = take(4 * (size_t)smax), o_fu = take(4 * (size_t)smax),
+                 o_fo = take(4 * (size_t)smax), o_scan = take(4 * scan_elems);
+    TileBalls balls;
+    const size_t total = carve_balls(nullptr, off, tiles, d, &balls);
+    char* base = nullptr;
+    if ((e = cudaMalloc(&base, total)) != cudaSuccess || (e = cudaMalloc(&o.B16, 128 * (size_t)o.m_pad)) != cudaSuccess) {
+        cudaFree(base);
+        atlas_order_free(&o);
+        cudaGetLastError();
+        return cuda_fail(st, e, "atlas ordering: allocation");
+    }
+    carve_balls(base, off, tiles, d, &balls);
+    float* terms = (float*)(base + o_t);
+    float *bA = terms, *beps = terms + o.m_pad, *bdelta = terms + 2 * o.m_pad, *beps2 = terms + 3 * o.m_pad;
+    RowOrder ord;
+    int32_t rc = build_row_order(ctx, atlas, m, d, means, words, false, bf16, base + o_A, o.B16, bA, beps, bdelta,
+                                 beps2, &ord, st);
+    auto bail = [&](int32_t code) {
+        cudaStreamSynchronize(s);
+        cudaFree(base);
+        atlas_order_free(&o);
+        cudaGetLastError();
+        return code;
+    };
+    if (rc) return bail(rc);
+    o.anchors = ord.anchors;
+    o.anchors_pad = ord.anchors_pad;
+    const size_t na = (size_t)o.anchors;
+    if ((e = cudaMalloc(&o.perm, 4 * (size_t)m)) != cudaSuccess ||
+        (e = cudaMalloc(&o.rows, 4 * (size_t)m * P)) != cudaSuccess ||
+        (e = cudaMalloc(&o.anchor_B16, 128 * (size_t)o.anchors_pad)) != cudaSuccess ||
+        (e = cudaMalloc(&o.anchor_rank, 4 * na)) != cudaSuccess ||
+        (e = cudaMalloc(&o.cell_start, 4 * (na + 1))) != cudaSuccess ||
+        (e = cudaMalloc(&o.cell_nb, 4 * na * kAnchorNeighbours)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(o.perm, ord.perm, 4 * (size_t)m, cudaMemcpyDeviceToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(o.anchor_B16, ord.anchor_B16, 128 * (size_t)o.anchors_pad, cudaMemcpyDeviceToDevice,
+                             s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(o.anchor_rank, ord.anchor_rank, 4 * na, cudaMemcpyDeviceToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(o.cell_start, ord.cell_start, 4 * (na + 1), cudaMemcpyDeviceToDevice, s)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(o.cell_nb, ord.cell_nb, 4 * na * kAnchorNeighbours, cudaMemcpyDeviceToDevice, s)) !=
+            cudaSuccess ||
+        (e = launch_gather_rows(atlas, ord.perm, m, d, P, o.rows, s)) != cudaSuccess ||
+        (e = launch_tensor_bounds(m, bA, beps, words + 1, words + 2, bdelta, beps2, s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(base + o_th, 0, 4 * 2 * (size_t)o.m_pad, s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(balls.nseg + tiles, 0, sizeof(uint32_t), s)) != cudaSuccess)
+        return bail(cuda_fail(st, e, "atlas ordering"));
+    // The cell-segment balls of the atlas tiles (their reach is not used).
+    uint32_t* seg_off = (uint32_t*)(base + o_so);
+    float* fc = (float*)(base + o_fc);
+    launch_tile_balls(bf16, base + o_A, m, d, tiles, ord.cell_of_pos, (const float*)(base + o_th), bA, bdelta,
+                              balls, s);
+    if ((e = cudaGetLastError()) != cudaSuccess ||
+        (e = device_exclusive_scan(ctx, balls.nseg, seg_off, (int64_t)tiles + 1, (uint32_t*)(base + o_scan),
+                                   scan_elems)) != cudaSuccess)
+        return bail(cuda_fail(st, e, "atlas ordering: tile balls"));
+    flatten_segments_kernel<<<tiles, 64, 0, s>>>(balls, d, tiles, seg_off, fc, (float*)(base + o_fr),
+                                                 (float*)(base + o_fu), (uint32_t*)(base + o_fo));
+    uint32_t segs = 0;
+    if ((e = cudaGetLastError()) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&segs, seg_off + tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return bail(cuda_fail(st, e, "atlas ordering: segments"));
+    o.segs = segs;
+    if ((e = cudaMalloc(&o.seg_centre_t, 4 * 64 * (size_t)std::max<uint32_t>(segs, 1))) != cudaSuccess ||
+        (e = cudaMalloc(&o.seg_radius, 4 * (size_t)std::max<uint32_t>(segs, 1))) != cudaSuccess ||
+        (e = cudaMalloc(&o.seg_tile, 4 * (size_t)std::max<uint32_t>(segs, 1))) != cudaSuccess ||
+        (e = cudaMemcpyAsync(o.seg_radius, base + o_fr, 4 * (size_t)segs, cudaMemcpyDeviceToDevice, s)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(o.seg_tile, base + o_fo, 4 * (size_t)segs, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+        return bail(cuda_fail(st, e, "atlas ordering: segments"));
+    if (segs) transpose_centres_kernel<<<(unsigned)((64 * (int64_t)segs + 255) / 256), 256, 0, s>>>(fc, segs,
+                                                                                                 o.seg_centre_t);
+    if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return bail(cuda_fail(st, e, "atlas ordering: segments"));
+    ctx->launches += 4;
+    cudaFree(base);
+    *out = o;
+    return ok(st);
+}
+
+int32_t cross_ordered_enqueue(scrust_context* ctx, const AtlasOrder& at, const float* atlas_rows, const double* means,
+                              const uint32_t* words, const float* dq, int64_t q, int k, uint32_t* d_idx,
+                              float* d_dist, scrust_status* st) {
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaSuccess;
+    const int d = at.d;
+    const bool bf16 = at.bf16;
+    const int64_t q_pad = (q + 255) / 256 * 256;
+    const int items = (int)(q_pad / 256), col_tiles = (int)(at.m_pad / 256), words_t = (col_tiles + 31) / 32;
+    const int P = padded_row_floats(d);
+    const int nblocks = radix_blocks(q);
+    const int64_t smax = (int64_t)items * kSegMax;
+    const size_t scan_elems =
+        scan_scratch_elems(std::max<int64_t>((int64_t)256 * nblocks, std::max<int64_t>(items, at.anchors) + 1));
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t a = off;
+        off = align_up(off + bytes);
+        return a;
+    };
+    const size_t o_A0 = take(128 * (size_t)q_pad), o_B0 = take(128 * (size_t)q_pad), o_t0 = take(4 * 2 * (size_t)q_pad),
+                 o_As = take(128 * (size_t)q_pad), o_Bs = take(128 * (size_t)q_pad), o_ts = take(4 * 4 * (size_t)q_pad),
+                 o_w = take(64), o_best = take(16 * (size_t)q_pad), o_kA = take(4 * (size_t)q), o_kB = take(4 * (size_t)q),
+                 o_vA = take(8 * (size_t)q), o_vB = take(8 * (size_t)q), o_qp = take(4 * (size_t)q),
+                 o_cell = take(4 * (size_t)q), o_cc = take(4 * ((size_t)at.anchors + 1)),
+                 o_xs = take(4 * (size_t)q * P), o_prio = take(4 * (size_t)items * kQueryPrio),
+                 o_pc = take(4 * (size_t)items), o_po = take(4 * (size_t)items), o_po2 = take(4 * (size_t)items),
+                 o_ws = take(work_order_scratch(items)),
+                 o_th = take(4 * 2 * (size_t)q_pad), o_so = take(4 * ((size_t)items + 1)),
+                 o_fc = take(4 * 64 * (size_t)smax), o_fr = take(4 * (size_t)smax), o_fu = take(4 * (size_t)smax),
+                 o_fo = take(4 * (size_t)smax), o_bm = take(4 * (size_t)items * words_t),
+                 o_cnt = take(4 * ((size_t)items + 1)), o_ent = take(4 * (size_t)items * col_tiles),
+                 o_hist = take(4 * ((size_t)256 * nblocks + 16)), o_scan = take(4 * scan_elems);
+    TileBalls qballs;
+    const size_t total = carve_balls(nullptr, off, items, d, &qballs);
+    char* base = (char*)ws_get(ctx, SLOT_XORDER, total, &e);
+    if (!base) return cuda_fail(st, e, "query routing: workspace");
+    carve_balls(base, off, items, d, &qballs);
+    float* t0 = (float*)(base + o_t0);
+    float *bA0 = t0, *eps0 = t0 + q_pad;
+    float* ts = (float*)(base + o_ts);
+    float *bA = ts, *beps = ts + q_pad, *bdelta = ts + 2 * q_pad, *beps2 = ts + 3 * q_pad;
+    uint32_t* qwords = (uint32_t*)(base + o_w);
+    uint32_t* qperm = (uint32_t*)(base + o_qp);
+    uint32_t* cell_of_pos = (uint32_t*)(base + o_cell);
+    uint32_t* prio = (uint32_t*)(base + o_prio);
+    uint32_t* prio_cnt = (uint32_t*)(base + o_pc);
+    uint32_t* prio_order = (uint32_t*)(base + o_po);
+    float* theta = (float*)(base + o_th);
+    float* xs = (float*)(base + o_xs);
+    uint32_t* seg_off = (uint32_t*)(base + o_so);
+    uint32_t* bitmap = (uint32_t*)(base + o_bm);
+    uint32_t* counts = (uint32_t*)(base + o_cnt);
+    uint32_t* entries = (uint32_t*)(base + o_ent);
+    unsigned long long* best = (unsigned long long*)(base + o_best);
+
+    // The queries' operands, in input order; every query's nearest anchor.
+    if ((e = cudaMemsetAsync(qwords, 0, 64, s)) != cudaSuccess ||
+        (e = launch_tensor_operands(dq, q, q_pad, d, means, words, false, bf16, nullptr, base + o_A0, base + o_B0, bA0,
+                                    eps0, qwords, qwords + 1, s)) != cudaSuccess)
+        return cuda_fail(st, e, "query routing: operands");
+    KnnPlan px;
+    px.nq = q;
+    px.nr = at.anchors;
+    px.d = d;
+    px.k = 1;
+    px.self = false;
+    px.form = SCRUST_FORM_TENSOR;
+    Lists lx;  // no storage: the pass keeps no lists
+    lx.cap = 64;
+    lx.ctot = 64 + 128;
+    lx.segments = 2;
+    px.cap = lx.cap;
+    px.ctot = lx.ctot;
+    px.segments = lx.segments;
+    if ((e = launch_tensor_candidates(ctx, px, base + o_A0, q_pad, at.anchor_B16, at.anchors_pad, bA0, eps0, eps0, lx,
+                                      bf16, nullptr, false, nullptr, nullptr, nullptr, best)) != cudaSuccess)
+        return cuda_fail(st, e, "query routing: nearest anchor");
+    nearest_anchor_kernel<<<(unsigned)((q + 255) / 256), 256, 0, s>>>(best, q, at.anchors, at.anchor_rank,
+                                                                     (uint32_t*)(base + o_kA),
+                                                                     (unsigned long long*)(base + o_vA));
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "query routing: nearest anchor");
+    ctx->launches += 3;
+    // The queries sorted by the walk place of their cell; their operands,
+    // bounds and rows in that order.
+    int bits = 1;
+    while (((int64_t)1 << bits) < at.anchors) bits++;
+    uint32_t* skeys = nullptr;
+    unsigned long long* svals = nullptr;
+    if ((e = radix_sort_pairs(ctx, (uint32_t*)(base + o_kA), (unsigned long long*)(base + o_vA),
+                              (uint32_t*)(base + o_kB), (unsigned long long*)(base + o_vB), q, bits,
+                              (uint32_t*)(base + o_hist), (uint32_t*)(base + o_scan), scan_elems, &skeys, &svals)) !=
+            cudaSuccess ||
+        (e = cudaMemsetAsync(base + o_cc, 0, 4 * ((size_t)at.anchors + 1), s)) != cudaSuccess)
+        return cuda_fail(st, e, "query routing: sort");
+    unpack_perm_kernel<<<(unsigned)((q + 255) / 256), 256, 0, s>>>(skeys, svals, q, qperm, cell_of_pos,
+                                                                  (uint32_t*)(base + o_cc));
+    gather_operands_kernel<<<(unsigned)((q_pad * 8 + 255) / 256), 256, 0, s>>>(
+        (const uint4*)(base + o_A0), (const uint4*)(base + o_B0), bA0, eps0, qperm, q, q_pad, (uint4*)(base + o_As),
+        (uint4*)(base + o_Bs), bA, beps);
+    if ((e = cudaGetLastError()) != cudaSuccess ||
+        (e = launch_tensor_bounds(q, bA, beps, words + 1, words + 2, bdelta, beps2, s)) != cudaSuccess ||
+        (e = launch_gather_rows(dq, qperm, q, d, P, xs, s)) != cudaSuccess)
+        return cuda_fail(st, e, "query routing: gather");
+    const size_t prio_smem = 8 * (size_t)words_t;
+    if ((e = set_smem_limit(ctx, (const void*)query_prio_kernel, (int)prio_smem)) != cudaSuccess)
+        return cuda_fail(st, e, "query routing: priority tiles");
+    query_prio_kernel<<<items, 256, prio_smem, s>>>(cell_of_pos, q, at.cell_start, (int)at.anchors, at.cell_nb,
+                                                    col_tiles, prio, prio_cnt);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "query routing: priority tiles");
+    if ((e = sort_by_work(ctx, prio_cnt, items, base + o_ws, prio_order)) != cudaSuccess)
+        return cuda_fail(st, e, "query routing: work order");
+    ctx->launches += 5;
+
+    // The threshold pass over the priority tiles.
+    KnnPlan plan;
+    plan.nq = q;
+    plan.nr = at.m;
+    plan.d = d;
+    plan.k = k;
+    plan.self = false;
+    plan.form = SCRUST_FORM_TENSOR;
+    plan.precision = bf16 ? SCRUST_PRECISION_BF16 : SCRUST_PRECISION_FP16;
+    Lists lists;
+    lists.cap = 256;
+    lists.ctot = 256 + 128;
+    lists.segments = 2;
+    int32_t rc = alloc_lists(ctx, q_pad, &lists, st);
+    if (rc) return rc;
+    plan.cap = lists.cap;
+    plan.ctot = lists.ctot;
+    plan.segments = lists.segments;
+    TileLists first;
+    first.tiles = prio;
+    first.count = prio_cnt;
+    first.stride = kQueryPrio;
+    first.order = prio_order;
+    // A row the pass leaves without a threshold (a block with no priority
+    // tile) keeps a huge one: every tile stays in its second list.
+    if ((e = cudaMemsetAsync(theta, 0x7f, 4 * 2 * (size_t)q_pad, s)) != cudaSuccess)
+        return cuda_fail(st, e, "query knn: memset");
+    if ((e = launch_tensor_candidates(ctx, plan, base + o_As, q_pad, at.B16, at.m_pad, bA, bdelta, beps2, lists, bf16,
+                                      &first, false, theta, nullptr, nullptr, nullptr, kPassThresholds)) != cudaSuccess)
+        return cuda_fail(st, e, "query knn: threshold pass");
+    // The atlas tiles each query block cannot rule out: query-block segment
+    // balls (reach from the thresholds) against the atlas segment balls.
+    if ((e = cudaMemsetAsync(qballs.nseg + items, 0, sizeof(uint32_t), s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(bitmap, 0, 4 * (size_t)items * words_t, s)) != cudaSuccess)
+        return cuda_fail(st, e, "query knn: memset");
+    launch_tile_balls(bf16, base + o_As, q, d, items, cell_of_pos, theta, bA, bdelta, qballs, s);
+    if ((e = cudaGetLastError()) != cudaSuccess ||
+        (e = device_exclusive_scan(ctx, qballs.nseg, seg_off, (int64_t)items + 1, (uint32_t*)(base + o_scan),
+                                   scan_elems)) != cudaSuccess)
+        return cuda_fail(st, e, "query knn: query balls");
+    flatten_segments_kernel<<<items, 64, 0, s>>>(qballs, d, items, seg_off, (float*)(base + o_fc),
+                                                 (float*)(base + o_fr), (float*)(base + o_fu),
+                                                 (uint32_t*)(base + o_fo));
+    cross_segment_pairs_kernel<<<(unsigned)std::min<int64_t>(smax, 8 * ctx->sm_count), 256, 0, s>>>(
+        (const float*)(base + o_fc), (const float*)(base + o_fr), (const float*)(base + o_fu),
+        (const uint32_t*)(base + o_fo), seg_off + items, at.seg_centre_t, at.seg_radius, at.seg_tile, at.segs, d,
+        words_t, bitmap);
+    const size_t lists_smem = 4 * (size_t)words_t;
+    if ((e = cudaGetLastError()) != cudaSuccess ||
+        (e = set_smem_limit(ctx, (const void*)tile_lists_kernel, (int)lists_smem)) != cudaSuccess)
+        return cuda_fail(st, e, "query knn: tile lists");
+    tile_lists_kernel<<<items, 256, lists_smem, s>>>(bitmap, words_t, col_tiles, prio, prio_cnt, counts, entries,
+                                                     kQueryPrio);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "query knn: tile lists");
+    ctx->launches += 6;
+    // The thresholds tightened over the kept tiles too: a query's neighbours
+    // spread over its cluster, so a block whose queries fall in many cells
+    // leaves the first pass with loose thresholds, and collecting at those
+    // would overflow the lists.
+    TileLists second;
+    second.tiles = entries;
+    second.count = counts;
+    second.stride = col_tiles;
+    if ((e = sort_by_work(ctx, counts, items, base + o_ws, (uint32_t*)(base + o_po2))) != cudaSuccess)
+        return cuda_fail(st, e, "query knn: work order");
+    second.order = (const uint32_t*)(base + o_po2);
+    if ((e = launch_tensor_candidates(ctx, plan, base + o_As, q_pad, at.B16, at.m_pad, bA, bdelta, beps2, lists, bf16,
+                                      &second, true, theta, nullptr, nullptr, nullptr, kPassThresholds)) != cudaSuccess)
+        return cuda_fail(st, e, "query knn: second threshold pass");
+    // One collect pass over both lists, then the exact finish.
+    TileLists both = first;
+    both.tiles2 = entries;
+    both.count2 = counts;
+    both.stride2 = col_tiles;
+    if ((e = launch_tensor_candidates(ctx, plan, base + o_As, q_pad, at.B16, at.m_pad, bA, bdelta, beps2, lists, bf16,
+                                      &both, false, theta, nullptr, nullptr, nullptr, kPassCollect)) != cudaSuccess)
+        return cuda_fail(st, e, "query knn: collect pass");
+    RowBounds bounds;
+    bounds.A = bA;
+    bounds.delta = bdelta;
+    bounds.eps2 = beps2;
+    if ((e = launch_rerank(ctx, plan, dq, atlas_rows, nullptr, nullptr, nullptr, nullptr, dq, atlas_rows, bounds,
+                           lists, at.perm, xs, theta, d_idx, d_dist, nullptr, nullptr, at.rows, P, true, qperm)) !=
+        cudaSuccess)
+        return cuda_fail(st, e, "query knn: rerank");
+    ctx->launches += 2;
+    return ok(st);
 }
 
 }  // namespace scrust

@@ -38,7 +38,8 @@ struct RerankArgs {
     const float* rraw;
     RowBounds bounds;
     Lists lists;
-    const uint32_t* perm;  // list row / list entry -> input row, or null
+    const uint32_t* perm;  // list entry (candidate id) -> input reference row, or null
+    const uint32_t* qperm; // list row -> input query row, or null (a self solve: perm)
     const float* xs;       // working rows in list order (ordered solves), or null
     const float* xr_list;  // reference rows indexed by list entry (xs for a self solve)
     int ids_only;          // the lists hold ids only (collected below their thresholds): keep every entry
@@ -182,6 +183,10 @@ __device__ void push_fallback(const RerankArgs& a, int64_t slot) {
 __device__ __forceinline__ int64_t input_row(const RerankArgs& a, int64_t s) {
     return a.perm ? (int64_t)a.perm[s] : s;
 }
+// The input query row of list row `slot`.
+__device__ __forceinline__ int64_t query_row(const RerankArgs& a, int64_t slot) {
+    return a.qperm ? (int64_t)a.qperm[slot] : slot;
+}
 
 __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a) {
     extern __shared__ unsigned long long rr_smem[];
@@ -191,13 +196,13 @@ __global__ void __launch_bounds__(RR_WARPS * 32) rerank_warp_kernel(RerankArgs a
     unsigned long long* B = A + RC;
     uint8_t* flags = reinterpret_cast<uint8_t*>(rr_smem + (size_t)RR_WARPS * 2 * RC) + (size_t)warp * RC;
     const int64_t slot = (int64_t)blockIdx.x * RR_WARPS + warp;  // list row
-    if (slot >= a.nq || (a.perm && a.perm[slot] == 0xffffffffu)) return;
+    if (slot >= a.nq || (a.qperm && a.qperm[slot] == 0xffffffffu)) return;
     WarpTeam team;
     if (a.lists.overflow[slot]) {
         if (lane == 0) push_fallback(a, slot);
         return;
     }
-    const int64_t q = input_row(a, slot);
+    const int64_t q = query_row(a, slot);
     const int segs = a.lists.segments;
     int m0 = 0;
     for (int s = 0; s < segs; ++s) m0 += (int)min(a.lists.cnt[slot * segs + s], (uint32_t)a.lists.ctot);
@@ -311,7 +316,7 @@ __device__ int sorted_row(const RerankArgs& a, int64_t slot, unsigned long long*
     for (int p = m + lane; p < P; p += 32) keys[p] = ~0ull;
     __syncwarp();
     team_bitonic_sort(team, keys, P);
-    finalize_row(team, a, input_row(a, slot), keys, m, dbl, flags);
+    finalize_row(team, a, query_row(a, slot), keys, m, dbl, flags);
     return 0;
 }
 
@@ -476,7 +481,7 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
         ((unsigned long long)__ballot_sync(0xffffffffu, start[1]) << 32);
     const int k = a.k;
     const bool cosine = a.metric == SCRUST_METRIC_COSINE;
-    const int64_t q = input_row(a, slot);
+    const int64_t q = query_row(a, slot);
     // The common case: positions 0..k all start a group, so the first k are
     // singletons and the sort's order and FP32 values are final.
     if (!cosine && k < 63 && (S & ((2ull << k) - 1)) == ((2ull << k) - 1)) {
@@ -571,7 +576,7 @@ __global__ void __launch_bounds__(RS_WARPS * 32, 6) rerank_sorted_kernel(RerankA
     double* dbl = reinterpret_cast<double*>(keys + RS_KEYS);
     uint8_t* flags = reinterpret_cast<uint8_t*>(rs_smem + (size_t)RS_WARPS * 2 * RS_KEYS) + (size_t)warp * RS_KEYS;
     const int64_t slot = (int64_t)blockIdx.x * RS_WARPS + warp;
-    if (slot >= a.nq || (a.perm && a.perm[slot] == 0xffffffffu)) return;  // padding of a batch layout
+    if (slot >= a.nq || (a.qperm && a.qperm[slot] == 0xffffffffu)) return;  // padding of a batch layout
     int r = sorted_row_regs(a, slot, keys, dbl);
     if (r == 3) r = sorted_row<RS_KEYS>(a, slot, keys, dbl, flags);
     if (r && lane == 0) {
@@ -630,7 +635,7 @@ __global__ void __launch_bounds__(FB_THREADS) rerank_fallback_kernel(RerankArgs 
         const uint32_t row = row_s;
         __syncthreads();
         if (row == 0xffffffffu) break;
-        const int64_t q = input_row(a, row);
+        const int64_t q = query_row(a, row);
         // The columns of the row's own solve: [lo, hi) of the input rows.
         const int64_t lo = a.row_lo ? (int64_t)a.row_lo[q] : 0, hi = a.row_lo ? (int64_t)a.row_hi[q] : a.nr;
         for (int64_t j = tid; j < a.nr; j += blockDim.x)
@@ -719,7 +724,7 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
                           const float* rraw, const RowBounds& bounds, const Lists& lists,
                           const uint32_t* perm, const float* xs, const float* theta, uint32_t* out_idx,
                           float* out_dist, const uint32_t* row_lo, const uint32_t* row_hi, const float* xr_list,
-                          int xs_stride, bool ids_only) {
+                          int xs_stride, bool ids_only, const uint32_t* qperm) {
     cudaError_t e;
     uint32_t* fb_rows = (uint32_t*)ws_get(ctx, SLOT_FALLBACK_ROWS, sizeof(uint32_t) * (size_t)plan.nq, &e);
     if (!fb_rows) return e;
@@ -738,11 +743,15 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     a.bounds = bounds;
     a.lists = lists;
     a.perm = perm;
+    a.qperm = qperm ? qperm : perm;
     a.xs = xs;
     a.xr_list = xr_list ? xr_list : xs;
     a.xs_stride = xs_stride > 0 ? xs_stride : plan.d;
     a.ids_only = ids_only ? 1 : 0;
-    a.xs_v8 = !xr_list && xs && a.xs_stride % 8 == 0 && ((uintptr_t)xs & 31) == 0;
+    // 32-byte loads need rows padded to 8 floats on both sides: the lists'
+    // query rows and the reference rows the candidate ids index.
+    a.xs_v8 = xs && a.xs_stride % 8 == 0 && ((uintptr_t)xs & 31) == 0 && ((uintptr_t)a.xr_list & 31) == 0 &&
+              (!xr_list || a.xs_stride == padded_row_floats(plan.d));
     a.theta = theta;
     a.row_lo = row_lo;
     a.row_hi = row_hi;

@@ -6,10 +6,14 @@
 // stream and workspace.  Requests that arrive while other batches are on the
 // GPU are admitted as soon as a slot and budget free up, so batches on
 // different slots overlap on the device (continuous batching).  A solve is
-// the tensor-form sweep of the batch's rows against every atlas tile, the
-// exact rerank, and per-row directed connectivities (the rows of smooth_knn
-// and exp weights, no symmetrisation).  Every result is exact, so a request's
-// output does not depend on what it was batched with.
+// the tensor-form sweep of the batch's rows against the atlas, the exact
+// rerank, and per-row directed connectivities (the rows of smooth_knn and exp
+// weights, no symmetrisation).  For k <= 32 the atlas is ordered once when the
+// service starts, and a batch of at least kRoutedMinQueries rows is routed to
+// its cells: threshold passes over the tiles of their cells and neighbouring
+// cells and over the tiles the balls keep, then one collect pass (order.cu).
+// Every result is exact, so a request's output does not depend on what it was
+// batched with.
 #include <string.h>
 
 #include <algorithm>
@@ -93,6 +97,10 @@ struct scrust_server {
     double* means = nullptr;
     void* B16 = nullptr;
     uint32_t* words = nullptr;
+    // The atlas ordered once (k <= 32): queries are routed to its cells and
+    // sweep only the tiles that can hold their neighbours.
+    scrust::AtlasOrder order;
+    bool ordered = false;
     uint64_t budget = 0, atlas_bytes = 0, max_batch_cells = 0, bytes_per_cell = 0;
     std::vector<scrust::ServeSlot> slots;
     std::mutex mu;
@@ -111,6 +119,8 @@ namespace {
 
 size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+constexpr int64_t kRoutedMinQueries = 8192;
+
 // Query rows of one batch against the atlas, on the slot's stream.
 int32_t cross_enqueue(scrust_server* sv, scrust_context* ctx, const float* dq, int64_t q, uint32_t* d_idx,
                       float* d_dist, CsrBuffers* csr, scrust_status* st) {
@@ -123,7 +133,14 @@ int32_t cross_enqueue(scrust_server* sv, scrust_context* ctx, const float* dq, i
     ref.words = sv->words;
     ref.B16 = sv->B16;
     ref.bf16 = sv->bf16;
-    int32_t rc = cross_knn_enqueue(ctx, ref, dq, q, sv->k, -1, d_idx, d_dist, st);
+    // A routed solve runs one CTA per 256 queries over the tiles near them;
+    // a smaller batch fills the GPU better sweeping every tile in column
+    // segments (measured at 500k atlas cells: the routed solve wins from
+    // about 8k queries, 2x at 20k).
+    const bool routed = sv->ordered && q >= kRoutedMinQueries;
+    int32_t rc = routed ? cross_ordered_enqueue(ctx, sv->order, sv->atlas, sv->means, sv->words, dq, q, sv->k, d_idx,
+                                                d_dist, st)
+                        : cross_knn_enqueue(ctx, ref, dq, q, sv->k, -1, d_idx, d_dist, st);
     if (rc) return rc;
     return run_query_connectivities(ctx, d_idx, d_dist, q, sv->k, csr, st);
 }
@@ -319,6 +336,7 @@ void destroy_server(scrust_server* sv) {
         cudaFree(sl.csr.values);
         if (sl.ctx) scrust_cuda_context_destroy(sl.ctx);
     }
+    atlas_order_free(&sv->order);
     cudaFree(sv->atlas);
     cudaFree(sv->means);
     cudaFree(sv->B16);
@@ -412,6 +430,16 @@ scrust_server* scrust_serve_create(int32_t device, const float* atlas, uint64_t 
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         cudaFree(A16);
         cudaFree(tmp);
+        // The ordering the query solves route through (k <= 32, as the
+        // threshold pass needs; an atlas of fewer than 1024 cells is swept
+        // whole).
+        if (e == cudaSuccess && k <= 32 && m >= 1024) {
+            if (atlas_order_build(c0, sv->atlas, (int64_t)m, (int)d, sv->means, sv->words, sv->bf16, &sv->order, st)) {
+                destroy_server(sv);
+                return nullptr;
+            }
+            sv->ordered = true;
+        }
     }
     if (e != cudaSuccess) {
         cuda_fail(st, e, "serve: atlas");
@@ -422,6 +450,10 @@ scrust_server* scrust_serve_create(int32_t device, const float* atlas, uint64_t 
     // Budget: the atlas plus, per admitted cell, its lists, operands,
     // outputs and connectivities.
     sv->atlas_bytes = sizeof(float) * m * d + (size_t)sv->m_pad * 128 + sizeof(double) * d * (mean_blocks + 1);
+    if (sv->ordered)  // list-order operands and rows, the permutation, anchors and balls
+        sv->atlas_bytes += (size_t)sv->m_pad * 128 + sizeof(float) * m * padded_row_floats((int)d) + 4 * m +
+                           (size_t)sv->order.anchors_pad * 128 + 4 * (size_t)sv->order.anchors * (kAnchorNeighbours + 2) +
+                           4 * 66 * (size_t)sv->order.segs;
     sv->bytes_per_cell = (uint64_t)(2 * 16) * (std::max(64, (2 * (int)k + 32 + 31) / 32 * 32) + 128) * 8 + 512 +
                          (uint64_t)k * 24 + (uint64_t)d * 8;
     sv->budget = budget_bytes ? budget_bytes : (uint64_t)150 << 30;

@@ -98,3 +98,27 @@ def test_bad_requests_are_refused(world):
     _, _, sv = world
     with pytest.raises(ValueError):
         sv.submit(np.zeros((4, 29), np.float32))
+
+
+@pytest.mark.parametrize("q", [8192, 10000])
+def test_routed_batches_are_exact(built_library, oracle, q):
+    """Batches of at least 8192 queries are routed through the atlas ordered
+    once (cells, priority tiles, tile balls): exact all the same, including
+    queries that duplicate atlas cells and queries far from every cell."""
+    from mrustsc_gb300 import serving
+
+    atlas, centres = synthetic.serving_atlas(seed=5, m=40_000, d=30, clusters=20)
+    x = synthetic.serving_queries(centres, q, seed=q)
+    x[:40] = atlas[np.arange(40) * 997]          # exact copies of atlas cells
+    x[40:48] = 50.0 + np.arange(8)[:, None]      # far from every cell
+    with serving.Server(atlas, K, slots=1, max_batch_cells=65536) as sv:
+        idx, dist, (indptr, cols, vals), _ = sv.query(x)
+    oi, od, _ = oracle.knn_fp64_cross_c(x, atlas, K)
+    np.testing.assert_array_equal(idx, oi)
+    rel = np.abs(dist.astype(np.float64) - od) / np.maximum(od, 1e-30)
+    assert rel.max() <= 1e-6
+    assert np.all(dist[:40, 0] == 0)
+    ep, ec, ev = expected_rows(oracle, idx, dist)
+    np.testing.assert_array_equal(indptr, ep)
+    np.testing.assert_array_equal(cols, ec)
+    np.testing.assert_allclose(vals, ev, atol=1e-5, rtol=0)
