@@ -163,11 +163,14 @@ struct TileOrder {
         : list(nullptr), list2(nullptr), count(ct1_ - ct0_), count1(0), home(qt * ROWS / TBN), ct0(ct0_),
           ct1(ct1_) {
         if (a.tl) {
+            // An explicit list holds distinct column tiles from anywhere in
+            // the reference (a column segment's list is not confined to the
+            // segment's own range).
             list = a.tl + (a.tl_off ? (int64_t)a.tl_off[w] : (int64_t)w * a.tl_stride);
-            count = count1 = (int)min(a.tl_cnt[w], (uint32_t)(ct1_ - ct0_));
+            count = count1 = (int)min(a.tl_cnt[w], (uint32_t)a.col_tiles);
             if (TWO && a.tl2) {
                 list2 = a.tl2 + (int64_t)w * a.tl2_stride;
-                count += (int)min(a.tl2_cnt[w], (uint32_t)(ct1_ - ct0_ - count1));
+                count += (int)min(a.tl2_cnt[w], (uint32_t)(a.col_tiles - count1));
             }
         }
     }
@@ -762,7 +765,9 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (valid) bnd = TensorBound{a.bA[row], a.bdelta[row], a.beps2[row]};
             const int64_t lslot = (row * col_segs + seg) * PARTS + part;
             if (valid && collect) {
-                // One column segment: the row's lists are lslot and lslot ^ 1.
+                // The row's lists in this column segment are lslot and
+                // lslot ^ 1; other segments' thresholds arrive through
+                // row_theta below.
                 th = fminf(a.theta_io[lslot], a.theta_io[lslot ^ 1]);
                 if (a.resume) cnt = min(a.lists.cnt[lslot], (uint32_t)cap);
             } else if (valid && a.resume) {
@@ -1312,8 +1317,10 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     if (tiles && !tiles->tiles) a.item_order = tiles->order;
     if (a.item_range && lists.segments != PARTS) return cudaErrorInvalidValue;
     if (tiles && tiles->tiles) {
-        // Explicit tile lists are per row block: one column segment only.
-        if (col_segs != 1 || !tiles->count) return cudaErrorInvalidValue;
+        // Explicit tile lists are per work item (row block and column
+        // segment); several segments of a row block must share its threshold
+        // through row_theta.
+        if ((col_segs != 1 && !tiles->row_theta) || !tiles->count) return cudaErrorInvalidValue;
         a.tl = tiles->tiles;
         a.tl_off = tiles->offset;
         a.tl_cnt = tiles->count;
@@ -1330,7 +1337,9 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.theta_io = theta_io;
     a.thr_only = pass_mode == kPassThresholds ? 1 : 0;
     a.collect = pass_mode == kPassCollect ? 1 : 0;
-    if ((a.thr_only || a.collect) && (!theta_io || plan.k > 32 || lists.segments != PARTS))
+    // Threshold and collect passes keep one column segment per row, or share
+    // the row's threshold between its segments through row_theta.
+    if ((a.thr_only || a.collect) && (!theta_io || plan.k > 32 || (lists.segments != PARTS && !a.row_theta)))
         return cudaErrorInvalidValue;
     a.argmin_out = argmin_out;
     if (argmin_out && (plan.k != 1 || resume)) return cudaErrorInvalidValue;

@@ -740,6 +740,37 @@ __global__ void __launch_bounds__(256) query_prio_kernel(const uint32_t* __restr
     }
 }
 
+// A row block's tile list cut into `segs` contiguous chunks of equal size,
+// one per column segment, so that each segment of a row block is its own
+// work item: dst row (block * segs + segment), `dst_stride` entries apart.
+// Contiguous, not dealt round robin: the list starts with the tiles nearest
+// the block, and one segment that sees them all finds a threshold near the
+// rows' k-th distance, which the others then share; tiles dealt out one by
+// one would leave every segment's own k-th smallest far out.  One block per
+// row block.
+__global__ void split_lists_kernel(const uint32_t* __restrict__ src, int src_stride, const uint32_t* __restrict__ cnt,
+                                   int segs, uint32_t* __restrict__ dst, int dst_stride,
+                                   uint32_t* __restrict__ dst_cnt) {
+    const int I = blockIdx.x;
+    const int c = (int)min(cnt[I], (uint32_t)src_stride);
+    const int chunk = (c + segs - 1) / segs;  // <= dst_stride = ceil(src_stride / segs)
+    for (int t = threadIdx.x; t < c; t += blockDim.x)
+        dst[((int64_t)I * segs + t / chunk) * dst_stride + t % chunk] = src[(int64_t)I * src_stride + t];
+    if (threadIdx.x < segs)
+        dst_cnt[(int64_t)I * segs + threadIdx.x] = (uint32_t)max(0, min(chunk, c - (int)threadIdx.x * chunk));
+}
+
+// Per row, its shared threshold as both part thresholds (the layout the
+// tile balls read).
+__global__ void row_theta_pairs_kernel(const uint32_t* __restrict__ row_theta, int64_t n, float* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = row_theta[i];
+    const float t = k == 0xffffffffu ? __int_as_float(0x7f800000) : key_float(k);  // none yet: reach everything
+    out[2 * i] = t;
+    out[2 * i + 1] = t;
+}
+
 __global__ void gather_rows_kernel(const float* __restrict__ x, const uint32_t* __restrict__ perm, int64_t n, int d,
                                    int stride, float* __restrict__ xs) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1192,6 +1223,16 @@ int32_t cross_ordered_enqueue(scrust_context* ctx, const AtlasOrder& at, const f
     const bool bf16 = at.bf16;
     const int64_t q_pad = (q + 255) / 256 * 256;
     const int items = (int)(q_pad / 256), col_tiles = (int)(at.m_pad / 256), words_t = (col_tiles + 31) / 32;
+    // Column segments per row block, so that a small batch still fills the
+    // GPU: each segment of a block is its own work item, and the segments of
+    // a row share its threshold through HBM.
+    // (At most 16: the rerank reads up to 32 lists of a row in registers;
+    // and a count the sweep's segment split reproduces.)
+    int csegs = std::max(1, std::min({16, col_tiles, (2 * ctx->sm_count + items - 1) / items}));
+    while (csegs > 1 && (col_tiles + (col_tiles + csegs - 1) / csegs - 1) / ((col_tiles + csegs - 1) / csegs) != csegs)
+        csegs--;
+    const int work = items * csegs;
+    const int ps = (kQueryPrio + csegs - 1) / csegs, es = (col_tiles + csegs - 1) / csegs;
     const int P = padded_row_floats(d);
     const int nblocks = radix_blocks(q);
     const int64_t smax = (int64_t)items * kSegMax;
@@ -1209,12 +1250,14 @@ int32_t cross_ordered_enqueue(scrust_context* ctx, const AtlasOrder& at, const f
                  o_vA = take(8 * (size_t)q), o_vB = take(8 * (size_t)q), o_qp = take(4 * (size_t)q),
                  o_cell = take(4 * (size_t)q), o_cc = take(4 * ((size_t)at.anchors + 1)),
                  o_xs = take(4 * (size_t)q * P), o_prio = take(4 * (size_t)items * kQueryPrio),
-                 o_pc = take(4 * (size_t)items), o_po = take(4 * (size_t)items), o_po2 = take(4 * (size_t)items),
-                 o_ws = take(work_order_scratch(items)),
-                 o_th = take(4 * 2 * (size_t)q_pad), o_so = take(4 * ((size_t)items + 1)),
+                 o_pc = take(4 * (size_t)items), o_ps = take(4 * (size_t)work * ps), o_psc = take(4 * (size_t)work),
+                 o_po = take(4 * (size_t)work), o_po2 = take(4 * (size_t)work), o_ws = take(work_order_scratch(work)),
+                 o_rt = take(4 * (size_t)q_pad), o_th = take(4 * 2 * (size_t)csegs * q_pad),
+                 o_th2 = take(4 * 2 * (size_t)q_pad), o_so = take(4 * ((size_t)items + 1)),
                  o_fc = take(4 * 64 * (size_t)smax), o_fr = take(4 * (size_t)smax), o_fu = take(4 * (size_t)smax),
                  o_fo = take(4 * (size_t)smax), o_bm = take(4 * (size_t)items * words_t),
                  o_cnt = take(4 * ((size_t)items + 1)), o_ent = take(4 * (size_t)items * col_tiles),
+                 o_es = take(4 * (size_t)work * es), o_esc = take(4 * (size_t)work),
                  o_hist = take(4 * ((size_t)256 * nblocks + 16)), o_scan = take(4 * scan_elems);
     TileBalls qballs;
     const size_t total = carve_balls(nullptr, off, items, d, &qballs);
@@ -1230,8 +1273,9 @@ int32_t cross_ordered_enqueue(scrust_context* ctx, const AtlasOrder& at, const f
     uint32_t* cell_of_pos = (uint32_t*)(base + o_cell);
     uint32_t* prio = (uint32_t*)(base + o_prio);
     uint32_t* prio_cnt = (uint32_t*)(base + o_pc);
-    uint32_t* prio_order = (uint32_t*)(base + o_po);
+    uint32_t* row_theta = (uint32_t*)(base + o_rt);
     float* theta = (float*)(base + o_th);
+    float* theta2 = (float*)(base + o_th2);
     float* xs = (float*)(base + o_xs);
     uint32_t* seg_off = (uint32_t*)(base + o_so);
     uint32_t* bitmap = (uint32_t*)(base + o_bm);
@@ -1287,15 +1331,18 @@ int32_t cross_ordered_enqueue(scrust_context* ctx, const AtlasOrder& at, const f
         (e = launch_tensor_bounds(q, bA, beps, words + 1, words + 2, bdelta, beps2, s)) != cudaSuccess ||
         (e = launch_gather_rows(dq, qperm, q, d, P, xs, s)) != cudaSuccess)
         return cuda_fail(st, e, "query routing: gather");
+    // Priority tiles per row block, dealt over its column segments.
     const size_t prio_smem = 8 * (size_t)words_t;
     if ((e = set_smem_limit(ctx, (const void*)query_prio_kernel, (int)prio_smem)) != cudaSuccess)
         return cuda_fail(st, e, "query routing: priority tiles");
     query_prio_kernel<<<items, 256, prio_smem, s>>>(cell_of_pos, q, at.cell_start, (int)at.anchors, at.cell_nb,
                                                     col_tiles, prio, prio_cnt);
+    split_lists_kernel<<<items, 256, 0, s>>>(prio, kQueryPrio, prio_cnt, csegs, (uint32_t*)(base + o_ps), ps,
+                                             (uint32_t*)(base + o_psc));
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "query routing: priority tiles");
-    if ((e = sort_by_work(ctx, prio_cnt, items, base + o_ws, prio_order)) != cudaSuccess)
+    if ((e = sort_by_work(ctx, (uint32_t*)(base + o_psc), work, base + o_ws, (uint32_t*)(base + o_po))) != cudaSuccess)
         return cuda_fail(st, e, "query routing: work order");
-    ctx->launches += 5;
+    ctx->launches += 7;
 
     // The threshold pass over the priority tiles.
     KnnPlan plan;
@@ -1309,30 +1356,34 @@ int32_t cross_ordered_enqueue(scrust_context* ctx, const AtlasOrder& at, const f
     Lists lists;
     lists.cap = 256;
     lists.ctot = 256 + 128;
-    lists.segments = 2;
+    lists.segments = 2 * csegs;
     int32_t rc = alloc_lists(ctx, q_pad, &lists, st);
     if (rc) return rc;
     plan.cap = lists.cap;
     plan.ctot = lists.ctot;
     plan.segments = lists.segments;
     TileLists first;
-    first.tiles = prio;
-    first.count = prio_cnt;
-    first.stride = kQueryPrio;
-    first.order = prio_order;
-    // A row the pass leaves without a threshold (a block with no priority
-    // tile) keeps a huge one: every tile stays in its second list.
-    if ((e = cudaMemsetAsync(theta, 0x7f, 4 * 2 * (size_t)q_pad, s)) != cudaSuccess)
+    first.tiles = (const uint32_t*)(base + o_ps);
+    first.count = (const uint32_t*)(base + o_psc);
+    first.stride = ps;
+    first.order = (const uint32_t*)(base + o_po);
+    first.row_theta = row_theta;
+    // A list the pass leaves without a threshold (a segment with no tile)
+    // keeps a huge one; a row without any keeps reach everywhere.
+    if ((e = cudaMemsetAsync(theta, 0x7f, 4 * 2 * (size_t)csegs * q_pad, s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(row_theta, 0xff, 4 * (size_t)q_pad, s)) != cudaSuccess)
         return cuda_fail(st, e, "query knn: memset");
     if ((e = launch_tensor_candidates(ctx, plan, base + o_As, q_pad, at.B16, at.m_pad, bA, bdelta, beps2, lists, bf16,
                                       &first, false, theta, nullptr, nullptr, nullptr, kPassThresholds)) != cudaSuccess)
         return cuda_fail(st, e, "query knn: threshold pass");
-    // The atlas tiles each query block cannot rule out: query-block segment
-    // balls (reach from the thresholds) against the atlas segment balls.
+    // The atlas tiles each row block cannot rule out: its segment balls
+    // (reach from the rows' shared thresholds) against the atlas segment
+    // balls.
+    row_theta_pairs_kernel<<<(unsigned)((q + 255) / 256), 256, 0, s>>>(row_theta, q, theta2);
     if ((e = cudaMemsetAsync(qballs.nseg + items, 0, sizeof(uint32_t), s)) != cudaSuccess ||
         (e = cudaMemsetAsync(bitmap, 0, 4 * (size_t)items * words_t, s)) != cudaSuccess)
         return cuda_fail(st, e, "query knn: memset");
-    launch_tile_balls(bf16, base + o_As, q, d, items, cell_of_pos, theta, bA, bdelta, qballs, s);
+    launch_tile_balls(bf16, base + o_As, q, d, items, cell_of_pos, theta2, bA, bdelta, qballs, s);
     if ((e = cudaGetLastError()) != cudaSuccess ||
         (e = device_exclusive_scan(ctx, qballs.nseg, seg_off, (int64_t)items + 1, (uint32_t*)(base + o_scan),
                                    scan_elems)) != cudaSuccess)
@@ -1350,17 +1401,20 @@ int32_t cross_ordered_enqueue(scrust_context* ctx, const AtlasOrder& at, const f
         return cuda_fail(st, e, "query knn: tile lists");
     tile_lists_kernel<<<items, 256, lists_smem, s>>>(bitmap, words_t, col_tiles, prio, prio_cnt, counts, entries,
                                                      kQueryPrio);
+    split_lists_kernel<<<items, 256, 0, s>>>(entries, col_tiles, counts, csegs, (uint32_t*)(base + o_es), es,
+                                             (uint32_t*)(base + o_esc));
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "query knn: tile lists");
-    ctx->launches += 6;
+    ctx->launches += 7;
     // The thresholds tightened over the kept tiles too: a query's neighbours
     // spread over its cluster, so a block whose queries fall in many cells
     // leaves the first pass with loose thresholds, and collecting at those
     // would overflow the lists.
     TileLists second;
-    second.tiles = entries;
-    second.count = counts;
-    second.stride = col_tiles;
-    if ((e = sort_by_work(ctx, counts, items, base + o_ws, (uint32_t*)(base + o_po2))) != cudaSuccess)
+    second.tiles = (const uint32_t*)(base + o_es);
+    second.count = (const uint32_t*)(base + o_esc);
+    second.stride = es;
+    second.row_theta = row_theta;
+    if ((e = sort_by_work(ctx, (uint32_t*)(base + o_esc), work, base + o_ws, (uint32_t*)(base + o_po2))) != cudaSuccess)
         return cuda_fail(st, e, "query knn: work order");
     second.order = (const uint32_t*)(base + o_po2);
     if ((e = launch_tensor_candidates(ctx, plan, base + o_As, q_pad, at.B16, at.m_pad, bA, bdelta, beps2, lists, bf16,
@@ -1368,9 +1422,9 @@ int32_t cross_ordered_enqueue(scrust_context* ctx, const AtlasOrder& at, const f
         return cuda_fail(st, e, "query knn: second threshold pass");
     // One collect pass over both lists, then the exact finish.
     TileLists both = first;
-    both.tiles2 = entries;
-    both.count2 = counts;
-    both.stride2 = col_tiles;
+    both.tiles2 = second.tiles;
+    both.count2 = second.count;
+    both.stride2 = es;
     if ((e = launch_tensor_candidates(ctx, plan, base + o_As, q_pad, at.B16, at.m_pad, bA, bdelta, beps2, lists, bf16,
                                       &both, false, theta, nullptr, nullptr, nullptr, kPassCollect)) != cudaSuccess)
         return cuda_fail(st, e, "query knn: collect pass");
@@ -1382,7 +1436,7 @@ int32_t cross_ordered_enqueue(scrust_context* ctx, const AtlasOrder& at, const f
                            lists, at.perm, xs, theta, d_idx, d_dist, nullptr, nullptr, at.rows, P, true, qperm)) !=
         cudaSuccess)
         return cuda_fail(st, e, "query knn: rerank");
-    ctx->launches += 2;
+    ctx->launches += 3;
     return ok(st);
 }
 

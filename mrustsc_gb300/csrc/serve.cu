@@ -9,11 +9,13 @@
 // the tensor-form sweep of the batch's rows against the atlas, the exact
 // rerank, and per-row directed connectivities (the rows of smooth_knn and exp
 // weights, no symmetrisation).  For k <= 32 the atlas is ordered once when the
-// service starts, and a batch of at least kRoutedMinQueries rows is routed to
-// its cells: threshold passes over the tiles of their cells and neighbouring
-// cells and over the tiles the balls keep, then one collect pass (order.cu).
+// service starts, and every batch is routed to its cells: threshold passes
+// over the tiles of their cells and neighbouring cells and over the tiles the
+// balls keep, then one collect pass, each row block's tiles split over column
+// segments that share its rows' thresholds (order.cu).
 // Every result is exact, so a request's output does not depend on what it was
 // batched with.
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -101,6 +103,7 @@ struct scrust_server {
     // sweep only the tiles that can hold their neighbours.
     scrust::AtlasOrder order;
     bool ordered = false;
+    int64_t routed_min = 0;  // batches of at least this many rows are routed
     uint64_t budget = 0, atlas_bytes = 0, max_batch_cells = 0, bytes_per_cell = 0;
     std::vector<scrust::ServeSlot> slots;
     std::mutex mu;
@@ -119,7 +122,7 @@ namespace {
 
 size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-constexpr int64_t kRoutedMinQueries = 8192;
+constexpr int64_t kRoutedMinQueries = 1;
 
 // Query rows of one batch against the atlas, on the slot's stream.
 int32_t cross_enqueue(scrust_server* sv, scrust_context* ctx, const float* dq, int64_t q, uint32_t* d_idx,
@@ -133,11 +136,11 @@ int32_t cross_enqueue(scrust_server* sv, scrust_context* ctx, const float* dq, i
     ref.words = sv->words;
     ref.B16 = sv->B16;
     ref.bf16 = sv->bf16;
-    // A routed solve runs one CTA per 256 queries over the tiles near them;
-    // a smaller batch fills the GPU better sweeping every tile in column
-    // segments (measured at 500k atlas cells: the routed solve wins from
-    // about 8k queries, 2x at 20k).
-    const bool routed = sv->ordered && q >= kRoutedMinQueries;
+    // A routed solve visits only the tiles near the batch's rows (measured
+    // at 500k atlas cells: 0.6 ms against 0.8 ms for one query, 1.3 against
+    // 2.0 ms for 1000, 4.9 against 14.3 ms for 20,000); the sweep of every
+    // tile stays for unordered atlases.
+    const bool routed = sv->ordered && q >= sv->routed_min;
     int32_t rc = routed ? cross_ordered_enqueue(ctx, sv->order, sv->atlas, sv->means, sv->words, dq, q, sv->k, d_idx,
                                                 d_dist, st)
                         : cross_knn_enqueue(ctx, ref, dq, q, sv->k, -1, d_idx, d_dist, st);
@@ -439,6 +442,14 @@ scrust_server* scrust_serve_create(int32_t device, const float* atlas, uint64_t 
                 return nullptr;
             }
             sv->ordered = true;
+            // SCRUST_ROUTED_MIN_QUERIES moves the batch size from which
+            // queries are routed (a tuning knob; every result is exact
+            // either way).
+            sv->routed_min = kRoutedMinQueries;
+            if (const char* v = getenv("SCRUST_ROUTED_MIN_QUERIES")) {
+                const long long r = atoll(v);
+                if (r > 0) sv->routed_min = r;
+            }
         }
     }
     if (e != cudaSuccess) {

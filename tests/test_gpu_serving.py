@@ -20,13 +20,26 @@ pytestmark = pytest.mark.gpu
 K = 15
 
 
-@pytest.fixture(scope="module")
-def world(built_library):
+@pytest.fixture(scope="module", params=["routed", "swept"])
+def world(built_library, request):
+    """A service over a 20k-cell atlas, its batches routed to the atlas cells
+    (the default) or swept over every atlas tile."""
+    import os
+
     from mrustsc_gb300 import _scrust, serving
 
     assert _scrust.gpu_available(), "these tests need an sm_103a GPU"
     atlas, centres = synthetic.serving_atlas(seed=3, m=20_000, d=30, clusters=12)
-    sv = serving.Server(atlas, K, slots=2, max_batch_cells=4096)
+    old = os.environ.get("SCRUST_ROUTED_MIN_QUERIES")
+    if request.param == "swept":
+        os.environ["SCRUST_ROUTED_MIN_QUERIES"] = str(1 << 40)
+    try:
+        sv = serving.Server(atlas, K, slots=2, max_batch_cells=4096)
+    finally:
+        if old is None:
+            os.environ.pop("SCRUST_ROUTED_MIN_QUERIES", None)
+        else:
+            os.environ["SCRUST_ROUTED_MIN_QUERIES"] = old
     yield atlas, centres, sv
     sv.close()
 
@@ -100,24 +113,27 @@ def test_bad_requests_are_refused(world):
         sv.submit(np.zeros((4, 29), np.float32))
 
 
-@pytest.mark.parametrize("q", [8192, 10000])
+@pytest.mark.parametrize("q", [1, 300, 2500, 8192, 10000])
 def test_routed_batches_are_exact(built_library, oracle, q):
-    """Batches of at least 8192 queries are routed through the atlas ordered
-    once (cells, priority tiles, tile balls): exact all the same, including
-    queries that duplicate atlas cells and queries far from every cell."""
+    """Batches are routed through the atlas ordered once (cells, priority
+    tiles, tile balls; each row block's tiles split over column segments that
+    share its rows' thresholds): exact all the same, including queries that
+    duplicate atlas cells and queries far from every cell."""
     from mrustsc_gb300 import serving
 
     atlas, centres = synthetic.serving_atlas(seed=5, m=40_000, d=30, clusters=20)
     x = synthetic.serving_queries(centres, q, seed=q)
-    x[:40] = atlas[np.arange(40) * 997]          # exact copies of atlas cells
-    x[40:48] = 50.0 + np.arange(8)[:, None]      # far from every cell
+    dup = min(40, q)
+    x[:dup] = atlas[np.arange(dup) * 997]        # exact copies of atlas cells
+    if q > 48:
+        x[40:48] = 50.0 + np.arange(8)[:, None]  # far from every cell
     with serving.Server(atlas, K, slots=1, max_batch_cells=65536) as sv:
         idx, dist, (indptr, cols, vals), _ = sv.query(x)
     oi, od, _ = oracle.knn_fp64_cross_c(x, atlas, K)
     np.testing.assert_array_equal(idx, oi)
     rel = np.abs(dist.astype(np.float64) - od) / np.maximum(od, 1e-30)
     assert rel.max() <= 1e-6
-    assert np.all(dist[:40, 0] == 0)
+    assert np.all(dist[:dup, 0] == 0)
     ep, ec, ev = expected_rows(oracle, idx, dist)
     np.testing.assert_array_equal(indptr, ep)
     np.testing.assert_array_equal(cols, ec)
