@@ -214,6 +214,29 @@ __device__ __forceinline__ float min32(const uint32_t (&v)[32]) {
     return fminf(min3f(a, b, c), d);
 }
 
+// The columns of a 32-column chunk below th, as a mask in an interleaved bit
+// order (below_col decodes it).  Each difference v - th is formed on the FMA
+// pipe; a byte permute replicates the signs of two differences into bytes,
+// and one logic op merges them into the mask: 32 ALU-pipe instructions a
+// chunk where a compare and a select per column take 64.  v < th exactly
+// when v - th is negative (the difference of two distinct floats is never
+// zero).
+__device__ __forceinline__ uint32_t below_mask(const uint32_t (&v)[32], float th) {
+    uint32_t acc = 0;
+#pragma unroll
+    for (int p = 0; p < 16; ++p) {
+        const uint32_t d0 = __float_as_uint(__fsub_rn(f_of(v[2 * p]), th));
+        const uint32_t d1 = __float_as_uint(__fsub_rn(f_of(v[2 * p + 1]), th));
+        uint32_t y;  // bytes: sign(d0), sign(d1), sign(d0), sign(d1), each 0x00 or 0xff
+        asm("prmt.b32 %0, %1, %2, 0xFBFB;" : "=r"(y) : "r"(d0), "r"(d1));
+        acc |= y & ((0x0101u << (p & 7)) << (p >= 8 ? 16 : 0));
+    }
+    return acc;
+}
+// The chunk column of bit b of a below_mask: column 2p + i sits in byte
+// i + 2 (p / 8), bit p % 8.
+__device__ __forceinline__ int below_col(int b) { return 2 * ((b & 7) | ((b >> 4) << 3)) + ((b >> 3) & 1); }
+
 // Appends the columns of one 32-column chunk that pass the row's threshold.
 // `valid` masks out columns past the reference rows and the row itself.  The
 // survivors' slots come from prefix popcounts of the mask, so the stores are
@@ -815,18 +838,14 @@ __global__ void __launch_bounds__(THREADS, 1)
                         for (int c = 0; c < 4; ++c) {
                             tmem_ld32(tbase + 32 * c, va);
                             tmem_ld_wait(va);
-                            cm[c] = min32(va);
-                            if (__any_sync(0xffffffffu, cm[c] < th)) {
-                                uint32_t mask = 0;
-#pragma unroll
-                                for (int j = 0; j < 32; j++) mask |= (f_of(va[j]) < th) ? (1u << j) : 0u;
-                                mask &= chunk_valid(col0 + 32 * c, a.nr, a.self != 0, row + a.self_offset);
-                                while (mask) {
-                                    const int j = __ffs(mask) - 1;
-                                    mask &= mask - 1;
-                                    ids[cnt] = (uint32_t)(col0 + 32 * c + j);  // ids only: no values
-                                    cnt++;
-                                }
+                            uint32_t mask = below_mask(va, th);
+                            const int64_t cb = col0 + 32 * c;
+                            while (mask) {
+                                const int64_t col = cb + below_col(__ffs(mask) - 1);
+                                mask &= mask - 1;
+                                // Not past the reference rows, not the row itself.
+                                if (col < a.nr && !(a.self && col == row + a.self_offset))
+                                    ids[cnt++] = (uint32_t)col;  // ids only: no values
                             }
                         }
                     } else if constexpr (PASS == 3) {
