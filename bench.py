@@ -470,12 +470,14 @@ def run_ours(args):
         dh = torch.empty((n, k), dtype=torch.float32).pin_memory()
         e2e_steps = max(1, args.steps)
         nnz_e = 0
-        # One untimed call first: it sizes the device workspaces and the
-        # pinned pool, as the warm-up steps do for the device-resident timing.
-        out = ctypes.c_void_p()
-        _lib.check(L.scrust_cuda_neighbors_graph(ctx, xh.data_ptr(), n, d, k, ctypes.byref(opts), ih.data_ptr(),
-                                                 dh.data_ptr(), ctypes.byref(out), ctypes.byref(st)), st)
-        L.scrust_csr_free(out)
+        # W untimed calls first (at least one): they size the device
+        # workspaces and the pinned pool, as the warm-up steps do for the
+        # device-resident timing.
+        for _ in range(max(1, args.warmup)):
+            out = ctypes.c_void_p()
+            _lib.check(L.scrust_cuda_neighbors_graph(ctx, xh.data_ptr(), n, d, k, ctypes.byref(opts), ih.data_ptr(),
+                                                     dh.data_ptr(), ctypes.byref(out), ctypes.byref(st)), st)
+            L.scrust_csr_free(out)
         times = []
         for _ in range(e2e_steps):
             t0 = time.perf_counter()

@@ -525,12 +525,15 @@ void return_csr_buffers(scrust_context* ctx, const CsrBuffers& b) {
 
 // `distinct_rows`: the graph is one this library's kNN built (every row's ids
 // distinct), which the faster bucket transpose relies on.
+// `ranges`: run the union in row ranges for a streamed download (see
+// CsrStream); *streamed says whether it did.
 int32_t conn_device_impl(scrust_context* ctx, const uint32_t* idx, const float* dist, uint64_t n, uint32_t k,
-                         bool validate, scrust_csr** out, scrust_status* st, bool distinct_rows = false) {
+                         bool validate, scrust_csr** out, scrust_status* st, bool distinct_rows = false,
+                         bool ranges = false, bool* streamed = nullptr) {
     CsrBuffers b;
     int32_t rc = take_csr_buffers(ctx, n, 2 * n * (uint64_t)k, &b, st);
     if (rc) return rc;
-    rc = run_connectivities(ctx, idx, dist, (int64_t)n, (int)k, validate, &b, st, distinct_rows);
+    rc = run_connectivities(ctx, idx, dist, (int64_t)n, (int)k, validate, &b, st, distinct_rows, ranges, streamed);
     mark(ctx, PH_CONN);
     if (rc) {
         ctx->csr_pool.push_back(b);
@@ -641,6 +644,67 @@ int32_t csr_to_host(scrust_context* ctx, scrust_csr* dev, scrust_csr** out, scru
 
 }  // namespace
 
+// csr_to_host for a CSR built in ctx->csr_stream's row ranges: the host slab
+// is sized by the CSR's capacity, and as each range is placed (its event;
+// its end offset is then in h_bounds) its rows and entries are queued on the
+// copy stream, so the link carries the early ranges while the later ones
+// merge.  Synchronises the copy stream.
+int32_t csr_to_host_streamed(scrust_context* ctx, scrust_csr* dev, scrust_csr** out, scrust_status* st) {
+    CsrStream& cs = ctx->csr_stream;
+    scrust_csr* h = new (std::nothrow) scrust_csr;
+    if (!h) return fail(st, SCRUST_OOM, "host allocation failed");
+    const uint64_t n = dev->n_rows;
+    const size_t cap = dev->buf.nnz_cap;
+    const size_t ip_bytes = sizeof(uint32_t) * (n + 1);
+    const size_t off_idx = (ip_bytes + 255) & ~(size_t)255;
+    const size_t off_val = off_idx + ((sizeof(uint32_t) * cap + 255) & ~(size_t)255);
+    const size_t bytes = off_val + sizeof(float) * cap;
+    h->pinned = pinned_take(bytes, &h->pinned_bytes);
+    if (!h->pinned) {
+        delete h;
+        return fail(st, SCRUST_OOM, "pinned host allocation of %zu bytes failed", bytes);
+    }
+    h->p_indptr = reinterpret_cast<uint32_t*>(h->pinned);
+    h->p_indices = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(h->pinned) + off_idx);
+    h->p_values = reinterpret_cast<float*>(reinterpret_cast<char*>(h->pinned) + off_val);
+    h->n_rows = n;
+    h->n_cols = dev->n_cols;
+    h->on_device = 0;
+    cudaStream_t c = ctx->copy_stream;
+    cudaError_t e = cudaSuccess;
+    uint32_t lo = 0;
+    for (int r = 0; r < kCsrRanges && e == cudaSuccess; ++r) {
+        if ((e = cudaEventSynchronize(cs.merged[r])) != cudaSuccess) break;
+        const uint32_t hi = cs.h_bounds[r];
+        if (hi < lo || hi > cap) {
+            e = cudaErrorIllegalState;
+            break;
+        }
+        const uint64_t r0 = n * r / kCsrRanges, r1 = n * (r + 1) / kCsrRanges;
+        if ((e = cudaStreamWaitEvent(c, cs.merged[r], 0)) != cudaSuccess) break;
+        // Rows r0..r1 (indptr[r1] is the next range's first offset, final now).
+        e = cudaMemcpyAsync(h->p_indptr + r0, dev->buf.indptr + r0, sizeof(uint32_t) * (r1 - r0 + 1),
+                            cudaMemcpyDeviceToHost, c);
+        if (e == cudaSuccess && hi > lo)
+            e = cudaMemcpyAsync(h->p_indices + lo, dev->buf.indices + lo, sizeof(uint32_t) * (hi - lo),
+                                cudaMemcpyDeviceToHost, c);
+        if (e == cudaSuccess && hi > lo)
+            e = cudaMemcpyAsync(h->p_values + lo, dev->buf.values + lo, sizeof(float) * (hi - lo),
+                                cudaMemcpyDeviceToHost, c);
+        lo = hi;
+    }
+    h->nnz = lo;
+    const cudaError_t es = cudaStreamSynchronize(c);
+    if (e == cudaSuccess) e = es;
+    if (e != cudaSuccess) {
+        pinned_give(h->pinned, h->pinned_bytes);
+        delete h;
+        return cuda_fail(st, e, "csr readback");
+    }
+    *out = h;
+    return ok(st);
+}
+
 int32_t csr_take(scrust_context* ctx, uint64_t rows, uint64_t nnz_cap, CsrBuffers* out, scrust_status* st) {
     return take_csr_buffers(ctx, rows, nnz_cap, out, st);
 }
@@ -723,6 +787,9 @@ scrust_context* scrust_cuda_context_create(int32_t device, scrust_status* st) {
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->copy_ev, cudaEventDisableTiming);
+    for (int i = 0; i < kCsrRanges && e == cudaSuccess; i++)
+        e = cudaEventCreateWithFlags(&ctx->csr_stream.merged[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->csr_stream.h_bounds, sizeof(uint32_t) * (kCsrRanges + 1));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int) * DERR_COUNT);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, sizeof(uint32_t) * 16);
     if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(int) * DERR_COUNT);
@@ -756,8 +823,11 @@ void scrust_cuda_context_destroy(scrust_context* ctx) {
         cudaFree(b.indices);
         cudaFree(b.values);
     }
-    for (int i = 0; i < 7; i++)
+    for (int i = 0; i < PH_COUNT; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    for (int i = 0; i < kCsrRanges; i++)
+        if (ctx->csr_stream.merged[i]) cudaEventDestroy(ctx->csr_stream.merged[i]);
+    if (ctx->csr_stream.h_bounds) cudaFreeHost(ctx->csr_stream.h_bounds);
     if (ctx->copy_stream) {
         cudaStreamSynchronize(ctx->copy_stream);
         cudaStreamDestroy(ctx->copy_stream);
@@ -928,11 +998,12 @@ int32_t scrust_cuda_neighbors_graph(scrust_context* ctx, const float* x, uint64_
         return cuda_fail(st, e, "download");
     }
     scrust_csr* dev = nullptr;
-    if ((rc = conn_device_impl(ctx, di, dd, n, k, false, &dev, st, true))) {
+    bool streamed = false;
+    if ((rc = conn_device_impl(ctx, di, dd, n, k, false, &dev, st, true, true, &streamed))) {
         cudaStreamSynchronize(ctx->copy_stream);
         return rc;
     }
-    rc = csr_to_host(ctx, dev, conn, st);
+    rc = streamed ? csr_to_host_streamed(ctx, dev, conn, st) : csr_to_host(ctx, dev, conn, st);
     ctx->csr_pool.push_back(dev->buf);
     delete dev;
     if ((e = cudaStreamSynchronize(ctx->copy_stream)) != cudaSuccess) {

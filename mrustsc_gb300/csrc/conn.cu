@@ -366,7 +366,7 @@ __device__ void warp_sort_bucket(unsigned long long* v, uint32_t len) {
 // at i * k + start[i] (room for k + nb entries) and its length to rowcnt[i];
 // merge_place_kernel then copies the runs into the CSR.  Rows with more than
 // 64 entries in all sort their bucket in place and place every entry by
-// binary search.
+// binary search.  Rows [r0, r1) only.
 __device__ __forceinline__ uint32_t mask_below(int c) { return c >= 32 ? 0xffffffffu : ((1u << c) - 1u); }
 
 template <int P>
@@ -469,12 +469,12 @@ __global__ void __launch_bounds__(256) merge_union_kernel(const uint32_t* __rest
                                                           const float* __restrict__ dw,
                                                           const uint32_t* __restrict__ dcnt,
                                                           unsigned long long* __restrict__ tval,
-                                                          const uint32_t* __restrict__ tstart, int64_t n, int k,
-                                                          uint32_t* __restrict__ scol, float* __restrict__ sval,
+                                                          const uint32_t* __restrict__ tstart, int64_t r0, int64_t r1,
+                                                          int k, uint32_t* __restrict__ scol, float* __restrict__ sval,
                                                           uint32_t* __restrict__ rowcnt) {
     const int lane = threadIdx.x & 31;
-    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= n) return;
+    const int64_t i = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (i >= r1) return;
     const int nf = (int)dcnt[i];
     const uint32_t b0 = tstart[i];
     const int nb = (int)(tstart[i + 1] - b0);
@@ -543,20 +543,34 @@ __global__ void __launch_bounds__(256) merge_union_kernel(const uint32_t* __rest
     if (lane == 0) rowcnt[i] = (uint32_t)total;
 }
 
-// The writing pass: every merged run into its place in the CSR.
+// The writing pass of rows [r0, r1): every merged run into its place in the
+// CSR.  `rel` holds the range's row lengths scanned in place (rel[r0] = 0,
+// rel[r1] = the range's total); the range starts at *carry_in, the offset
+// past the earlier ranges, and the offset past this one goes to *carry_out
+// and indptr[r1].
 __global__ void __launch_bounds__(256) merge_place_kernel(const uint32_t* __restrict__ scol,
                                                           const float* __restrict__ sval,
-                                                          const uint32_t* __restrict__ tstart, int64_t n, int k,
-                                                          const uint32_t* __restrict__ indptr,
+                                                          const uint32_t* __restrict__ tstart, int64_t r0, int64_t r1,
+                                                          int k, const uint32_t* __restrict__ rel,
+                                                          const uint32_t* __restrict__ carry_in,
+                                                          uint32_t* __restrict__ carry_out, uint32_t* __restrict__ indptr,
                                                           uint32_t* __restrict__ out_cols, float* __restrict__ out_vals) {
     const int lane = threadIdx.x & 31;
-    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= n) return;
+    const int64_t i = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (i >= r1) return;
+    const uint32_t c0 = *carry_in;
     const int64_t run = i * k + tstart[i];
-    const uint32_t base = indptr[i], len = indptr[i + 1] - base;
+    const uint32_t base = c0 + rel[i], len = rel[i + 1] - rel[i];
     for (uint32_t j = lane; j < len; j += 32) {
         out_cols[base + j] = scol[run + j];
         out_vals[base + j] = sval[run + j];
+    }
+    if (lane == 0) {
+        indptr[i] = base;
+        if (i == r1 - 1) {
+            indptr[r1] = c0 + rel[r1];
+            *carry_out = c0 + rel[r1];
+        }
     }
 }
 
@@ -915,10 +929,14 @@ int32_t run_query_connectivities(scrust_context* ctx, const uint32_t* idx, const
 
 // The fuzzy union of a graph whose rows hold distinct ids, k <= 32: weights
 // with bucket places from one atomic per edge, the in-degree scan, the bucket
-// scatter, then a counting and a writing merge with one warp per row.  The
-// CSR is bit-identical to the radix-sort path's.
+// scatter, then per row range a merge with one warp per row into scratch
+// runs, the scan of the range's row lengths (in place) and the writing pass,
+// each range continuing the last one's offsets.  One range, or with `ranges`
+// ctx->csr_stream's kCsrRanges, each range's end recorded (and its end offset
+// sent to the host) for a download that overlaps the later ranges.  The CSR
+// is bit-identical to the radix-sort path's.
 int32_t run_connectivities_distinct(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n, int k,
-                                    CsrBuffers* out, scrust_status* st) {
+                                    CsrBuffers* out, scrust_status* st, bool ranges) {
     cudaError_t e = cudaSuccess;
     cudaStream_t s = ctx->stream;
     const int64_t E = n * (int64_t)k;
@@ -937,9 +955,14 @@ int32_t run_connectivities_distinct(scrust_context* ctx, const uint32_t* idx, co
     float* sig = (float*)a;
     float* rho = sig + n;
     uint32_t* indeg = (uint32_t*)(rho + n);  // n + 1, then the bucket starts in place
-    uint32_t* rowcnt = indeg + (n + 1);      // n + 1
+    uint32_t* rowcnt = indeg + (n + 1);      // n + 1: row lengths, scanned range by range in place
     uint32_t* dcnt = rowcnt + (n + 1);       // n (+1 spare)
-    if ((e = cudaMemsetAsync(indeg, 0, sizeof(uint32_t) * (size_t)(n + 1), s)) != cudaSuccess)
+    uint32_t* carry = dcnt + (n + 1);        // kCsrRanges + 1 offsets, in the 256 spare bytes
+    static_assert(sizeof(uint32_t) * (kCsrRanges + 1) <= 256, "range offsets fit the spare bytes");
+    const int R = ranges ? kCsrRanges : 1;
+    if ((e = cudaMemsetAsync(indeg, 0, sizeof(uint32_t) * (size_t)(n + 1), s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(carry, 0, sizeof(uint32_t), s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(rowcnt + n, 0, sizeof(uint32_t), s)) != cudaSuccess)
         return cuda_fail(st, e, "memset");
     if ((e = launch_smooth_knn(ctx, dist, n, k, sig, rho, false)) != cudaSuccess) return cuda_fail(st, e, "smooth_knn");
     if (k <= 16)
@@ -952,21 +975,42 @@ int32_t run_connectivities_distinct(scrust_context* ctx, const uint32_t* idx, co
     if ((e = device_exclusive_scan(ctx, indeg, indeg, n + 1, scan_scratch, scan_elems)) != cudaSuccess)
         return cuda_fail(st, e, "in-degree scan");
     bucket_scatter_kernel<<<(unsigned)((E + 255) / 256), 256, 0, s>>>(dcol, dw, dcnt, erank, indeg, n, k, tval);
-    const unsigned merge_blocks = (unsigned)((n * 32 + 255) / 256);
-    merge_union_kernel<<<merge_blocks, 256, 0, s>>>(dcol, dw, dcnt, tval, indeg, n, k, scol, sval, rowcnt);
-    if ((e = cudaMemsetAsync(rowcnt + n, 0, sizeof(uint32_t), s)) != cudaSuccess) return cuda_fail(st, e, "memset");
-    if ((e = device_exclusive_scan(ctx, rowcnt, out->indptr, n + 1, scan_scratch, scan_elems)) != cudaSuccess)
-        return cuda_fail(st, e, "row scan");
-    merge_place_kernel<<<merge_blocks, 256, 0, s>>>(scol, sval, indeg, n, k, out->indptr, out->indices, out->values);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "merge");
-    ctx->launches += 4;
+    ctx->launches += 2;
+    for (int r = 0; r < R; ++r) {
+        const int64_t r0 = n * r / R, r1 = n * (r + 1) / R;
+        if (r1 > r0) {
+            const unsigned blocks = (unsigned)(((r1 - r0) * 32 + 255) / 256);
+            merge_union_kernel<<<blocks, 256, 0, s>>>(dcol, dw, dcnt, tval, indeg, r0, r1, k, scol, sval, rowcnt);
+            // rowcnt[r1] is the next range's first row (or the zero past the
+            // last): it only receives the range's total.
+            if ((e = cudaGetLastError()) != cudaSuccess ||
+                (e = device_exclusive_scan(ctx, rowcnt + r0, rowcnt + r0, r1 - r0 + 1, scan_scratch, scan_elems)) !=
+                    cudaSuccess)
+                return cuda_fail(st, e, "row scan");
+            merge_place_kernel<<<blocks, 256, 0, s>>>(scol, sval, indeg, r0, r1, k, rowcnt, carry + r, carry + r + 1,
+                                                      out->indptr, out->indices, out->values);
+            ctx->launches += 2;
+        } else if ((e = cudaMemcpyAsync(carry + r + 1, carry + r, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s)) !=
+                   cudaSuccess) {
+            return cuda_fail(st, e, "merge");
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "merge");
+        if (ranges && ((e = cudaMemcpyAsync(ctx->csr_stream.h_bounds + r, carry + r + 1, sizeof(uint32_t),
+                                            cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+                       (e = cudaEventRecord(ctx->csr_stream.merged[r], s)) != cudaSuccess))
+            return cuda_fail(st, e, "merge");
+    }
+    if (n == 0 && (e = cudaMemsetAsync(out->indptr, 0, sizeof(uint32_t), s)) != cudaSuccess)
+        return cuda_fail(st, e, "memset");
     return ok(st);
 }
 
 int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n, int k,
-                           bool validate, CsrBuffers* out, scrust_status* st, bool distinct_rows) {
-    if (distinct_rows && !validate && k <= 32 && n < ((int64_t)1 << 31))
-        return run_connectivities_distinct(ctx, idx, dist, n, k, out, st);
+                           bool validate, CsrBuffers* out, scrust_status* st, bool distinct_rows, bool ranges,
+                           bool* streamed) {
+    const bool distinct = distinct_rows && !validate && k <= 32 && n < ((int64_t)1 << 31);
+    if (streamed) *streamed = distinct && ranges;
+    if (distinct) return run_connectivities_distinct(ctx, idx, dist, n, k, out, st, ranges);
     cudaError_t e = cudaSuccess;
     cudaStream_t s = ctx->stream;
     const int64_t E = n * (int64_t)k;

@@ -102,6 +102,17 @@ struct CsrBuffers {
     size_t nnz_cap = 0;
 };
 
+// A kNN graph's connectivities CSR downloaded while it is built: the fuzzy
+// union, its row scan and the placing of its rows run range by range
+// (kCsrRanges row ranges, each range's offsets continuing the last one's),
+// and each placed range goes down on the copy stream while the later ranges
+// merge.
+constexpr int kCsrRanges = 8;
+struct CsrStream {
+    cudaEvent_t merged[kCsrRanges] = {};  // on the main stream, after each range is placed
+    uint32_t* h_bounds = nullptr;         // pinned: the CSR offset past each range
+};
+
 }  // namespace scrust
 
 struct scrust_context {
@@ -111,6 +122,7 @@ struct scrust_context {
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // downloads that overlap later kernels on `stream`
     cudaEvent_t copy_ev = nullptr;
+    scrust::CsrStream csr_stream;        // the streamed download of kNN-graph connectivities
     std::mutex mu;
     scrust::Workspace ws;
     int* d_err = nullptr;          // scrust::DERR_COUNT ints
@@ -414,8 +426,12 @@ int32_t csr_download(scrust_context* ctx, const CsrBuffers& b, uint64_t rows, ui
 // The UMAP connectivities CSR of an n x k graph.  `distinct_rows`: every row's
 // ids are distinct (true of every kNN graph this library builds), which
 // allows the bucket transpose; graphs from callers take the stable radix sort.
+// `ranges`: run the union in ctx->csr_stream's row ranges and record its
+// events (the distinct-rows form only; returns whether it did through
+// *streamed).
 int32_t run_connectivities(scrust_context* ctx, const uint32_t* idx, const float* dist, int64_t n,
-                           int k, bool validate, CsrBuffers* out, scrust_status* st, bool distinct_rows = false);
+                           int k, bool validate, CsrBuffers* out, scrust_status* st, bool distinct_rows = false,
+                           bool ranges = false, bool* streamed = nullptr);
 // Rows of the directed fuzzy set of query rows against a reference (no
 // symmetrisation, no self to drop): sigma/rho per row as smooth_knn, then
 // exp weights, zero weights dropped, columns ascending, as a CSR of q rows.

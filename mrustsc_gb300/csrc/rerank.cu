@@ -568,23 +568,29 @@ __device__ int sorted_row_regs(const RerankArgs& a, int64_t slot, unsigned long 
     return 0;
 }
 
-__global__ void __launch_bounds__(RS_WARPS * 32, 6) rerank_sorted_kernel(RerankArgs a) {
+// Each block walks its own contiguous range of list rows, its warps on
+// consecutive rows: the rows an SM holds at once come from a few ranges, and
+// neighbouring rows' candidate rows (mostly the same cells) stay in its L1.
+__global__ void __launch_bounds__(RS_WARPS * 32, 6) rerank_sorted_kernel(RerankArgs a, int64_t span) {
     extern __shared__ unsigned long long rs_smem[];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     unsigned long long* keys = rs_smem + (size_t)warp * 2 * RS_KEYS;
     double* dbl = reinterpret_cast<double*>(keys + RS_KEYS);
     uint8_t* flags = reinterpret_cast<uint8_t*>(rs_smem + (size_t)RS_WARPS * 2 * RS_KEYS) + (size_t)warp * RS_KEYS;
-    const int64_t slot = (int64_t)blockIdx.x * RS_WARPS + warp;
-    if (slot >= a.nq || (a.qperm && a.qperm[slot] == 0xffffffffu)) return;  // padding of a batch layout
-    int r = sorted_row_regs(a, slot, keys, dbl);
-    if (r == 3) r = sorted_row<RS_KEYS>(a, slot, keys, dbl, flags);
-    if (r && lane == 0) {
-        if (r == 1) {
-            a.big_rows[atomicAdd(a.big_count, 1u)] = (uint32_t)slot;
-        } else {
-            push_fallback(a, slot);
+    const int64_t lo = (int64_t)blockIdx.x * span, hi = min(a.nq, lo + span);
+    for (int64_t slot = lo + warp; slot < hi; slot += RS_WARPS) {
+        if (a.qperm && a.qperm[slot] == 0xffffffffu) continue;  // padding of a batch layout
+        int r = sorted_row_regs(a, slot, keys, dbl);
+        if (r == 3) r = sorted_row<RS_KEYS>(a, slot, keys, dbl, flags);
+        if (r && lane == 0) {
+            if (r == 1) {
+                a.big_rows[atomicAdd(a.big_count, 1u)] = (uint32_t)slot;
+            } else {
+                push_fallback(a, slot);
+            }
         }
+        __syncwarp();
     }
 }
 
@@ -782,13 +788,17 @@ cudaError_t launch_rerank(scrust_context* ctx, const KnnPlan& plan, const float*
     if (e != cudaSuccess) return e;
     if (xs && theta) {
         const size_t smem_s = (size_t)RS_WARPS * (2 * RS_KEYS * sizeof(unsigned long long) + RS_KEYS);
-        const unsigned blocks = (unsigned)((plan.nq + RS_WARPS - 1) / RS_WARPS);
+        // As many blocks as stay resident (6 an SM), each over a contiguous
+        // range of rows.
+        const int64_t groups = (plan.nq + RS_WARPS - 1) / RS_WARPS;
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(groups, 6 * (int64_t)ctx->sm_count));
+        const int64_t span = (groups + blocks - 1) / blocks * RS_WARPS;
         // Most rows need no shared memory (the register path): leave the rest
         // of the SM's unified memory to L1, which caches the candidate rows
         // that neighbouring rows share.
         static_assert(RS_WARPS * (2 * RS_KEYS * 8 + RS_KEYS) <= 24 * 1024, "rerank block smem");
         if ((e = set_smem_carveout(ctx, (const void*)rerank_sorted_kernel, 50)) != cudaSuccess) return e;
-        rerank_sorted_kernel<<<blocks, RS_WARPS * 32, smem_s, ctx->stream>>>(a);
+        rerank_sorted_kernel<<<(unsigned)((plan.nq + span - 1) / span), RS_WARPS * 32, smem_s, ctx->stream>>>(a, span);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         const size_t smem_b = (size_t)RS_BIG_WARPS * (2 * RS_BIG_KEYS * sizeof(unsigned long long) + RS_BIG_KEYS);
         if ((e = set_smem_limit(ctx, (const void*)rerank_sorted_big_kernel, (int)smem_b)) != cudaSuccess) return e;
