@@ -44,9 +44,6 @@ sys.path.insert(0, str(ROOT))
 WORKLOAD = {"name": "knn_graph_1M_x50_k15", "n": 1_000_000, "d": 50, "k": 15, "clusters": 200,
             "dup_frac": 0.01, "seed": 0}
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
-# DRAM bytes (read + write) of the tensor sweep's launches in one step, from
-# an ncu capture of this workload (profiles/tensor_sweep_1M_x50_k15.md gives
-# the command); keyed by (cells, dims, k).
 # DRAM bytes of the sweep launches of one step at (n, d, k), from one ncu
 # capture of this bench's own workload (dram__bytes_read.sum +
 # dram__bytes_write.sum, a single-pass metric; profiles/tensor_sweep_1M_x50_k15.md):
