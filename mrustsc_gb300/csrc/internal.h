@@ -357,8 +357,8 @@ struct TileLists {
 // from the diagonal.  `resume`: lists and thresholds continue from an earlier
 // pass (counts in lists.cnt, thresholds in theta_io); theta_io, when given,
 // receives each list's threshold as its row block ends.  `argmin_out` (k = 1
-// only): no lists; per (row, column part) the smallest value and its column,
-// packed as float_key << 32 | column.
+// only): no lists; per (row, column part) the smallest value and the 8-column
+// group holding it, packed as float_key << 32 | (column / 8).
 cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, const void* A16, int64_t nq_pad,
                                      const void* B16, int64_t nr_pad, const float* bA, const float* bdelta,
                                      const float* beps2, const Lists& lists, bool bf16, const TileLists* tiles,

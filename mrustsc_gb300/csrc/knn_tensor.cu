@@ -354,6 +354,14 @@ __device__ __forceinline__ void sort4(float (&g)[4]) {
 }
 #undef SCRUST_CAS
 
+// Whether no column of the part's 128 columns from col0 is past the
+// reference rows or the row itself, for the whole warp (one vote per tile
+// instead of a column mask per chunk).
+__device__ __forceinline__ bool tile_clean(int64_t col0, int64_t row, const TensorArgs& a) {
+    const int64_t self_col = row + a.self_offset;
+    return !__any_sync(0xffffffffu, col0 + kPartCols > a.nr || (a.self && self_col >= col0 && self_col < col0 + kPartCols));
+}
+
 // Columns past the reference rows and the row itself become +inf, so that
 // no group minimum is taken over them (they occur in at most two chunks of
 // a work item: the warp branches once).
@@ -367,8 +375,8 @@ __device__ __forceinline__ void mask_chunk(uint32_t (&v)[32], int64_t colbase, i
 
 // The minima of a chunk's four 8-column groups.
 __device__ __forceinline__ void quarter_mins(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a,
-                                             float (&g)[4]) {
-    mask_chunk(v, colbase, row, a);
+                                             float (&g)[4], bool clean) {
+    if (!clean) mask_chunk(v, colbase, row, a);
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         const int b = 8 * q;
@@ -377,32 +385,31 @@ __device__ __forceinline__ void quarter_mins(uint32_t (&v)[32], int64_t colbase,
     }
 }
 
-// Nearest-column pass: every value of the chunk carries its column in the low
-// five bits of its f32 pattern (an error of under 32 ulp, which an
-// approximately nearest column tolerates), so one minimum tree yields both
-// the smallest value and its column, with no vote or branch per chunk.
-// Columns past the reference rows (and the row itself) become +inf before
-// the column goes in (+inf or NaN after it, which the minimum never takes).
-__device__ __forceinline__ void argmin_chunk(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a,
-                                             float& best_v, uint32_t& best_c) {
-    const uint32_t valid = chunk_valid(colbase, a.nr, a.self != 0, row + a.self_offset);
-    if (__any_sync(0xffffffffu, valid != 0xffffffffu)) {
+// Nearest-group pass: the minimum of each 8-column group of the chunk; the
+// lane keeps the smallest group minimum it has met and that group's index
+// (column / 8).  The row's nearest column is found among the group's eight
+// columns afterwards, which saves carrying a column with every value.
+// Columns past the reference rows (and the row itself) become +inf first.
+__device__ __forceinline__ void group_argmin_chunk(uint32_t (&v)[32], int64_t colbase, int64_t row,
+                                                   const TensorArgs& a, bool clean, float& best_v,
+                                                   uint32_t& best_g) {
+    if (!clean) mask_chunk(v, colbase, row, a);
 #pragma unroll
-        for (int j = 0; j < 32; j++) v[j] = ((valid >> j) & 1u) ? v[j] : 0x7f800000u;
-    }
-#pragma unroll
-    for (int j = 0; j < 32; j++) v[j] = (v[j] & ~31u) | (uint32_t)j;
-    const float m = min32(v);
-    if (m < best_v) {
-        best_v = m;
-        best_c = (uint32_t)colbase + (__float_as_uint(m) & 31u);
+    for (int q = 0; q < 4; q++) {
+        const int b = 8 * q;
+        const float g = min3f(min3f(f_of(v[b]), f_of(v[b + 1]), f_of(v[b + 2])),
+                              min3f(f_of(v[b + 3]), f_of(v[b + 4]), f_of(v[b + 5])), fminf(f_of(v[b + 6]), f_of(v[b + 7])));
+        if (g < best_v) {
+            best_v = g;
+            best_g = (uint32_t)(colbase >> 3) + (uint32_t)q;
+        }
     }
 }
 
 // The minima of a chunk's eight 4-column groups.
 __device__ __forceinline__ void eighth_mins(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a,
-                                            float (&g)[8]) {
-    mask_chunk(v, colbase, row, a);
+                                            float (&g)[8], bool clean) {
+    if (!clean) mask_chunk(v, colbase, row, a);
 #pragma unroll
     for (int q = 0; q < 8; q++)
         g[q] = fminf(min3f(f_of(v[4 * q]), f_of(v[4 * q + 1]), f_of(v[4 * q + 2])), f_of(v[4 * q + 3]));
@@ -410,8 +417,8 @@ __device__ __forceinline__ void eighth_mins(uint32_t (&v)[32], int64_t colbase, 
 
 // The minima of a chunk's two 16-column halves.
 __device__ __forceinline__ void half_mins(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a,
-                                          float& lo, float& hi) {
-    mask_chunk(v, colbase, row, a);
+                                          float& lo, float& hi, bool clean) {
+    if (!clean) mask_chunk(v, colbase, row, a);
     float m[12];
 #pragma unroll
     for (int h = 0; h < 2; h++) {
@@ -604,10 +611,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     tensor_candidates_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
                              TensorArgs a) {
     // PASS fixes the pass kind at compile time (1: thresholds only, 2:
-    // collect, 3: nearest column only, 0: taken from the arguments), so a
+    // collect for a self solve, 4: collect for query rows, 3: nearest column
+    // group only, 0: taken from the arguments), so a
     // specialised pass carries none of the others' code or registers.
     const bool thr_only = PASS == 1 || (PASS == 0 && a.thr_only);
-    const bool collect = PASS == 2 || (PASS == 0 && a.collect);
+    const bool collect = PASS == 2 || PASS == 4 || (PASS == 0 && a.collect);
     const bool argmin = PASS == 3 || (PASS == 0 && a.argmin_out != nullptr);
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -664,7 +672,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const int qt = w / csegs, seg = w % csegs;
                 const int ct0 = a.item_range ? (int)a.item_range[w].x : seg * a.tiles_per_seg;
                 const int ct1 = a.item_range ? (int)a.item_range[w].y : min(a.col_tiles, ct0 + a.tiles_per_seg);
-                const TileOrder<PASS == 2 || PASS == 0> order(a, w, qt, ct0, ct1);
+                const TileOrder<PASS == 2 || PASS == 4 || PASS == 0> order(a, w, qt, ct0, ct1);
                 if (order.count == 0) continue;
                 const uint32_t ab = ac & 1, au = ac >> 1;
                 if (!mbar_wait_bounded(&aempty[ab], (au & 1) ^ 1, a.err)) {
@@ -707,7 +715,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const int qt = w / csegs, seg = w % csegs;
                 const int ct0 = a.item_range ? (int)a.item_range[w].x : seg * a.tiles_per_seg;
                 const int ct1 = a.item_range ? (int)a.item_range[w].y : min(a.col_tiles, ct0 + a.tiles_per_seg);
-                const TileOrder<PASS == 2 || PASS == 0> order(a, w, qt, ct0, ct1);
+                const TileOrder<PASS == 2 || PASS == 4 || PASS == 0> order(a, w, qt, ct0, ct1);
                 if (order.count == 0) continue;
                 const uint32_t ab = ac & 1, au = ac >> 1;
                 if (!mbar_wait_bounded(&afull[ab], au & 1, a.err)) {
@@ -778,7 +786,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int qt = w / col_segs, seg = w % col_segs;
             const int ct0 = a.item_range ? (int)a.item_range[w].x : seg * a.tiles_per_seg;
             const int ct1 = a.item_range ? (int)a.item_range[w].y : min(a.col_tiles, ct0 + a.tiles_per_seg);
-            const TileOrder<PASS == 2 || PASS == 0> order(a, w, qt, ct0, ct1);
+            const TileOrder<PASS == 2 || PASS == 4 || PASS == 0> order(a, w, qt, ct0, ct1);
             if (order.count == 0) continue;
             const int64_t row = (int64_t)qt * ROWS + h * TBM + r_local;
             const bool valid = row < a.nq && (!a.row_map || a.row_map[row] != 0xffffffffu);
@@ -838,30 +846,38 @@ __global__ void __launch_bounds__(THREADS, 1)
                         for (int c = 0; c < 4; ++c) {
                             tmem_ld32(tbase + 32 * c, va);
                             tmem_ld_wait(va);
-                            uint32_t mask = below_mask(va, th);
-                            const int64_t cb = col0 + 32 * c;
-                            while (mask) {
-                                const int64_t col = cb + below_col(__ffs(mask) - 1);
-                                mask &= mask - 1;
-                                // Not past the reference rows, not the row itself.
-                                if (col < a.nr && !(a.self && col == row + a.self_offset))
-                                    ids[cnt++] = (uint32_t)col;  // ids only: no values
+                            // A self solve's rows collect among their own
+                            // cells, nearly every chunk holding some row's
+                            // candidate: the mask is formed at once (PASS 2).
+                            // Query rows meet many chunks with none: a
+                            // minimum tree and a vote skip those (PASS 4).
+                            if (PASS == 2 || __any_sync(0xffffffffu, min32(va) < th)) {
+                                uint32_t mask = below_mask(va, th);
+                                const int64_t cb = col0 + 32 * c;
+                                while (mask) {
+                                    const int64_t col = cb + below_col(__ffs(mask) - 1);
+                                    mask &= mask - 1;
+                                    // Not past the reference rows, not the row itself.
+                                    if (col < a.nr && !(a.self && col == row + a.self_offset))
+                                        ids[cnt++] = (uint32_t)col;  // ids only: no values
+                                }
                             }
                         }
                     } else if constexpr (PASS == 3) {
+                        const bool clean = tile_clean(col0, row, a);
                         uint32_t vb[32];
                         tmem_ld32(tbase, va);
                         tmem_ld_wait(va);
                         tmem_ld32(tbase + 32, vb);
-                        argmin_chunk(va, col0, row, a, top.v[0], best);
+                        group_argmin_chunk(va, col0, row, a, clean, top.v[0], best);
                         tmem_ld_wait(vb);
                         tmem_ld32(tbase + 64, va);
-                        argmin_chunk(vb, col0 + 32, row, a, top.v[0], best);
+                        group_argmin_chunk(vb, col0 + 32, row, a, clean, top.v[0], best);
                         tmem_ld_wait(va);
                         tmem_ld32(tbase + 96, vb);
-                        argmin_chunk(va, col0 + 64, row, a, top.v[0], best);
+                        group_argmin_chunk(va, col0 + 64, row, a, clean, top.v[0], best);
                         tmem_ld_wait(vb);
-                        argmin_chunk(vb, col0 + 96, row, a, top.v[0], best);
+                        group_argmin_chunk(vb, col0 + 96, row, a, clean, top.v[0], best);
                     } else if constexpr (TOPK == 16 && PASS == 1) {
                         // Threshold pass: each group of columns offers only
                         // its minimum.  The top-K then holds values of
@@ -872,6 +888,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                         // of an insertion per entrant.  Groups of 8 on an
                         // item's first tile (16 minima per lane: the K-th is
                         // finite after one tile), of 16 after it.
+                        const bool clean = false;  // (a vote per tile measured slower here than a mask per chunk)
                         const float kth0 = top.kth();
                         uint32_t vb[32];
                         if (it == 0) {
@@ -880,7 +897,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                 float q[4];
                                 tmem_ld32(tbase + 32 * c, va);
                                 tmem_ld_wait(va);
-                                quarter_mins(va, col0 + 32 * c, row, a, q);
+                                quarter_mins(va, col0 + 32 * c, row, a, q, clean);
                                 cm[c] = fminf(fminf(q[0], q[1]), fminf(q[2], q[3]));
                                 if (__any_sync(0xffffffffu, cm[c] < fminf(top.kth(), th))) {
                                     sort4(q);
@@ -893,15 +910,15 @@ __global__ void __launch_bounds__(THREADS, 1)
                             tmem_ld32(tbase, va);
                             tmem_ld_wait(va);
                             tmem_ld32(tbase + 32, vb);
-                            half_mins(va, col0, row, a, g[0], g[1]);
+                            half_mins(va, col0, row, a, g[0], g[1], clean);
                             tmem_ld_wait(vb);
                             tmem_ld32(tbase + 64, va);
-                            half_mins(vb, col0 + 32, row, a, g[2], g[3]);
+                            half_mins(vb, col0 + 32, row, a, g[2], g[3], clean);
                             tmem_ld_wait(va);
                             tmem_ld32(tbase + 96, vb);
-                            half_mins(va, col0 + 64, row, a, g[4], g[5]);
+                            half_mins(va, col0 + 64, row, a, g[4], g[5], clean);
                             tmem_ld_wait(vb);
-                            half_mins(vb, col0 + 96, row, a, g[6], g[7]);
+                            half_mins(vb, col0 + 96, row, a, g[6], g[7], clean);
 #pragma unroll
                             for (int c = 0; c < 4; ++c) cm[c] = fminf(g[2 * c], g[2 * c + 1]);
                             const float lim = fminf(top.kth(), th);
@@ -928,6 +945,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                         // first tile (32 minima per lane), of 16 after it; one
                         // chunk in flight (a top-32 leaves no registers for
                         // two).
+                        const bool clean = false;  // (a vote per tile measured slower here than a mask per chunk)
                         const float kth0 = top.kth();
                         if (it == 0) {
 #pragma unroll 1
@@ -935,7 +953,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                 float q[8];
                                 tmem_ld32(tbase + 32 * c, va);
                                 tmem_ld_wait(va);
-                                eighth_mins(va, col0 + 32 * c, row, a, q);
+                                eighth_mins(va, col0 + 32 * c, row, a, q, clean);
                                 cm[c] = fminf(fminf(fminf(q[0], q[1]), fminf(q[2], q[3])),
                                               fminf(fminf(q[4], q[5]), fminf(q[6], q[7])));
                                 if (__any_sync(0xffffffffu, cm[c] < fminf(top.kth(), th))) {
@@ -950,7 +968,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             for (int c = 0; c < 4; ++c) {
                                 tmem_ld32(tbase + 32 * c, va);
                                 tmem_ld_wait(va);
-                                half_mins(va, col0 + 32 * c, row, a, g[2 * c], g[2 * c + 1]);
+                                half_mins(va, col0 + 32 * c, row, a, g[2 * c], g[2 * c + 1], clean);
                                 cm[c] = fminf(g[2 * c], g[2 * c + 1]);
                             }
                             const float tmin = fminf(fminf(cm[0], cm[1]), fminf(cm[2], cm[3]));
@@ -1374,10 +1392,10 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     }
     auto kern = width == 1    ? (argmin_out ? tensor_candidates_kernel<1, 3> : tensor_candidates_kernel<1, 0>)
                 : width == 16 ? (a.thr_only ? tensor_candidates_kernel<16, 1>
-                                 : a.collect ? tensor_candidates_kernel<16, 2>
+                                 : a.collect ? (a.self ? tensor_candidates_kernel<16, 2> : tensor_candidates_kernel<16, 4>)
                                              : tensor_candidates_kernel<16, 0>)
                 : width == 32 ? (a.thr_only ? tensor_candidates_kernel<32, 1>
-                                 : a.collect ? tensor_candidates_kernel<32, 2>
+                                 : a.collect ? (a.self ? tensor_candidates_kernel<32, 2> : tensor_candidates_kernel<32, 4>)
                                              : tensor_candidates_kernel<32, 0>)
                               : tensor_candidates_kernel<0, 0>;
     cudaError_t e = set_smem_limit(ctx, (const void*)kern, (int)SMEM_BYTES);

@@ -23,6 +23,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 #include "internal.h"
@@ -135,18 +136,24 @@ __global__ void __launch_bounds__(128) anchor_top_kernel(const float* __restrict
 // then mostly neighbours, so a 256-row block rarely mixes far-apart cells.
 // The block stages the first kChainNb neighbours of every anchor (16-bit
 // ids) in shared memory, many loads in flight; then one thread walks, since
-// every step depends on the one before: its neighbour ids and their visited
-// bits are independent shared loads issued together, and no warp vote stands
-// between steps.  rank[a] is anchor a's place.
+// every step depends on the one before.  A step is kept short: the
+// neighbour ids and their visited bytes are independent shared loads issued
+// together, the first unvisited one is found from a mask of the twelve tests
+// (no chain of selects), and marking an anchor visited is a single byte
+// store.  rank[a] is anchor a's place.
 constexpr int kChainNb = 12;
 constexpr int kChainThreads = 1024;
 __global__ void __launch_bounds__(kChainThreads) anchor_chain_kernel(const uint32_t* __restrict__ nb, int m,
                                                                      uint32_t* __restrict__ rank) {
     extern __shared__ uint32_t ch_smem[];
-    uint32_t* visited = ch_smem;                                           // (m + 31) / 32 words
-    uint16_t* nbs = reinterpret_cast<uint16_t*>(ch_smem + ((m + 31) / 32 + 1) / 2 * 2);  // m * kChainNb, 8-byte aligned
-    const int words = (m + 31) / 32;
-    for (int i = threadIdx.x; i < words; i += blockDim.x) visited[i] = 0u;
+    const int words = (m + 3) / 4 + 1;                      // visited bytes, then one full word past them
+    uint8_t* vis = reinterpret_cast<uint8_t*>(ch_smem);     // m bytes (+ padding), 1 = visited
+    uint16_t* nbs = reinterpret_cast<uint16_t*>(ch_smem + (words + 1) / 2 * 2);  // m * kChainNb, 8-byte aligned
+    for (int i = threadIdx.x; i < words; i += blockDim.x) ch_smem[i] = 0u;
+    __syncthreads();
+    // Bytes past m read as visited, so neither the tests nor the scan for
+    // the lowest unvisited anchor ever pick one.
+    for (int i = m + threadIdx.x; i < 4 * words; i += blockDim.x) vis[i] = 1;
     for (int a = threadIdx.x; a < m; a += blockDim.x) {
         const uint4* src = reinterpret_cast<const uint4*>(nb + (int64_t)a * kAnchorNeighbours);
         uint32_t c[kChainNb];
@@ -158,50 +165,52 @@ __global__ void __launch_bounds__(kChainThreads) anchor_chain_kernel(const uint3
             c[4 * q + 2] = w.z;
             c[4 * q + 3] = w.w;
         }
+        // Missing neighbours point past m (a visited byte).
 #pragma unroll
         for (int j = 0; j < kChainNb; ++j)
-            nbs[(int64_t)a * kChainNb + j] = c[j] < (uint32_t)m ? (uint16_t)c[j] : (uint16_t)0xffffu;
+            nbs[(int64_t)a * kChainNb + j] = c[j] < (uint32_t)m ? (uint16_t)c[j] : (uint16_t)m;
     }
     __syncthreads();
     if (threadIdx.x != 0) return;
-    visited[0] = 1u;
+    vis[0] = 1;
     rank[0] = 0;
+    const uint32_t* vis4 = ch_smem;
     int cur = 0, scan = 0, pos = 1;
     for (; pos < m; ++pos) {
-        // The 12 neighbour ids of cur as three 8-byte words.
+        // The 12 neighbour ids of cur as six 32-bit words (two ids each).
         const uint2* row = reinterpret_cast<const uint2*>(nbs + (size_t)cur * kChainNb);
-        uint32_t c[kChainNb];
+        const uint2 r0 = row[0], r1 = row[1], r2 = row[2];
+        const uint32_t w[6] = {r0.x, r0.y, r1.x, r1.y, r2.x, r2.y};
+        uint32_t free = 0;
 #pragma unroll
-        for (int q = 0; q < kChainNb / 4; ++q) {
-            const uint2 w = row[q];
-            c[4 * q] = w.x & 0xffffu;
-            c[4 * q + 1] = w.x >> 16;
-            c[4 * q + 2] = w.y & 0xffffu;
-            c[4 * q + 3] = w.y >> 16;
+        for (int j = 0; j < kChainNb; ++j) {
+            const uint32_t c = (w[j >> 1] >> (16 * (j & 1))) & 0xffffu;
+            free |= vis[c] ? 0u : (1u << j);
         }
-        uint32_t word[kChainNb];
-#pragma unroll
-        for (int j = 0; j < kChainNb; ++j) word[j] = c[j] < (uint32_t)m ? visited[c[j] >> 5] : ~0u;
-        int next = -1;
-#pragma unroll
-        for (int j = kChainNb - 1; j >= 0; --j)
-            if (c[j] < (uint32_t)m && !((word[j] >> (c[j] & 31u)) & 1u)) next = (int)c[j];
-        if (next < 0) {
-            // The lowest unvisited anchor (words below `scan` are full).
-            while (scan < words && visited[scan] == ~0u) ++scan;
+        int next;
+        if (free) {
+            const int j = __ffs(free) - 1;
+            const uint32_t wj = (j >> 2) == 0 ? ((j & 2) ? w[1] : w[0]) : (j >> 2) == 1 ? ((j & 2) ? w[3] : w[2])
+                                                                                       : ((j & 2) ? w[5] : w[4]);
+            next = (int)((wj >> (16 * (j & 1))) & 0xffffu);
+        } else {
+            // The lowest unvisited anchor (words below `scan` are all visited).
+            while (scan < words && vis4[scan] == 0x01010101u) ++scan;
             if (scan >= words) break;  // cannot happen: an unvisited anchor exists while pos < m
-            const uint32_t free = ~visited[scan];
-            next = scan * 32 + __ffs(free) - 1;
-            if (next >= m) break;      // cannot happen: an unvisited anchor below m comes first
+            const uint32_t v = vis4[scan];
+            int b = 0;
+            while (b < 3 && ((v >> (8 * b)) & 0xffu)) ++b;
+            next = 4 * scan + b;
+            if (next >= m) break;      // cannot happen: bytes past m are marked visited
         }
-        visited[next >> 5] |= 1u << (next & 31);
+        vis[next] = 1;
         rank[next] = (uint32_t)pos;
         cur = next;
     }
     // Every anchor gets a rank whatever happened above.
     for (int a = 0; a < m && pos < m; ++a)
-        if (!((visited[a >> 5] >> (a & 31)) & 1u)) {
-            visited[a >> 5] |= 1u << (a & 31);
+        if (!vis[a]) {
+            vis[a] = 1;
             rank[a] = (uint32_t)pos++;
         }
 }
@@ -217,18 +226,64 @@ __global__ void relabel_neighbours_kernel(const uint32_t* __restrict__ nb, const
     out[(int64_t)rank[a] * kAnchorNeighbours + j] = c < (uint32_t)m ? rank[c] : 0xffffffffu;
 }
 
-// Per row, the nearer of its two column parts' nearest anchors (an
-// approximately nearest anchor, which is all an ordering needs), as the
-// anchor's walk rank, with the row as payload.
+// Each row's nearest anchor from the nearest-group pass: the better of its
+// two parts' groups, then, with eight lanes per row, the eight anchors of
+// that group measured on the same 16-bit operands (a row's [a, 1, 1, 1] times
+// an anchor's [-2b, three norm parts], summed in f32 over the `words`
+// 16-byte words that hold them) and the smallest taken (ties to the lower
+// anchor): an approximately nearest anchor, which is all an ordering needs.
+// keys[i] receives the anchor (anchor_rank_kernel turns it into the sort
+// key once the walk is done), vals[i] the row.
+template <class T>
 __global__ void nearest_anchor_kernel(const unsigned long long* __restrict__ best, int64_t n, int64_t m,
-                                      const uint32_t* __restrict__ rank, uint32_t* __restrict__ keys,
-                                      unsigned long long* __restrict__ vals) {
+                                      const T* __restrict__ A, const T* __restrict__ B, int words,
+                                      uint32_t* __restrict__ keys, unsigned long long* __restrict__ vals) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t i = t >> 3;
+    const int j = (int)(t & 7);
+    const bool row_ok = i < n;
+    const uint32_t g = row_ok ? (uint32_t)min(best[2 * i], best[2 * i + 1]) : 0u;
+    const int64_t col = (int64_t)g * 8 + j;
+    float v = __int_as_float(0x7f800000);
+    if (row_ok && col < m) {
+        const uint4* a4 = reinterpret_cast<const uint4*>(A + i * 64);
+        const uint4* b4 = reinterpret_cast<const uint4*>(B + col * 64);
+        float acc = 0.f;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) {
+            if (w >= words) break;
+            const uint4 x = __ldg(a4 + w), y = __ldg(b4 + w);
+            const uint32_t xs[4] = {x.x, x.y, x.z, x.w}, ys[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                float2 p, q;
+                if constexpr (std::is_same<T, __nv_bfloat16>::value) {
+                    p = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&xs[h]));
+                    q = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&ys[h]));
+                } else {
+                    p = __half22float2(*reinterpret_cast<const __half2*>(&xs[h]));
+                    q = __half22float2(*reinterpret_cast<const __half2*>(&ys[h]));
+                }
+                acc = fmaf(p.x, q.x, acc);
+                acc = fmaf(p.y, q.y, acc);
+            }
+        }
+        v = acc;
+    }
+    unsigned long long key = ((unsigned long long)float_key(v) << 32) | (uint32_t)j;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) key = min(key, __shfl_xor_sync(0xffffffffu, key, o));
+    if (row_ok && j == 0) {
+        const int64_t arg = (int64_t)g * 8 + (int64_t)(key & 7u);
+        keys[i] = (uint32_t)(arg < m ? arg : m - 1);
+        vals[i] = (unsigned long long)i;
+    }
+}
+
+// keys[i] = rank[keys[i]]: each row's anchor becomes the anchor's walk rank.
+__global__ void anchor_rank_kernel(uint32_t* __restrict__ keys, int64_t n, const uint32_t* __restrict__ rank) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const unsigned long long b = min(best[2 * i], best[2 * i + 1]);
-    const uint32_t arg = (uint32_t)b;
-    keys[i] = rank[arg < (uint32_t)m ? arg : (uint32_t)(m - 1)];
-    vals[i] = (unsigned long long)i;
+    if (i < n) keys[i] = rank[keys[i]];
 }
 
 __global__ void unpack_perm_kernel(const uint32_t* __restrict__ skeys, const unsigned long long* __restrict__ svals,
@@ -892,7 +947,7 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     // The anchor neighbourhoods and the walk that orders the cells run on the
     // copy stream beside the operands and the rows x anchors pass below; the
     // main stream waits for them before the cells are formed.
-    const size_t chain_smem = 4 * (size_t)(((m + 31) / 32 + 1) / 2 * 2) + 2 * (size_t)m * kChainNb;
+    const size_t chain_smem = 4 * (size_t)((((m + 3) / 4 + 1) + 1) / 2 * 2) + 2 * (size_t)m * kChainNb;
     if ((e = set_smem_limit(ctx, (const void*)anchor_chain_kernel, (int)chain_smem)) != cudaSuccess ||
         (e = cudaEventRecord(ctx->copy_ev, s)) != cudaSuccess ||
         (e = cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev, 0)) != cudaSuccess)
@@ -943,12 +998,21 @@ int32_t build_row_order(scrust_context* ctx, const float* x, int64_t n, int d, c
     px.max_ctas = ctx->sm_count - 1;
     unsigned long long* best = (unsigned long long*)(base + o_best);
     if ((e = launch_tensor_candidates(ctx, px, A0, n_pad, base + o_aB, m_pad, bA0, bdelta, beps2, lx, bf16, nullptr,
-                                      false, nullptr, nullptr, nullptr, best)) != cudaSuccess ||
-        (e = cudaStreamWaitEvent(s, ctx->copy_ev, 0)) != cudaSuccess)
+                                      false, nullptr, nullptr, nullptr, best)) != cudaSuccess)
         return cuda_fail(st, e, "ordering: anchor candidates");
-    nearest_anchor_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(best, n, m, rank, keysA, valsA);
+    const int op_words = (d + 3 + 7) / 8;  // 16-byte words of an operand row holding values
+    if (bf16)
+        nearest_anchor_kernel<__nv_bfloat16><<<(unsigned)((n * 8 + 255) / 256), 256, 0, s>>>(
+            best, n, m, (const __nv_bfloat16*)A0, (const __nv_bfloat16*)(base + o_aB), op_words, keysA, valsA);
+    else
+        nearest_anchor_kernel<__half><<<(unsigned)((n * 8 + 255) / 256), 256, 0, s>>>(
+            best, n, m, (const __half*)A0, (const __half*)(base + o_aB), op_words, keysA, valsA);
+    // The walk ranks (copy stream) are needed from here on.
+    if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaStreamWaitEvent(s, ctx->copy_ev, 0)) != cudaSuccess)
+        return cuda_fail(st, e, "ordering: nearest anchor");
+    anchor_rank_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(keysA, n, rank);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "ordering: nearest anchor");
-    ctx->launches += 2;
+    ctx->launches += 3;
 
     // Stable sort of the rows by anchor: the permutation and the cells.
     int bits = 1;
@@ -1305,11 +1369,18 @@ int32_t cross_ordered_enqueue(scrust_context* ctx, const AtlasOrder& at, const f
     if ((e = launch_tensor_candidates(ctx, px, base + o_A0, q_pad, at.anchor_B16, at.anchors_pad, bA0, eps0, eps0, lx,
                                       bf16, nullptr, false, nullptr, nullptr, nullptr, best)) != cudaSuccess)
         return cuda_fail(st, e, "query routing: nearest anchor");
-    nearest_anchor_kernel<<<(unsigned)((q + 255) / 256), 256, 0, s>>>(best, q, at.anchors, at.anchor_rank,
-                                                                     (uint32_t*)(base + o_kA),
-                                                                     (unsigned long long*)(base + o_vA));
+    const int op_words = (d + 3 + 7) / 8;  // 16-byte words of an operand row holding values
+    if (bf16)
+        nearest_anchor_kernel<__nv_bfloat16><<<(unsigned)((q * 8 + 255) / 256), 256, 0, s>>>(
+            best, q, at.anchors, (const __nv_bfloat16*)(base + o_A0), (const __nv_bfloat16*)at.anchor_B16, op_words,
+            (uint32_t*)(base + o_kA), (unsigned long long*)(base + o_vA));
+    else
+        nearest_anchor_kernel<__half><<<(unsigned)((q * 8 + 255) / 256), 256, 0, s>>>(
+            best, q, at.anchors, (const __half*)(base + o_A0), (const __half*)at.anchor_B16, op_words,
+            (uint32_t*)(base + o_kA), (unsigned long long*)(base + o_vA));
+    anchor_rank_kernel<<<(unsigned)((q + 255) / 256), 256, 0, s>>>((uint32_t*)(base + o_kA), q, at.anchor_rank);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(st, e, "query routing: nearest anchor");
-    ctx->launches += 3;
+    ctx->launches += 4;
     // The queries sorted by the walk place of their cell; their operands,
     // bounds and rows in that order.
     int bits = 1;
