@@ -227,55 +227,69 @@ __global__ void relabel_neighbours_kernel(const uint32_t* __restrict__ nb, const
 }
 
 // Each row's nearest anchor from the nearest-group pass: the better of its
-// two parts' groups, then, with eight lanes per row, the eight anchors of
-// that group measured on the same 16-bit operands (a row's [a, 1, 1, 1] times
-// an anchor's [-2b, three norm parts], summed in f32 over the `words`
-// 16-byte words that hold them) and the smallest taken (ties to the lower
-// anchor): an approximately nearest anchor, which is all an ordering needs.
-// keys[i] receives the anchor (anchor_rank_kernel turns it into the sort
-// key once the walk is done), vals[i] the row.
+// two parts' groups, then the group's eight anchors measured on the same
+// 16-bit operands (a row's [a, 1, 1, 1] times an anchor's [-2b, three norm
+// parts], summed in f32 over the `words` 16-byte words that hold them) and
+// the smallest taken (ties to the lower anchor): an approximately nearest
+// anchor, which is all an ordering needs.  Eight lanes per row, lane l
+// holding word l of the row and of each of the eight anchors, so that every
+// load of an anchor row is one contiguous line for the eight lanes; the
+// partial sums meet by shuffles.  keys[i] receives the anchor
+// (anchor_rank_kernel turns it into the sort key once the walk is done),
+// vals[i] the row.
+template <class T>
+__device__ __forceinline__ float dot_word(uint4 x, uint4 y) {
+    const uint32_t xs[4] = {x.x, x.y, x.z, x.w}, ys[4] = {y.x, y.y, y.z, y.w};
+    float acc = 0.f;
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        float2 p, q;
+        if constexpr (std::is_same<T, __nv_bfloat16>::value) {
+            p = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&xs[h]));
+            q = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&ys[h]));
+        } else {
+            p = __half22float2(*reinterpret_cast<const __half2*>(&xs[h]));
+            q = __half22float2(*reinterpret_cast<const __half2*>(&ys[h]));
+        }
+        acc = fmaf(p.x, q.x, acc);
+        acc = fmaf(p.y, q.y, acc);
+    }
+    return acc;
+}
+
 template <class T>
 __global__ void nearest_anchor_kernel(const unsigned long long* __restrict__ best, int64_t n, int64_t m,
                                       const T* __restrict__ A, const T* __restrict__ B, int words,
                                       uint32_t* __restrict__ keys, unsigned long long* __restrict__ vals) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t i = t >> 3;
-    const int j = (int)(t & 7);
+    const int l = (int)(t & 7);
     const bool row_ok = i < n;
     const uint32_t g = row_ok ? (uint32_t)min(best[2 * i], best[2 * i + 1]) : 0u;
-    const int64_t col = (int64_t)g * 8 + j;
-    float v = __int_as_float(0x7f800000);
-    if (row_ok && col < m) {
-        const uint4* a4 = reinterpret_cast<const uint4*>(A + i * 64);
-        const uint4* b4 = reinterpret_cast<const uint4*>(B + col * 64);
-        float acc = 0.f;
+    const int64_t c0 = (int64_t)g * 8;
+    float part[8];
+    const bool lane_ok = row_ok && l < words;
+    const uint4 x = lane_ok ? __ldg(reinterpret_cast<const uint4*>(A + i * 64) + l) : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
-        for (int w = 0; w < 8; ++w) {
-            if (w >= words) break;
-            const uint4 x = __ldg(a4 + w), y = __ldg(b4 + w);
-            const uint32_t xs[4] = {x.x, x.y, x.z, x.w}, ys[4] = {y.x, y.y, y.z, y.w};
-#pragma unroll
-            for (int h = 0; h < 4; ++h) {
-                float2 p, q;
-                if constexpr (std::is_same<T, __nv_bfloat16>::value) {
-                    p = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&xs[h]));
-                    q = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&ys[h]));
-                } else {
-                    p = __half22float2(*reinterpret_cast<const __half2*>(&xs[h]));
-                    q = __half22float2(*reinterpret_cast<const __half2*>(&ys[h]));
-                }
-                acc = fmaf(p.x, q.x, acc);
-                acc = fmaf(p.y, q.y, acc);
-            }
-        }
-        v = acc;
+    for (int a = 0; a < 8; ++a) {
+        part[a] = 0.f;
+        if (lane_ok && c0 + a < m) part[a] = dot_word<T>(x, __ldg(reinterpret_cast<const uint4*>(B + (c0 + a) * 64) + l));
     }
-    unsigned long long key = ((unsigned long long)float_key(v) << 32) | (uint32_t)j;
 #pragma unroll
-    for (int o = 1; o < 8; o <<= 1) key = min(key, __shfl_xor_sync(0xffffffffu, key, o));
-    if (row_ok && j == 0) {
-        const int64_t arg = (int64_t)g * 8 + (int64_t)(key & 7u);
-        keys[i] = (uint32_t)(arg < m ? arg : m - 1);
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) part[a] += __shfl_xor_sync(0xffffffffu, part[a], o);
+    if (row_ok && l == 0) {
+        int arg = 0;
+        float bv = c0 < m ? part[0] : __int_as_float(0x7f800000);
+#pragma unroll
+        for (int a = 1; a < 8; ++a)
+            if (c0 + a < m && part[a] < bv) {
+                bv = part[a];
+                arg = a;
+            }
+        const int64_t col = c0 + arg;
+        keys[i] = (uint32_t)(col < m ? col : m - 1);
         vals[i] = (unsigned long long)i;
     }
 }
