@@ -56,6 +56,7 @@ enum Slot : int {
     SLOT_BATCH_TABLE,   // batch sample table
     SLOT_THETA,         // list thresholds of an unordered tensor-form solve
     SLOT_ROWTHETA,      // per-row shared thresholds across column segments
+    SLOT_TOPK,          // a threshold pass's register top-K per list
     SLOT_RERANK_BIG,    // rows for the rerank's second sorted pass
     SLOT_QTERMS,        // per-query-row bound terms of a query-versus-reference solve
     SLOT_QSCRATCH,      // scratch operands of a query-versus-reference solve
@@ -363,7 +364,14 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
                                      const void* B16, int64_t nr_pad, const float* bA, const float* bdelta,
                                      const float* beps2, const Lists& lists, bool bf16, const TileLists* tiles,
                                      bool resume, float* theta_io, int* grid_out, unsigned long long* stats,
-                                     unsigned long long* argmin_out = nullptr, int pass_mode = 0);
+                                     unsigned long long* argmin_out = nullptr, int pass_mode = 0,
+                                     float* topk_out = nullptr);
+// After a threshold pass that wrote its register top-K per list (topk_out,
+// one column segment): each row's threshold from the k-th of both column
+// parts' lists together, into both of its theta slots (knn_tensor.cu).
+cudaError_t launch_merge_part_thresholds(const float* topk, int width, int64_t n, int64_t n_pad, int k,
+                                         const float* bA, const float* bdelta, const float* beps2, float* theta,
+                                         cudaStream_t s);
 // Pass modes of launch_tensor_candidates (k <= 32, one column segment):
 // thresholds only (register top-k, theta_io written, lists untouched), then
 // collection at the fixed thresholds (appends only).

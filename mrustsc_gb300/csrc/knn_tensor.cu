@@ -108,6 +108,10 @@ struct TensorArgs {
     // smaller of each row's theta_io entries and the pass only appends.
     int thr_only, collect;
     float* theta_io;            // per list: the threshold when the item ends (read when resuming)
+    float* topk_out;            // threshold passes: per list, the register top-K when the item ends
+                                // (ascending, the first K - k slots -inf; slot t of list l at
+                                // t * topk_stride + l, so a warp's stores are contiguous), or null
+    int64_t topk_stride;        // lists in all
 };
 
 // Counters gathered when statistics are on (summed over all CTAs).
@@ -1090,6 +1094,12 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (valid && ok) {
                 if (!thr_only) a.lists.cnt[lslot] = min(cnt, (uint32_t)a.lists.ctot);
                 if (a.theta_io && !collect) a.theta_io[lslot] = th;
+                if constexpr (TOPK > 1) {
+                    if (thr_only && a.topk_out) {
+#pragma unroll
+                        for (int t = 0; t < TOPK; ++t) a.topk_out[t * a.topk_stride + lslot] = top.v[t];
+                    }
+                }
             }
         }
         if (a.stats) {
@@ -1310,7 +1320,7 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
                                      const void* B16, int64_t nr_pad, const float* bA, const float* bdelta,
                                      const float* beps2, const Lists& lists, bool bf16, const TileLists* tiles,
                                      bool resume, float* theta_io, int* grid_out, unsigned long long* stats,
-                                     unsigned long long* argmin_out, int pass_mode) {
+                                     unsigned long long* argmin_out, int pass_mode, float* topk_out) {
     if (nq_pad % ROWS || nr_pad % TBN) return cudaErrorInvalidValue;
     CUtensorMap ta, tb;
     const CUtensorMapDataType dt = bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
@@ -1379,6 +1389,9 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     if ((a.thr_only || a.collect) && (!theta_io || plan.k > 32 || (lists.segments != PARTS && !a.row_theta)))
         return cudaErrorInvalidValue;
     a.argmin_out = argmin_out;
+    a.topk_out = topk_out;
+    a.topk_stride = nq_pad * lists.segments;
+    if (topk_out && (!a.thr_only || lists.segments != PARTS)) return cudaErrorInvalidValue;
     if (argmin_out && (plan.k != 1 || resume)) return cudaErrorInvalidValue;
     if (a.tl2 && !a.collect) return cudaErrorInvalidValue;  // a second list is read by collect passes only
     if (resume && !theta_io) return cudaErrorInvalidValue;
@@ -1403,6 +1416,53 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     const int grid = std::min(a.items, plan.max_ctas > 0 ? std::min(plan.max_ctas, ctx->sm_count) : ctx->sm_count);
     if (grid_out) *grid_out = grid;
     kern<<<grid, THREADS, SMEM_BYTES, ctx->stream>>>(ta, tb, a);
+    return cudaGetLastError();
+}
+
+// The threshold of each row from both column parts' register top-K of a
+// threshold pass (k <= K; each list ascending with its first K - k slots
+// -inf): the k-th smallest of the two lists' union, which lies at or below
+// each part's own k-th (a row's nearest columns fall in both halves of a
+// tile, so each part alone sees only some of them), bounded as the sweep
+// bounds a k-th, and never above either part's threshold.  Both of the
+// row's theta slots receive it.
+template <int K>
+__global__ void merge_part_thresholds_kernel(const float* __restrict__ topk, int64_t stride, int64_t n, int k,
+                                             const float* __restrict__ bA, const float* __restrict__ bdelta,
+                                             const float* __restrict__ beps2, float* __restrict__ theta) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* p0 = topk + (int64_t)(K - k) * stride + i * PARTS;
+    const float* p1 = p0 + 1;
+    int u = 0, v = 0;
+    float kth = __int_as_float(0x7f800000);
+    for (int t = 0; t < k; ++t) {
+        const float x = u < k ? p0[u * stride] : __int_as_float(0x7f800000);
+        const float y = v < k ? p1[v * stride] : __int_as_float(0x7f800000);
+        if (x <= y) {
+            kth = x;
+            ++u;
+        } else {
+            kth = y;
+            ++v;
+        }
+    }
+    const float t0 = theta[i * PARTS], t1 = theta[i * PARTS + 1];
+    const float th = fminf(fminf(t0, t1), TensorBound{bA[i], bdelta[i], beps2[i]}.theta_f32(kth));
+    theta[i * PARTS] = th;
+    theta[i * PARTS + 1] = th;
+}
+
+cudaError_t launch_merge_part_thresholds(const float* topk, int width, int64_t n, int64_t n_pad, int k,
+                                         const float* bA, const float* bdelta, const float* beps2, float* theta,
+                                         cudaStream_t s) {
+    if (k < 1 || k > width || (width != 16 && width != 32)) return cudaErrorInvalidValue;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    const int64_t stride = n_pad * PARTS;  // one column segment: PARTS lists a row
+    if (width == 16)
+        merge_part_thresholds_kernel<16><<<blocks, 256, 0, s>>>(topk, stride, n, k, bA, bdelta, beps2, theta);
+    else
+        merge_part_thresholds_kernel<32><<<blocks, 256, 0, s>>>(topk, stride, n, k, bA, bdelta, beps2, theta);
     return cudaGetLastError();
 }
 
