@@ -150,6 +150,17 @@ def test_neighbors_graph_in_one_pass(scrust, oracle):
     assert_same_csr(conn, oracle.connectivities(idx, dist))
 
 
+@pytest.mark.parametrize("n", [3, 7, 9, 17, 1031])
+def test_neighbors_graph_few_rows(scrust, oracle, n):
+    """Graphs of fewer rows than the host call's download ranges (some ranges
+    empty) and of row counts that split unevenly over them: the CSR the
+    ranges place and download is the restated one."""
+    x = synthetic.mixture(n, 12, clusters=2, dup_frac=0.0, seed=n)
+    k = min(15, n - 1)
+    idx, dist, conn = scrust.neighbors_graph(x, k)
+    assert_same_csr(conn, oracle.connectivities(idx, dist))
+
+
 def test_host_graphs_held_and_freed_out_of_order(scrust, oracle):
     """Several downloaded graphs alive at once, of growing and shrinking
     sizes, freed in another order than made: each handle keeps its own host
