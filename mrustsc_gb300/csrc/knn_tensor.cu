@@ -618,8 +618,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     // collect for a self solve, 4: collect for query rows, 3: nearest column
     // group only, 0: taken from the arguments), so a
     // specialised pass carries none of the others' code or registers.
-    const bool thr_only = PASS == 1 || (PASS == 0 && a.thr_only);
-    const bool collect = PASS == 2 || PASS == 4 || (PASS == 0 && a.collect);
+    // (A general pass with a register top-16 or top-32 never runs as a
+    // threshold or collect pass: those have their own kinds.  Only k = 1 and
+    // the top-k-free form take the pass kind from the arguments.)
+    const bool thr_only = PASS == 1 || (PASS == 0 && TOPK <= 1 && a.thr_only);
+    const bool collect = PASS == 2 || PASS == 4 || (PASS == 0 && TOPK <= 1 && a.collect);
     const bool argmin = PASS == 3 || (PASS == 0 && a.argmin_out != nullptr);
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
