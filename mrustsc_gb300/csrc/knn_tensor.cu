@@ -379,8 +379,8 @@ __device__ __forceinline__ void mask_chunk(uint32_t (&v)[32], int64_t colbase, i
 
 // The minima of a chunk's four 8-column groups.
 __device__ __forceinline__ void quarter_mins(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a,
-                                             float (&g)[4], bool clean) {
-    if (!clean) mask_chunk(v, colbase, row, a);
+                                             float (&g)[4]) {
+    mask_chunk(v, colbase, row, a);
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         const int b = 8 * q;
@@ -412,8 +412,8 @@ __device__ __forceinline__ void group_argmin_chunk(uint32_t (&v)[32], int64_t co
 
 // The minima of a chunk's eight 4-column groups.
 __device__ __forceinline__ void eighth_mins(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a,
-                                            float (&g)[8], bool clean) {
-    if (!clean) mask_chunk(v, colbase, row, a);
+                                            float (&g)[8]) {
+    mask_chunk(v, colbase, row, a);
 #pragma unroll
     for (int q = 0; q < 8; q++)
         g[q] = fminf(min3f(f_of(v[4 * q]), f_of(v[4 * q + 1]), f_of(v[4 * q + 2])), f_of(v[4 * q + 3]));
@@ -421,8 +421,8 @@ __device__ __forceinline__ void eighth_mins(uint32_t (&v)[32], int64_t colbase, 
 
 // The minima of a chunk's two 16-column halves.
 __device__ __forceinline__ void half_mins(uint32_t (&v)[32], int64_t colbase, int64_t row, const TensorArgs& a,
-                                          float& lo, float& hi, bool clean) {
-    if (!clean) mask_chunk(v, colbase, row, a);
+                                          float& lo, float& hi) {
+    mask_chunk(v, colbase, row, a);
     float m[12];
 #pragma unroll
     for (int h = 0; h < 2; h++) {
@@ -895,7 +895,6 @@ __global__ void __launch_bounds__(THREADS, 1)
                         // of an insertion per entrant.  Groups of 8 on an
                         // item's first tile (16 minima per lane: the K-th is
                         // finite after one tile), of 16 after it.
-                        const bool clean = false;  // (a vote per tile measured slower here than a mask per chunk)
                         const float kth0 = top.kth();
                         uint32_t vb[32];
                         if (it == 0) {
@@ -904,7 +903,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                 float q[4];
                                 tmem_ld32(tbase + 32 * c, va);
                                 tmem_ld_wait(va);
-                                quarter_mins(va, col0 + 32 * c, row, a, q, clean);
+                                quarter_mins(va, col0 + 32 * c, row, a, q);
                                 cm[c] = fminf(fminf(q[0], q[1]), fminf(q[2], q[3]));
                                 if (__any_sync(0xffffffffu, cm[c] < fminf(top.kth(), th))) {
                                     sort4(q);
@@ -917,15 +916,15 @@ __global__ void __launch_bounds__(THREADS, 1)
                             tmem_ld32(tbase, va);
                             tmem_ld_wait(va);
                             tmem_ld32(tbase + 32, vb);
-                            half_mins(va, col0, row, a, g[0], g[1], clean);
+                            half_mins(va, col0, row, a, g[0], g[1]);
                             tmem_ld_wait(vb);
                             tmem_ld32(tbase + 64, va);
-                            half_mins(vb, col0 + 32, row, a, g[2], g[3], clean);
+                            half_mins(vb, col0 + 32, row, a, g[2], g[3]);
                             tmem_ld_wait(va);
                             tmem_ld32(tbase + 96, vb);
-                            half_mins(va, col0 + 64, row, a, g[4], g[5], clean);
+                            half_mins(va, col0 + 64, row, a, g[4], g[5]);
                             tmem_ld_wait(vb);
-                            half_mins(vb, col0 + 96, row, a, g[6], g[7], clean);
+                            half_mins(vb, col0 + 96, row, a, g[6], g[7]);
 #pragma unroll
                             for (int c = 0; c < 4; ++c) cm[c] = fminf(g[2 * c], g[2 * c + 1]);
                             const float lim = fminf(top.kth(), th);
@@ -952,7 +951,6 @@ __global__ void __launch_bounds__(THREADS, 1)
                         // first tile (32 minima per lane), of 16 after it; one
                         // chunk in flight (a top-32 leaves no registers for
                         // two).
-                        const bool clean = false;  // (a vote per tile measured slower here than a mask per chunk)
                         const float kth0 = top.kth();
                         if (it == 0) {
 #pragma unroll 1
@@ -960,7 +958,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                 float q[8];
                                 tmem_ld32(tbase + 32 * c, va);
                                 tmem_ld_wait(va);
-                                eighth_mins(va, col0 + 32 * c, row, a, q, clean);
+                                eighth_mins(va, col0 + 32 * c, row, a, q);
                                 cm[c] = fminf(fminf(fminf(q[0], q[1]), fminf(q[2], q[3])),
                                               fminf(fminf(q[4], q[5]), fminf(q[6], q[7])));
                                 if (__any_sync(0xffffffffu, cm[c] < fminf(top.kth(), th))) {
@@ -975,7 +973,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             for (int c = 0; c < 4; ++c) {
                                 tmem_ld32(tbase + 32 * c, va);
                                 tmem_ld_wait(va);
-                                half_mins(va, col0 + 32 * c, row, a, g[2 * c], g[2 * c + 1], clean);
+                                half_mins(va, col0 + 32 * c, row, a, g[2 * c], g[2 * c + 1]);
                                 cm[c] = fminf(g[2 * c], g[2 * c + 1]);
                             }
                             const float tmin = fminf(fminf(cm[0], cm[1]), fminf(cm[2], cm[3]));
