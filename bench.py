@@ -47,8 +47,9 @@ PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 # DRAM bytes of the sweep launches of one step at (n, d, k), from one ncu
 # capture of this bench's own workload (dram__bytes_read.sum +
 # dram__bytes_write.sum, a single-pass metric; profiles/tensor_sweep_1M_x50_k15.md):
-# threshold pass 591.25 + 15.58 MB, collect pass 748.17 + 186.94 MB.
-SWEEP_TRAFFIC: dict = {(1_000_000, 50, 15): (591.25 + 15.58 + 748.17 + 186.94) * 1e6}
+# threshold pass 621.20 + 126.40 MB (its writes are the lists' register top-16),
+# collect pass 734.45 + 122.71 MB.
+SWEEP_TRAFFIC: dict = {(1_000_000, 50, 15): (621.20 + 126.40 + 734.45 + 122.71) * 1e6}
 SWEEP_TRAFFIC_NOTE = ("bytes, dram__bytes_read.sum + dram__bytes_write.sum summed over the step's two sweep "
                       "launches (threshold pass, collect pass), one ncu capture of this workload")
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
