@@ -392,22 +392,24 @@ int32_t knn_device_impl(scrust_context* ctx, const float* x, uint64_t n64, uint6
             const bool split = k <= 32;
             const int mode = split ? kPassThresholds : kPassFull;
             rerank_ids_only = split;
-            // The threshold pass leaves each list's register top-K, and each
+            // The threshold pass leaves each list's register top-K (a top-16
+            // or top-32: k >= 2; k = 1 keeps a single value a lane), and each
             // row's threshold is then taken from its two column parts'
             // lists together.
             const int width = k <= 16 ? 16 : 32;
+            const bool merge = split && k >= 2;
             float* topk = nullptr;
-            if (split) {
+            if (merge) {
                 topk = (float*)ws_get(ctx, SLOT_TOPK, sizeof(float) * (size_t)lists.segments * width * n_pad, &e);
                 if (!topk) return cuda_fail(st, e, "workspace");
             }
             if ((e = launch_tensor_candidates(ctx, plan, A16, n_pad, B16, n_pad, bA, bdelta, beps2, lists, bf16,
                                               &first, false, order.theta, nullptr, sweep_stats(ctx), nullptr, mode,
                                               topk)) != cudaSuccess ||
-                (split && (e = launch_merge_part_thresholds(topk, width, n, n_pad, (int)k, bA, bdelta, beps2,
+                (merge && (e = launch_merge_part_thresholds(topk, width, n, n_pad, (int)k, bA, bdelta, beps2,
                                                             order.theta, s)) != cudaSuccess))
                 return cuda_fail(st, e, "knn_candidates_tc");
-            ctx->launches += split ? 2 : 1;
+            ctx->launches += merge ? 2 : 1;
             mark(ctx, PH_PASS1);
             TileLists second;
             if ((rc = build_second_pass(ctx, A16, bf16, n, d, order, bA, bdelta, &second, st))) return rc;

@@ -1392,7 +1392,8 @@ cudaError_t launch_tensor_candidates(scrust_context* ctx, const KnnPlan& plan, c
     a.argmin_out = argmin_out;
     a.topk_out = topk_out;
     a.topk_stride = nq_pad * lists.segments;
-    if (topk_out && (!a.thr_only || lists.segments != PARTS)) return cudaErrorInvalidValue;
+    // (The top-K is written by the top-16 and top-32 threshold passes: k >= 2.)
+    if (topk_out && (!a.thr_only || lists.segments != PARTS || plan.k < 2)) return cudaErrorInvalidValue;
     if (argmin_out && (plan.k != 1 || resume)) return cudaErrorInvalidValue;
     if (a.tl2 && !a.collect) return cudaErrorInvalidValue;  // a second list is read by collect passes only
     if (resume && !theta_io) return cudaErrorInvalidValue;

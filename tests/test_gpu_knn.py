@@ -71,6 +71,17 @@ def test_random_embeddings_match_fp64(scrust, oracle, n, d, k, form):
     assert_exact(oracle, x, k, idx, dist)
 
 
+@pytest.mark.parametrize("k", [1, 2, 16, 17, 31, 32])
+def test_ordered_solves_every_top_k_width(scrust, oracle, k):
+    """Ordered tensor solves (3000 clustered cells) at the k that select each
+    threshold-pass kind: k = 1 (one value a lane), 2..16 (a register top-16
+    whose two column parts' lists are merged into each row's threshold) and
+    17..32 (top-32)."""
+    x = synthetic.mixture(3000, 20, clusters=6, dup_frac=0.01, seed=k)
+    idx, dist = scrust.knn(x, k, "auto", form="tensor", ordering="on")
+    assert_exact(oracle, x, k, idx, dist)
+
+
 @pytest.mark.parametrize(("n", "d", "k"), [(64, 8, 1), (100, 5, 7), (257, 3, 15), (300, 32, 16)])
 def test_reference_snap_equals_the_metal_twin(scrust, oracle, n, d, k):
     x = refdata.random_embedding(n, d, n)
